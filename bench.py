@@ -1,0 +1,395 @@
+"""Benchmark: LLG steps/s of the GSPM step on one GB300 (replicas across GPUs).
+
+Default workload: 128^3 hex with magnetoelastic coupling and the [111]
+rotation (plain FP64), the configuration the headline metric is quoted on.
+A "step" is one Gauss-Seidel-projection LLG step at the next field of the
+500-step sweep, with all operators and state resident in HBM.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--workload NAME]
+                  [--precision DP|IR] [--impl ours|reference]
+
+value:  steps/s over K steps timed with CUDA events (device-resident inputs;
+        operators of 18 GB > L2, so no flush is needed); max over ranks.
+e2e:    the same steps through the public API with the magnetisation copied in
+        from pinned host memory and the new m and <m> read back every step.
+roofline: the persistent CG kernel (dominant): algorithmic bytes per launch
+        (B_spmv + iterations * (B_spmv + 6 n s)) / measured launch time.
+cpu_baseline: the CPU oracle (NumPy/SciPy restatement of the reference's step)
+        sampled on this machine's host cores: one step with every CG capped at 3
+        iterations, timed per solve, extrapolated with this run's iteration counts.
+--impl reference: the same CPU sample as the whole measurement (the reference
+        itself needs CuPy + a CUDA GPU and is Python; its CPU path is the oracle).
+Multi-GPU: independent replicas (one per rank, no collective on the data path).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "LLG steps/s & SpMV HBM GB/s vs plain FP64 at |m| err<=1e-6; serving p50/p99"
+
+# CG iterations per solve of a warm-started 128^3 ME step (elasticity, demag,
+# g1n, g2n, g3n, g1*, g2*, m1**, m2**, m3**), measured on the GPU; used only to
+# extrapolate the CPU sample of --impl reference, which cannot afford the
+# full solves (a full CPU step takes tens of minutes).
+REFERENCE_ITERS = {"hex128_me": [200, 60, 12, 12, 12, 12, 12, 14, 14, 14],
+                   "hex32_plain": [60, 12, 12, 12, 12, 12, 14, 14, 14]}
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        self.rows = []
+        if self.proc is None:
+            return False
+        self.proc.terminate()
+        try:
+            out, _ = self.proc.communicate(timeout=5)
+        except Exception:
+            self.proc.kill()
+            out = ""
+        for line in out.splitlines():
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) >= 9:
+                self.rows.append(parts)
+        return False
+
+    def summary(self):
+        rows = getattr(self, "rows", [])
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+
+        def num(x):
+            try:
+                return float(x)
+            except ValueError:
+                return None
+        sm = [num(r[1]) for r in rows if num(r[1])]
+        mx = [num(r[2]) for r in rows if num(r[2])]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def spmv_bytes(A, nvec):
+    ip = A.indptr.element_size()
+    return A.nnz * (8 + 4) + (A.shape[0] + 1) * ip + nvec * (A.shape[1] * 8 + A.shape[0] * 8)
+
+
+def cg_launch_bytes(A, nvec, iters, warm):
+    n = A.shape[0]
+    per_it = spmv_bytes(A, nvec) + 6 * n * 8 * nvec
+    head = (spmv_bytes(A, nvec) + 3 * n * 8 * nvec) if warm else 2 * n * 8 * nvec
+    return head + iters * per_it
+
+
+# ------------------------------------------------------------------ CPU oracle sample
+def cpu_sample(p, S, iters_per_solve, cap=3):
+    """Time one oracle step at full size with every CG capped at `cap` iterations."""
+    import numpy as np
+    import oracle.cg as OC
+    import oracle.llg as OL
+    from oracle.volume_average import VolumeAverage as OVA
+    from cupymag_gb300.workloads import seeded_m0
+
+    ops = S.host_operators()
+    Avg = OVA(S.node_coords_np, S.elements_np, S.global_id_np)
+    m0 = seeded_m0(S.n_dof, S.DefDOF, seed=1234)
+    st = OL.LLGState(m0, Avg.average)
+    times = []
+    orig = OL.solve_cg
+
+    def capped(A, b, **kw):
+        t0 = time.perf_counter()
+        x, _ = OC.cg(A, b, x0=kw.get("x0") if kw.get("use_init") else None, tol=0.0, maxiter=cap)
+        times.append(time.perf_counter() - t0)
+        return x
+
+    OL.solve_cg = capped
+    try:
+        t0 = time.perf_counter()
+        OL.llg_step(st, ops, Avg.average, p, p.Hext, S.DefDOF)
+        t_step = time.perf_counter() - t0
+    finally:
+        OL.solve_cg = orig
+    t_fixed = t_step - sum(times)
+    per_it = [t / (cap + 1) for t in times]  # one SpMV for r0 plus `cap` iterations
+    est = t_fixed + sum((it + 1) * pi for it, pi in zip(iters_per_solve, per_it))
+    try:
+        import threadpoolctl  # noqa: F401
+        from threadpoolctl import threadpool_info
+        blas = max([d.get("num_threads", 1) for d in threadpool_info()] or [1])
+    except Exception:
+        blas = None
+    cores = len(os.sched_getaffinity(0))
+    return {"steps_per_s": 1.0 / est, "t_step_est_s": est, "t_fixed_s": t_fixed, "t_sample_s": t_step,
+            "per_iter_s": per_it, "cores": cores, "blas_threads": blas}
+
+
+# ------------------------------------------------------------------ our arm
+def run_ours(args):
+    import numpy as np
+    import torch
+    import torch.distributed as dist
+
+    rank, world, local = dist_env()
+    if world > 1:
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    torch.cuda.set_device(local)
+    from cupymag_gb300.build import build
+    build()
+    from cupymag_gb300 import _native as N
+    N.load()
+    from cupymag_gb300.core.assemble_simulation_operators import SimulationOperators
+    from cupymag_gb300.physics.llg import LLGSolver
+    from cupymag_gb300.workloads import seeded_m0, sweep_field, workload
+
+    p, w = workload(args.workload)
+    t_setup = time.perf_counter()
+    S = SimulationOperators(p)
+    L = LLGSolver(S, p, precision=args.precision)
+    torch.cuda.synchronize()
+    t_setup = time.perf_counter() - t_setup
+    m0 = seeded_m0(S.n_dof, S.DefDOF, seed=1234 + rank)
+    L.set_magnetization(torch.as_tensor(m0))
+    nsw = w["steps"]
+    fields = [sweep_field(p, s % nsw, nsw, w["B0"]) for s in range(args.warmup + 2 * args.steps)]
+    for s in range(args.warmup):
+        L.step(fields[s])
+        L.check()
+    stream = torch.cuda.current_stream()
+    # per-CG-launch events and solver infos for the roofline of the CG kernel
+    cg_events = []
+    orig_cg = L._cg
+
+    def timed_cg(A, b, x, k):
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        orig_cg(A, b, x, k)
+        e1.record(stream)
+        cg_events.append((A, 3 if b.dim() == 2 else 1, k, e0, e1))
+
+    L._cg = timed_cg
+    info_hist = []
+    warm_hist = []
+    launches0 = L.launches
+    if world > 1:
+        dist.barrier()
+    torch.cuda.synchronize()
+    t0 = torch.cuda.Event(enable_timing=True)
+    t1 = torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clk:
+        t0.record(stream)
+        for s in range(args.warmup, args.warmup + args.steps):
+            warm_hist.append(L.use_init.clone())
+            L.step(fields[s])
+            info_hist.append(L.info.clone())
+        t1.record(stream)
+        torch.cuda.synchronize()
+    if world > 1:
+        dist.barrier()
+    L._cg = orig_cg
+    launches = L.launches - launches0
+    L.check()
+    ms = t0.elapsed_time(t1)
+    # max over ranks
+    t_tensor = torch.tensor([ms], device="cuda")
+    if world > 1:
+        dist.all_reduce(t_tensor, op=dist.ReduceOp.MAX)
+    ms_max = float(t_tensor.item())
+    value = world * args.steps / (ms_max / 1e3)
+
+    # roofline of the CG kernel
+    from cupymag_gb300.solvers.linear_solvers import decode_info
+    per_step = len(cg_events) // args.steps
+    tot_bytes, tot_ms, dom = 0.0, 0.0, {}
+    iters_sum = np.zeros(10)
+    for i, (A, nv, k, e0, e1) in enumerate(cg_events):
+        s = i // per_step
+        inf = decode_info(info_hist[s][k].cpu().numpy())
+        warm = bool(warm_hist[s].item())
+        its = max(inf["iters"][:nv])
+        b = cg_launch_bytes(A, nv, its, warm)
+        d = e0.elapsed_time(e1)
+        tot_bytes += b
+        tot_ms += d
+        key = ["elasticity", "demag", "A1x3", "A1", "A1", "A2x3"][k]
+        dd = dom.setdefault(key, [0.0, 0.0, 0])
+        dd[0] += b
+        dd[1] += d
+        dd[2] += its
+    its_step = []
+    for s in range(args.steps):
+        infs = [decode_info(info_hist[s][k].cpu().numpy()) for k in range(6)]
+        row = ([infs[0]["iters"][0]] if L.ME else []) + [infs[1]["iters"][0]] + infs[2]["iters"][:3] + \
+              [infs[3]["iters"][0], infs[4]["iters"][0]] + infs[5]["iters"][:3]
+        its_step.append(row)
+    its_mean = [float(np.mean([r[j] for r in its_step])) for j in range(len(its_step[0]))]
+    peak, peak_kind = peaks()
+    achieved = tot_bytes / (tot_ms / 1e3) / 1e9
+    roof = {"kernel": "cg_fp64_kernel" if args.precision == "DP" else "cg_ir_kernel", "bound": "hbm",
+            "achieved": round(achieved, 1), "peak": peak, "peak_kind": peak_kind, "unit": "GB/s",
+            "frac": round(achieved / peak, 4), "traffic": None,
+            "share_of_step": round(tot_ms / ms, 4),
+            "per_solve": {k: {"GB/s": round(v[0] / (v[1] / 1e3) / 1e9, 1), "ms": round(v[1] / args.steps, 3),
+                              "iters": round(v[2] / args.steps, 1)} for k, v in dom.items()}}
+
+    # e2e: public API with host buffers
+    host_m = torch.empty((S.n_dof, 3), dtype=torch.float64).pin_memory()
+    host_m.copy_(L.m.cpu())
+    host_avg = torch.empty(3, dtype=torch.float64).pin_memory()
+    torch.cuda.synchronize()
+    tw = time.perf_counter()
+    for s in range(args.warmup + args.steps, args.warmup + 2 * args.steps):
+        L.m.copy_(host_m, non_blocking=True)
+        L.step(fields[s])
+        host_m.copy_(L.m, non_blocking=True)
+        host_avg.copy_(L.avg_m, non_blocking=True)
+        torch.cuda.current_stream().synchronize()
+    e2e_s = time.perf_counter() - tw
+    L.check()
+    e2e_t = torch.tensor([e2e_s], device="cuda")
+    if world > 1:
+        dist.all_reduce(e2e_t, op=dist.ReduceOp.MAX)
+    e2e_value = world * args.steps / float(e2e_t.item())
+
+    line = None
+    if rank == 0:
+        cpu = None
+        if world == 1 and not args.no_cpu_baseline:
+            try:
+                cs = cpu_sample(p, S, its_mean)
+                cpu = {"value": round(cs["steps_per_s"], 6), "unit": "steps/s", "cores": 1, "kind": "port",
+                       "sample": (f"oracle step at {w['n']}^3 with every CG capped at 3 iterations "
+                                  f"({cs['t_sample_s']:.1f} s), per-solve iteration time x this run's mean "
+                                  f"iterations {[round(x, 1) for x in its_mean]}; SciPy SpMV is single-threaded; "
+                                  f"host cores available {cs['cores']}, BLAS threads {cs['blas_threads']}"),
+                       "t_step_est_s": round(cs["t_step_est_s"], 2)}
+            except Exception as e:  # the baseline is reported, never required
+                cpu = {"value": None, "unit": "steps/s", "cores": 1, "kind": "port", "sample": f"failed: {e}"}
+        line = {
+            "metric": METRIC, "value": round(value, 4), "unit": "steps/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": round(ms_max / args.steps, 3), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64" if args.precision == "DP" else "f32+f64",
+            "data": "synthetic (seeded m0 = normalise((1,0,0)+N(0,1e-3)), fixed field sweep)",
+            "config": {"workload": args.workload, "mesh": f"hex {w['n']}^3 periodic, defect {w['defect']}^3",
+                       "n_dof": S.n_dof, "magnetoelastic": w["ME"], "rot111": w["rot111"],
+                       "precision": args.precision, "tol": p.tol, "sweep": f"+{w['B0']} T -> -{w['B0']} T over "
+                       f"{w['steps']} steps", "timed_steps": f"{args.warmup}..{args.warmup + args.steps - 1}",
+                       "l2": "inputs larger than L2 (operators %.1f GB resident)" % (
+                           sum(x.nbytes() for x in [L.A_demag, L.A1, L.A2, L.F1, L.Fx] +
+                               ([L.A_el, L.F_el] if L.ME else [])) / 1e9),
+                       "parallelism": f"replicas x{world}", "setup_s": round(t_setup, 1),
+                       "cg_iterations_per_step": [round(x, 1) for x in its_mean]},
+            "e2e": {"value": round(e2e_value, 4), "unit": "steps/s",
+                    "h2d_bytes_per_step": S.n_dof * 3 * 8, "d2h_bytes_per_step": S.n_dof * 3 * 8 + 24},
+            "gpu_launches": launches,
+            "roofline": roof,
+            "cpu_baseline": cpu,
+            "clocks": clk.summary(),
+        }
+        print(json.dumps(line))
+    if world > 1:
+        dist.barrier()
+        dist.destroy_process_group()
+    return line
+
+
+# ------------------------------------------------------------------ reference arm
+def run_reference(args):
+    rank, world, local = dist_env()
+    if rank != 0:
+        return None
+    import numpy as np
+    import torch
+    from cupymag_gb300.core.assemble_simulation_operators import SimulationOperators
+    from cupymag_gb300.workloads import workload
+
+    p, w = workload(args.workload)
+    dev = "cuda" if torch.cuda.is_available() else "cpu"
+    # setup only (not timed): the structured assembly builds the same CSR matrices
+    S = SimulationOperators(p, device=dev)
+    its = REFERENCE_ITERS.get(args.workload)
+    times = []
+    for s in range(args.warmup + args.steps):
+        cs = cpu_sample(p, S, its)
+        if s >= args.warmup:
+            times.append(cs["t_step_est_s"])
+    t = float(np.mean(times))
+    value = 1.0 / t
+    line = {"impl": "reference", "metric": METRIC, "value": round(value, 6), "unit": "steps/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(t * 1e3, 1), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": args.workload, "mesh": f"hex {w['n']}^3", "n_dof": S.n_dof},
+            "cpu_baseline": {"value": round(value, 6), "unit": "steps/s", "cores": 1, "kind": "port",
+                             "sample": (f"CPU oracle (NumPy/SciPy restatement of the reference step; the reference "
+                                        f"itself needs CuPy and a CUDA GPU): each step = one {w['n']}^3 step with "
+                                        f"every CG capped at 3 iterations, timed per solve and extrapolated with "
+                                        f"the GPU-measured warm-start iteration counts {its}")},
+            "e2e": {"value": round(value, 6), "unit": "steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+    return line
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--workload", default="hex128_me")
+    ap.add_argument("--precision", default="DP", choices=["DP", "IR"])
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

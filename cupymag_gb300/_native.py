@@ -1,0 +1,116 @@
+"""ctypes binding of ``libcupymag_gb300.so`` (the C-ABI of include/cupymag_gb300.h).
+
+The library is built in-tree by ``cupymag_gb300.build``.  There is no fallback:
+if the library is missing or no CUDA device is present, every device entry
+point raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import threading
+
+from .build import LIB
+
+_lock = threading.Lock()
+_lib = None
+
+CPM_OK, CPM_NOT_CONVERGED, CPM_BARRIER_TIMEOUT, CPM_NONFINITE, CPM_BAD_ARG, CPM_CUDA_ERROR = range(6)
+STATUS_NAMES = {0: "ok", 1: "not converged", 2: "grid barrier timeout", 3: "non-finite value", 4: "bad argument",
+                5: "CUDA error"}
+
+vp = C.c_void_p
+i64 = C.c_int64
+i32 = C.c_int32
+dbl = C.c_double
+
+
+class CSR(C.Structure):
+    _fields_ = [("rows", i64), ("cols", i64), ("nnz", i64), ("indptr", vp), ("indptr_is64", i32),
+                ("indices", vp), ("vals", vp), ("vals32", vp)]
+
+
+class CGInfo(C.Structure):
+    _fields_ = [("status", i32), ("iters", i32 * 3), ("outer", i32), ("pad", i32), ("resid", dbl * 3),
+                ("bnorm", dbl * 3)]
+
+
+class CGOpts(C.Structure):
+    _fields_ = [("tol", dbl), ("maxiter", i32), ("use_init_host", i32), ("use_init_dev", vp), ("precision", i32),
+                ("inner_tol", dbl), ("max_outer", i32), ("pad", i32), ("barrier_timeout_s", dbl)]
+
+
+class FieldParams(C.Structure):
+    _fields_ = [("K1", dbl), ("elasC1", dbl), ("elasC2", dbl), ("elasC3", dbl), ("lambda100", dbl),
+                ("Nd", dbl * 3), ("Hext", dbl * 3), ("R", dbl * 9), ("rot111", i32), ("has_E", i32)]
+
+
+CG_INFO_BYTES = C.sizeof(CGInfo)
+
+_PROTOS = {
+    "cpm_version": (C.c_char_p, []),
+    "cpm_last_error_string": (C.c_char_p, []),
+    "cpm_device_sm_count": (C.c_int, [C.c_int]),
+    "cpm_spmv_csr": (C.c_int, [C.POINTER(CSR), vp, vp, dbl, C.c_int, vp]),
+    "cpm_spmv_csr_multi": (C.c_int, [C.POINTER(CSR), vp, vp, vp, vp, dbl, C.c_int, vp, i64, vp]),
+    "cpm_cg_workspace_bytes": (C.c_size_t, [i64, C.c_int, C.c_int]),
+    "cpm_cg_solve": (C.c_int, [C.POINTER(CSR), vp, vp, C.c_int, C.POINTER(CGOpts), vp, C.c_size_t, vp, vp]),
+    "cpm_llg_field": (C.c_int, [C.POINTER(FieldParams), i64, vp, vp, vp, vp, dbl, vp, vp, vp]),
+    "cpm_gs_star": (C.c_int, [C.c_int, i64, vp, vp, vp, vp, vp, dbl, vp, vp, vp]),
+    "cpm_renorm_sumsq": (C.c_int, [i64, vp, vp, vp, vp, vp, dbl, dbl, vp, vp, vp, vp, vp]),
+    "cpm_volavg_scratch_doubles": (C.c_size_t, [C.c_int]),
+    "cpm_volavg": (C.c_int, [i64, C.c_int, vp, vp, dbl, vp, vp, vp, vp]),
+    "cpm_build_E0": (C.c_int, [i64, vp, dbl, dbl, vp, vp, vp, vp]),
+    "cpm_strain_from_u": (C.c_int, [C.POINTER(CSR), vp, vp, vp, vp, vp, vp]),
+    "cpm_strain_finalize": (C.c_int, [i64, vp, vp, vp, dbl, dbl, vp, vp, vp, C.c_int, vp]),
+}
+
+EXPORTED = tuple(_PROTOS)
+
+
+def load(build_if_missing: bool = False):
+    """Load the shared library (optionally building it first)."""
+    global _lib
+    with _lock:
+        if _lib is not None:
+            return _lib
+        import torch  # noqa: F401  (libcudart is resolved from the already-loaded torch)
+        if not LIB.exists():
+            if build_if_missing:
+                from .build import build
+                build()
+            else:
+                raise RuntimeError(
+                    f"cupymag_gb300 native library not found at {LIB}; build it with "
+                    "`python -m cupymag_gb300.build` (needs nvcc from CUDA 13)")
+        lib = C.CDLL(str(LIB), mode=C.RTLD_GLOBAL)
+        for name, (res, args) in _PROTOS.items():
+            fn = getattr(lib, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = lib
+        return lib
+
+
+def lib():
+    return _lib if _lib is not None else load()
+
+
+def last_error() -> str:
+    return lib().cpm_last_error_string().decode(errors="replace")
+
+
+def check(status: int, what: str):
+    if status != CPM_OK:
+        raise RuntimeError(f"{what} failed ({STATUS_NAMES.get(status, status)}): {last_error()}")
+
+
+def require_cuda():
+    import torch
+    if not torch.cuda.is_available():
+        raise RuntimeError("cupymag_gb300 needs a CUDA GPU (GB300, sm_103a); no CUDA device is available")
+
+
+def stream_ptr(stream=None) -> int:
+    import torch
+    s = torch.cuda.current_stream() if stream is None else stream
+    return s.cuda_stream

@@ -1,0 +1,164 @@
+"""Mesh + operators for one run (drop-in for cupymag/core/assemble_simulation_operators.py:27-118).
+
+``SimulationOperators(params)`` builds the mesh (FEMMesh of
+cupymag/mesh/setup_FEM_mesh.py:42-95), the periodic DOF map and the defect
+DOFs, and returns device CSR operators with the reference's method names:
+
+* csr_demag_and_deriv() -> A_demag (DOF-0 anchored Laplacian), Fx, Fy, Fz, Deriv
+* csr_GS()              -> A1 = alpha1 K + M, A2 = alpha2 K + M, F1 = M, with
+                           defect rows/columns enforced (:67-85)
+* csr_elasticity()      -> A_el (3 anchors), F_el, or (None, None) without ME
+* volume_average()      -> VolumeAverage
+
+Unlike the reference the parameters are an explicit object, not import-time
+globals, so one process can hold several meshes (serving).
+"""
+from __future__ import annotations
+
+import numpy as np
+import scipy.sparse as sp
+import torch
+
+from ..mesh.grids import HexGrid, TetraGrid, extract_defect_dofs
+from ..physics import assembly as AS
+from ..physics import structured_hex as SH
+from ..utils.compute_derivatives import ComputeDerivatives
+from ..utils.defect_shapes import get_defect_shape_function
+from ..utils.device_csr import DeviceCSR
+from ..utils.rot_111_matrices import get_M_matrix
+from ..utils.volume_average import VolumeAverage
+
+
+def _device_csr(indptr, indices, data, shape):
+    nnz = data.numel()
+    ip = indptr.to(torch.int64 if nnz >= 2 ** 31 else torch.int32)
+    return DeviceCSR(ip.contiguous(), indices.contiguous(), data.contiguous(), shape)
+
+
+class SimulationOperators:
+    def __init__(self, params, device=None, assembly="auto", mesh=None):
+        self.p = params
+        self.device = torch.device(device) if device is not None else torch.device("cuda", torch.cuda.current_device())
+        if mesh is not None:
+            self.fem_grid = mesh
+        elif params.grid_type == "Hex":
+            self.fem_grid = HexGrid(params.Nx, params.Ny, params.Nz, params.Ndx, params.Ndy, params.Ndz,
+                                    params.defect_center)
+        elif params.grid_type == "Tet":
+            params_shape = params.defect_parameters
+            if params.defect_shape == "RotatedEllipsoid":
+                params_shape = (params.defect_parameters, params.defect_rotation)
+            fn = get_defect_shape_function(params.defect_shape, params_shape)
+            self.fem_grid = TetraGrid(params.mesh_file, fn, params.defect_center)
+        else:
+            raise NotImplementedError(f"Grid type '{params.grid_type}' is not supported.")
+        self.node_coords_np, self.elements_np = self.fem_grid.std_fem_mesh()
+        self.global_id_np = self.fem_grid.build_periodic_node_map(self.node_coords_np)
+        self.n_dof = int(self.global_id_np.max()) + 1
+        self.n_nodes = self.node_coords_np.shape[0]
+        self.n_elements = self.elements_np.shape[0]
+        self.DefDOF = extract_defect_dofs(self.elements_np, self.global_id_np)
+        self.alpha1 = params.alpha1
+        self.alpha2 = params.alpha2
+        g = self.fem_grid
+        structured = isinstance(g, HexGrid) and min(g.Nx, g.Ny, g.Nz) >= 3
+        if assembly == "coo":
+            structured = False
+        elif assembly == "structured" and not structured:
+            raise ValueError("structured assembly needs a hex grid with at least 3 cells per axis")
+        self.structured = structured
+        self._coo_ops = None
+        self._elem = None
+
+    # ------------------------------------------------------------------ helpers
+    def _C(self):
+        p = self.p
+        return AS.stiffness_voigt(p.c11, p.c12, p.c44, get_M_matrix() if p.rot111 else None)
+
+    def _coo(self):
+        if self._coo_ops is None:
+            self._coo_ops = AS.assemble_coo(self.node_coords_np, self.elements_np, self.global_id_np, self.n_dof,
+                                            self.DefDOF, self.alpha1, self.alpha2, ME=self.p.ME,
+                                            C=self._C() if self.p.ME else None)
+        return self._coo_ops
+
+    def _cell(self):
+        """Element matrices of the unit cell at the origin (all cells are identical)."""
+        if self._elem is None:
+            el0 = self.elements_np[:1, :8]
+            xe = self.node_coords_np[el0]
+            K, M, F = AS.scalar_element_matrices(xe)
+            self._elem = {"K": K[0], "M": M[0], "F": [f[0] for f in F]}
+            if self.p.ME:
+                Kel, Fel = AS.elastic_element_matrices(xe, self._C())
+                self._elem["Kel"], self._elem["Fel"] = Kel[0], Fel[0]
+        return self._elem
+
+    def _scalar(self, Ke, anchors=(), defect=None, rows_only=False):
+        g = self.fem_grid
+        S = SH.stencil_from_element(Ke)[0, 0]
+        ip, ix, dv = SH.scalar_csr(g.Nx, g.Ny, g.Nz, S, self.device)
+        if anchors:
+            ip, ix, dv = SH.anchor(ip, ix, dv, anchors)
+        if defect is not None and len(defect):
+            ip, ix, dv = SH.drop_defect(ip, ix, dv, defect, cols_too=not rows_only, unit_diag=not rows_only)
+        return _device_csr(ip, ix, dv, (self.n_dof, self.n_dof))
+
+    # ------------------------------------------------------------------ reference API
+    def csr_demag_and_deriv(self):
+        if self.structured:
+            e = self._cell()
+            A = self._scalar(e["K"], anchors=(0,))
+            Fs = [self._scalar(f) for f in e["F"]]
+        else:
+            ops = self._coo()
+            A = DeviceCSR.from_scipy(ops["A_demag"], self.device)
+            Fs = [DeviceCSR.from_scipy(ops[k], self.device) for k in ("Fx", "Fy", "Fz")]
+        # the three derivative matrices share one pattern: keep one index copy
+        for f in Fs[1:]:
+            if f.same_pattern(Fs[0]):
+                f.indptr, f.indices, f._struct = Fs[0].indptr, Fs[0].indices, None
+        return A, Fs[0], Fs[1], Fs[2], ComputeDerivatives(*Fs)
+
+    def csr_GS(self):
+        if self.structured:
+            e = self._cell()
+            A1 = self._scalar(e["K"] * self.alpha1 + e["M"], defect=self.DefDOF)
+            A2 = self._scalar(e["K"] * self.alpha2 + e["M"], defect=self.DefDOF)
+            F1 = self._scalar(e["M"], defect=self.DefDOF, rows_only=True)
+            return A1, A2, F1
+        ops = self._coo()
+        return tuple(DeviceCSR.from_scipy(ops[k], self.device) for k in ("A1", "A2", "F1"))
+
+    def csr_elasticity(self):
+        if not self.p.ME:
+            return None, None
+        n = self.n_dof
+        if self.structured:
+            g = self.fem_grid
+            e = self._cell()
+            SA = SH.stencil_from_element(e["Kel"], 3, 3)
+            ip, ix, dv = SH.elastic_A_csr(g.Nx, g.Ny, g.Nz, SA, self.device)
+            ip, ix, dv = SH.anchor(ip, ix, dv, (0, n, 2 * n))
+            A_el = _device_csr(ip, ix, dv, (3 * n, 3 * n))
+            SF = SH.stencil_from_element(e["Fel"], 3, 6)
+            ip, ix, dv = SH.elastic_F_csr(g.Nx, g.Ny, g.Nz, SF, self.device)
+            ip, ix, dv = SH.anchor(ip, ix, dv, (0, n, 2 * n), cols_too=False, diag_one=False)
+            F_el = _device_csr(ip, ix, dv, (3 * n, 6 * n))
+            return A_el, F_el
+        ops = self._coo()
+        return DeviceCSR.from_scipy(ops["A_el"], self.device), DeviceCSR.from_scipy(ops["F_el"], self.device)
+
+    def volume_average(self):
+        return VolumeAverage(self.node_coords_np, self.elements_np, self.global_id_np, device=self.device)
+
+    # host copies (tests, CPU baseline)
+    def host_operators(self):
+        """All operators as SciPy CSR matrices on the host."""
+        A, Fx, Fy, Fz, _ = self.csr_demag_and_deriv()
+        A1, A2, F1 = self.csr_GS()
+        out = {"A_demag": A, "Fx": Fx, "Fy": Fy, "Fz": Fz, "A1": A1, "A2": A2, "F1": F1}
+        A_el, F_el = self.csr_elasticity()
+        if A_el is not None:
+            out.update(A_el=A_el, F_el=F_el)
+        return {k: v.to_scipy() for k, v in out.items()}

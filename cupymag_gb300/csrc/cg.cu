@@ -1,0 +1,668 @@
+// Persistent fused conjugate gradient for the GSPM LLG step (sm_103a).
+//
+// Replaces cupymag/solvers/linear_solvers.py:20-74, i.e. cupyx's cg, whose
+// algorithm is restated here:
+//   x = x0 if use_init else 0;  if ||b|| == 0 return b;  atol = tol ||b||;
+//   r = b - A x;  repeat: rho = r.r; p = r (first) or r + (rho/rho_old) p;
+//   q = A p; alpha = rho / (p.q); x += alpha p; r -= alpha q; iters++;
+//   stop when ||r|| <= atol (after the update) or iters == maxiter.
+//
+// One cooperative launch runs every iteration.  Each CTA owns a contiguous
+// block of rows; one iteration is two phases separated by a grid barrier:
+//   phase 1 (warp per row): p_new = r + beta p_old is formed on the fly while
+//     gathering, q = A p_new, and the CTA's partial of p.q;
+//   phase 2 (thread per row): x += alpha p, r -= alpha q, partial of r.r.
+// p is double-buffered so rows can gather neighbours' p_old while the owner
+// writes p_new.  Dot products are reduced in a fixed order (warp shuffle
+// tree, warps in order, CTAs in order) so results are deterministic, and every
+// CTA reduces the per-CTA partials itself, so all CTAs agree on alpha, beta
+// and on the stopping test without a third barrier.
+//
+// nrhs = 3 solves three systems with the same matrix (the g1n/g2n/g3n and
+// m1ss/m2ss/m3ss triples of Micromagnetics.py:221-223,280-290) in one sweep of
+// the matrix; each right-hand side keeps its own scalars, iteration count and
+// stopping test, so each result equals the single-system solve.
+//
+// precision = 1: FP32 CG (FP32 values and vectors, FP64 dot accumulation)
+// inside FP64 iterative refinement: r = b - A64 x in FP64, solve A32 d = r to
+// inner_tol relative, x += d, until ||b - A64 x|| <= tol ||b||.
+#include <cmath>
+#include <cstdio>
+
+#include "cpm_common.cuh"
+
+namespace cpm {
+
+constexpr int kCGThreads = 256;
+constexpr int kCGWarps = kCGThreads / kWarp;
+constexpr int kMaxGrid = 4096;                 // CTAs of one cooperative launch (upper bound)
+constexpr size_t kPartHalf = (size_t)6 * kMaxGrid;  // doubles per half of the partials buffer
+
+template <int NR, typename IT>
+struct CGArgs {
+  int64_t n;
+  const IT *rp;
+  const int *ci;
+  const double *av;
+  const float *av32;
+  const double *b;
+  double *x;
+  double tol;
+  int maxiter;
+  int use_init_host;
+  const int *use_init_dev;
+  double inner_tol;
+  int max_outer;
+  // workspace
+  double *r, *p0, *p1, *q;                 // FP64 vectors (n*NR each)
+  float *r32, *pa32, *pb32, *q32, *d32;    // FP32 vectors (mixed precision)
+  double *part;                            // [G][2*NR]
+  GridBarrier *bar;
+  cpm_cg_info *info;
+  unsigned long long timeout_ns;
+  int64_t rows_per_cta;
+};
+
+// Block-wide sum of NV values per thread, deterministic; result broadcast.
+template <int NV>
+__device__ __forceinline__ void block_sum(double (&v)[NV], double (*s)[kCGWarps]) {
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+#pragma unroll
+  for (int j = 0; j < NV; ++j) {
+    double t = warp_sum(v[j]);
+    if (lane == 0) s[j][w] = t;
+  }
+  __syncthreads();
+#pragma unroll
+  for (int j = 0; j < NV; ++j) {
+    double t = 0.0;
+#pragma unroll
+    for (int k = 0; k < kCGWarps; ++k) t += s[j][k];
+    v[j] = t;
+  }
+  __syncthreads();
+}
+
+// Write this CTA's NV partials, barrier, and reduce all CTAs' partials.
+// The partials buffer alternates between two halves: a CTA may start writing
+// the next reduction's partials while slower CTAs still read this one's, and
+// the barrier of the next reduction orders the reuse of a half.
+template <int NV>
+__device__ __forceinline__ bool grid_sum(double (&v)[NV], double *part, int &parity, GridBarrier *bar,
+                                         unsigned long long tns, double (*s)[kCGWarps]) {
+  block_sum<NV>(v, s);
+  const int G = gridDim.x;
+  part += (size_t)parity * kPartHalf;
+  parity ^= 1;
+  if (threadIdx.x < NV) part[(size_t)blockIdx.x * NV + threadIdx.x] = v[threadIdx.x];
+  if (!grid_sync(bar, G, tns)) return false;
+  double acc[NV];
+#pragma unroll
+  for (int j = 0; j < NV; ++j) acc[j] = 0.0;
+  for (int g = threadIdx.x; g < G; g += blockDim.x) {
+#pragma unroll
+    for (int j = 0; j < NV; ++j) acc[j] += __ldcg(&part[(size_t)g * NV + j]);
+  }
+  block_sum<NV>(acc, s);
+#pragma unroll
+  for (int j = 0; j < NV; ++j) v[j] = acc[j];
+  return true;
+}
+
+template <typename IT>
+__device__ __forceinline__ void row_range(const IT *rp, int64_t row, int64_t &s, int64_t &e) {
+  s = (int64_t)__ldg(rp + row);
+  e = (int64_t)__ldg(rp + row + 1);
+}
+
+__device__ __forceinline__ void set_status(cpm_cg_info *info, int st) {
+  atomicMax(&info->status, st);
+}
+
+// ------------------------------------------------------------------ FP64 CG
+template <int NR, typename IT>
+__global__ void __launch_bounds__(kCGThreads) cg_fp64_kernel(CGArgs<NR, IT> a) {
+  __shared__ double s_red[2 * NR][kCGWarps];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int64_t r0 = min(a.n, (int64_t)blockIdx.x * a.rows_per_cta);
+  const int64_t r1 = min(a.n, r0 + a.rows_per_cta);
+  const bool use_init = a.use_init_dev ? (__ldcg(a.use_init_dev) != 0) : (a.use_init_host != 0);
+  const unsigned long long tns = a.timeout_ns;
+  int par = 0;
+
+  // ---- prologue: r = b - A x (or r = b, x = 0), ||b||^2, ||r||^2
+  double v[2 * NR];
+#pragma unroll
+  for (int j = 0; j < 2 * NR; ++j) v[j] = 0.0;
+  if (use_init) {
+    for (int64_t row = r0 + warp; row < r1; row += kCGWarps) {
+      int64_t s, e;
+      row_range(a.rp, row, s, e);
+      double acc[NR];
+#pragma unroll
+      for (int j = 0; j < NR; ++j) acc[j] = 0.0;
+      for (int64_t k = s + lane; k < e; k += kWarp) {
+        const double av = ld_stream(a.av + k);
+        const int c = ld_stream(a.ci + k);
+#pragma unroll
+        for (int j = 0; j < NR; ++j) acc[j] = fma(av, a.x[(int64_t)c * NR + j], acc[j]);
+      }
+#pragma unroll
+      for (int j = 0; j < NR; ++j) acc[j] = warp_sum(acc[j]);
+      if (lane == 0) {
+#pragma unroll
+        for (int j = 0; j < NR; ++j) {
+          const double bj = a.b[row * NR + j];
+          const double rj = bj - acc[j];
+          a.r[row * NR + j] = rj;
+          v[j] = fma(bj, bj, v[j]);
+          v[NR + j] = fma(rj, rj, v[NR + j]);
+        }
+      }
+    }
+  } else {
+    for (int64_t row = r0 + threadIdx.x; row < r1; row += kCGThreads) {
+#pragma unroll
+      for (int j = 0; j < NR; ++j) {
+        const double bj = a.b[row * NR + j];
+        a.r[row * NR + j] = bj;
+        a.x[row * NR + j] = 0.0;
+        v[j] = fma(bj, bj, v[j]);
+        v[NR + j] = fma(bj, bj, v[NR + j]);
+      }
+    }
+  }
+  if (!grid_sum<2 * NR>(v, a.part, par, a.bar, tns, s_red)) {
+    set_status(a.info, CPM_BARRIER_TIMEOUT);
+    return;
+  }
+  double atol[NR], rho[NR], rho_old[NR], resid[NR];
+  int active[NR], iters[NR];
+  bool any = false;
+#pragma unroll
+  for (int j = 0; j < NR; ++j) {
+    const double bn = sqrt(v[j]);
+    atol[j] = a.tol * bn;
+    rho[j] = v[NR + j];
+    rho_old[j] = 1.0;
+    resid[j] = sqrt(v[NR + j]);
+    active[j] = bn != 0.0;
+    iters[j] = 0;
+    any |= active[j] != 0;
+    if (bn == 0.0 && use_init) {
+      // cupyx returns b itself when ||b|| == 0
+      for (int64_t row = r0 + threadIdx.x; row < r1; row += kCGThreads) a.x[row * NR + j] = a.b[row * NR + j];
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) a.info->bnorm[j] = bn;
+  }
+
+  int status = CPM_OK;
+  for (int k = 0; any && k < a.maxiter; ++k) {
+    double beta[NR];
+#pragma unroll
+    for (int j = 0; j < NR; ++j) beta[j] = (k == 0 || !active[j]) ? 0.0 : rho[j] / rho_old[j];
+    const double *pin = (k & 1) ? a.p1 : a.p0;
+    double *pout = (k & 1) ? a.p0 : a.p1;
+
+    // ---- phase 1: q = A (r + beta p_old), p_new, partial p.q
+#pragma unroll
+    for (int j = 0; j < NR; ++j) v[j] = 0.0;
+    for (int64_t row = r0 + warp; row < r1; row += kCGWarps) {
+      int64_t s, e;
+      row_range(a.rp, row, s, e);
+      double acc[NR];
+#pragma unroll
+      for (int j = 0; j < NR; ++j) acc[j] = 0.0;
+      if (k == 0) {
+        for (int64_t kk = s + lane; kk < e; kk += kWarp) {
+          const double av = ld_stream(a.av + kk);
+          const int64_t c = ld_stream(a.ci + kk);
+#pragma unroll
+          for (int j = 0; j < NR; ++j) acc[j] = fma(av, a.r[c * NR + j], acc[j]);
+        }
+      } else {
+        for (int64_t kk = s + lane; kk < e; kk += kWarp) {
+          const double av = ld_stream(a.av + kk);
+          const int64_t c = ld_stream(a.ci + kk);
+#pragma unroll
+          for (int j = 0; j < NR; ++j) acc[j] = fma(av, __fma_rn(beta[j], pin[c * NR + j], a.r[c * NR + j]), acc[j]);
+        }
+      }
+#pragma unroll
+      for (int j = 0; j < NR; ++j) acc[j] = warp_sum(acc[j]);
+      if (lane == 0) {
+#pragma unroll
+        for (int j = 0; j < NR; ++j) {
+          const double pn = (k == 0) ? a.r[row * NR + j] : __fma_rn(beta[j], pin[row * NR + j], a.r[row * NR + j]);
+          pout[row * NR + j] = pn;
+          a.q[row * NR + j] = acc[j];
+          v[j] = fma(pn, acc[j], v[j]);
+        }
+      }
+    }
+    double pq[NR];
+#pragma unroll
+    for (int j = 0; j < NR; ++j) pq[j] = v[j];
+    if (!grid_sum<NR>(pq, a.part, par, a.bar, tns, s_red)) { status = CPM_BARRIER_TIMEOUT; break; }
+    double alpha[NR];
+    bool bad = false;
+#pragma unroll
+    for (int j = 0; j < NR; ++j) {
+      alpha[j] = active[j] ? rho[j] / pq[j] : 0.0;
+      if (active[j] && !isfinite(alpha[j])) bad = true;
+    }
+    if (bad) { status = CPM_NONFINITE; break; }
+
+    // ---- phase 2: x += alpha p, r -= alpha q, partial r.r
+    double rr[NR];
+#pragma unroll
+    for (int j = 0; j < NR; ++j) rr[j] = 0.0;
+    for (int64_t row = r0 + threadIdx.x; row < r1; row += kCGThreads) {
+#pragma unroll
+      for (int j = 0; j < NR; ++j) {
+        const int64_t i = row * NR + j;
+        a.x[i] = __fma_rn(alpha[j], pout[i], a.x[i]);
+        const double rn = __fma_rn(-alpha[j], a.q[i], a.r[i]);
+        a.r[i] = rn;
+        rr[j] = fma(rn, rn, rr[j]);
+      }
+    }
+    if (!grid_sum<NR>(rr, a.part, par, a.bar, tns, s_red)) { status = CPM_BARRIER_TIMEOUT; break; }
+    any = false;
+#pragma unroll
+    for (int j = 0; j < NR; ++j) {
+      if (!active[j]) continue;
+      if (!isfinite(rr[j])) bad = true;
+      iters[j] += 1;
+      rho_old[j] = rho[j];
+      rho[j] = rr[j];
+      resid[j] = sqrt(rr[j]);
+      if (resid[j] <= atol[j]) active[j] = 0;
+      any |= active[j] != 0;
+    }
+    if (bad) { status = CPM_NONFINITE; break; }
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    int st = status;
+#pragma unroll
+    for (int j = 0; j < NR; ++j) {
+      if (st == CPM_OK && active[j]) st = CPM_NOT_CONVERGED;
+      a.info->iters[j] = iters[j];
+      a.info->resid[j] = resid[j];
+    }
+    a.info->outer = 0;
+    set_status(a.info, st);
+  } else if (status != CPM_OK && threadIdx.x == 0) {
+    set_status(a.info, status);
+  }
+}
+
+// ------------------------------------------------ FP32 CG in FP64 refinement
+template <int NR, typename IT>
+__global__ void __launch_bounds__(kCGThreads) cg_ir_kernel(CGArgs<NR, IT> a) {
+  __shared__ double s_red[2 * NR][kCGWarps];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int64_t r0 = min(a.n, (int64_t)blockIdx.x * a.rows_per_cta);
+  const int64_t r1 = min(a.n, r0 + a.rows_per_cta);
+  const bool use_init = a.use_init_dev ? (__ldcg(a.use_init_dev) != 0) : (a.use_init_host != 0);
+  const unsigned long long tns = a.timeout_ns;
+  int par = 0;
+
+  // ---- ||b||, x0
+  double v[2 * NR];
+#pragma unroll
+  for (int j = 0; j < 2 * NR; ++j) v[j] = 0.0;
+  for (int64_t row = r0 + threadIdx.x; row < r1; row += kCGThreads) {
+#pragma unroll
+    for (int j = 0; j < NR; ++j) {
+      const double bj = a.b[row * NR + j];
+      if (!use_init) a.x[row * NR + j] = 0.0;
+      v[j] = fma(bj, bj, v[j]);
+    }
+  }
+  double bb[NR];
+#pragma unroll
+  for (int j = 0; j < NR; ++j) bb[j] = v[j];
+  if (!grid_sum<NR>(bb, a.part, par, a.bar, tns, s_red)) {
+    set_status(a.info, CPM_BARRIER_TIMEOUT);
+    return;
+  }
+  double atol[NR], resid[NR];
+  int active[NR], iters[NR];
+  bool any = false;
+#pragma unroll
+  for (int j = 0; j < NR; ++j) {
+    const double bn = sqrt(bb[j]);
+    atol[j] = a.tol * bn;
+    resid[j] = bn;
+    active[j] = bn != 0.0;
+    iters[j] = 0;
+    any |= active[j] != 0;
+    if (bn == 0.0 && use_init)
+      for (int64_t row = r0 + threadIdx.x; row < r1; row += kCGThreads) a.x[row * NR + j] = a.b[row * NR + j];
+    if (blockIdx.x == 0 && threadIdx.x == 0) a.info->bnorm[j] = bn;
+  }
+  int status = CPM_OK;
+  int outer = 0;
+  int total = 0;
+  while (any) {
+    // ---- outer residual r = b - A64 x in FP64; FP32 copy; d = 0
+    double rr64[NR], rr32[NR];
+#pragma unroll
+    for (int j = 0; j < NR; ++j) { rr64[j] = 0.0; rr32[j] = 0.0; }
+    for (int64_t row = r0 + warp; row < r1; row += kCGWarps) {
+      int64_t s, e;
+      row_range(a.rp, row, s, e);
+      double acc[NR];
+#pragma unroll
+      for (int j = 0; j < NR; ++j) acc[j] = 0.0;
+      for (int64_t kk = s + lane; kk < e; kk += kWarp) {
+        const double av = ld_stream(a.av + kk);
+        const int64_t c = ld_stream(a.ci + kk);
+#pragma unroll
+        for (int j = 0; j < NR; ++j) acc[j] = fma(av, a.x[c * NR + j], acc[j]);
+      }
+#pragma unroll
+      for (int j = 0; j < NR; ++j) acc[j] = warp_sum(acc[j]);
+      if (lane == 0) {
+#pragma unroll
+        for (int j = 0; j < NR; ++j) {
+          const double rj = a.b[row * NR + j] - acc[j];
+          const float rf = (float)rj;
+          a.r32[row * NR + j] = rf;
+          a.d32[row * NR + j] = 0.0f;
+          rr64[j] = fma(rj, rj, rr64[j]);
+          rr32[j] = fma((double)rf, (double)rf, rr32[j]);
+        }
+      }
+    }
+    double red[2 * NR];
+#pragma unroll
+    for (int j = 0; j < NR; ++j) { red[j] = rr64[j]; red[NR + j] = rr32[j]; }
+    if (!grid_sum<2 * NR>(red, a.part, par, a.bar, tns, s_red)) { status = CPM_BARRIER_TIMEOUT; break; }
+    any = false;
+    double rho[NR], rho_old[NR], iatol[NR];
+    int iact[NR];
+    bool iany = false;
+#pragma unroll
+    for (int j = 0; j < NR; ++j) {
+      if (active[j]) {
+        resid[j] = sqrt(red[j]);
+        if (!(resid[j] > atol[j])) active[j] = 0;
+      }
+      any |= active[j] != 0;
+      rho[j] = red[NR + j];
+      rho_old[j] = 1.0;
+      iact[j] = active[j];
+      iatol[j] = a.inner_tol * sqrt(red[NR + j]);
+      iany |= iact[j] != 0;
+    }
+    if (!any) break;
+    if (outer >= a.max_outer || total >= a.maxiter) break;
+    ++outer;
+
+    // ---- inner FP32 CG on A32 d = r32
+    int kin = 0;
+    while (iany && total < a.maxiter) {
+      double beta[NR];
+#pragma unroll
+      for (int j = 0; j < NR; ++j) beta[j] = (kin == 0 || !iact[j]) ? 0.0 : rho[j] / rho_old[j];
+      const float *pin = (kin & 1) ? a.pb32 : a.pa32;
+      float *pout = (kin & 1) ? a.pa32 : a.pb32;
+      float fb[NR];
+#pragma unroll
+      for (int j = 0; j < NR; ++j) fb[j] = (float)beta[j];
+#pragma unroll
+      for (int j = 0; j < NR; ++j) v[j] = 0.0;
+      for (int64_t row = r0 + warp; row < r1; row += kCGWarps) {
+        int64_t s, e;
+        row_range(a.rp, row, s, e);
+        float acc[NR];
+#pragma unroll
+        for (int j = 0; j < NR; ++j) acc[j] = 0.0f;
+        if (kin == 0) {
+          for (int64_t kk = s + lane; kk < e; kk += kWarp) {
+            const float av = ld_stream(a.av32 + kk);
+            const int64_t c = ld_stream(a.ci + kk);
+#pragma unroll
+            for (int j = 0; j < NR; ++j) acc[j] = fmaf(av, a.r32[c * NR + j], acc[j]);
+          }
+        } else {
+          for (int64_t kk = s + lane; kk < e; kk += kWarp) {
+            const float av = ld_stream(a.av32 + kk);
+            const int64_t c = ld_stream(a.ci + kk);
+#pragma unroll
+            for (int j = 0; j < NR; ++j) acc[j] = fmaf(av, __fmaf_rn(fb[j], pin[c * NR + j], a.r32[c * NR + j]), acc[j]);
+          }
+        }
+        double accd[NR];
+#pragma unroll
+        for (int j = 0; j < NR; ++j) accd[j] = warp_sum((double)acc[j]);
+        if (lane == 0) {
+#pragma unroll
+          for (int j = 0; j < NR; ++j) {
+            const float pn = (kin == 0) ? a.r32[row * NR + j] : __fmaf_rn(fb[j], pin[row * NR + j], a.r32[row * NR + j]);
+            const float qf = (float)accd[j];
+            pout[row * NR + j] = pn;
+            a.q32[row * NR + j] = qf;
+            v[j] = fma((double)pn, (double)qf, v[j]);
+          }
+        }
+      }
+      double pq[NR];
+#pragma unroll
+      for (int j = 0; j < NR; ++j) pq[j] = v[j];
+      if (!grid_sum<NR>(pq, a.part, par, a.bar, tns, s_red)) { status = CPM_BARRIER_TIMEOUT; break; }
+      double alpha[NR];
+      bool bad = false;
+#pragma unroll
+      for (int j = 0; j < NR; ++j) {
+        alpha[j] = iact[j] ? rho[j] / pq[j] : 0.0;
+        if (iact[j] && !isfinite(alpha[j])) bad = true;
+      }
+      if (bad) { status = CPM_NONFINITE; break; }
+      double rr[NR];
+#pragma unroll
+      for (int j = 0; j < NR; ++j) rr[j] = 0.0;
+      for (int64_t row = r0 + threadIdx.x; row < r1; row += kCGThreads) {
+#pragma unroll
+        for (int j = 0; j < NR; ++j) {
+          const int64_t i = row * NR + j;
+          a.d32[i] = (float)fma(alpha[j], (double)pout[i], (double)a.d32[i]);
+          const float rn = (float)fma(-alpha[j], (double)a.q32[i], (double)a.r32[i]);
+          a.r32[i] = rn;
+          rr[j] = fma((double)rn, (double)rn, rr[j]);
+        }
+      }
+      if (!grid_sum<NR>(rr, a.part, par, a.bar, tns, s_red)) { status = CPM_BARRIER_TIMEOUT; break; }
+      iany = false;
+#pragma unroll
+      for (int j = 0; j < NR; ++j) {
+        if (!iact[j]) continue;
+        if (!isfinite(rr[j])) bad = true;
+        iters[j] += 1;
+        rho_old[j] = rho[j];
+        rho[j] = rr[j];
+        if (sqrt(rr[j]) <= iatol[j]) iact[j] = 0;
+        iany |= iact[j] != 0;
+      }
+      if (bad) { status = CPM_NONFINITE; break; }
+      ++kin;
+      ++total;
+    }
+    if (status != CPM_OK) break;
+    // ---- x += d (FP64)
+    for (int64_t row = r0 + threadIdx.x; row < r1; row += kCGThreads) {
+#pragma unroll
+      for (int j = 0; j < NR; ++j)
+        if (active[j]) a.x[row * NR + j] += (double)a.d32[row * NR + j];
+    }
+    if (!grid_sync(a.bar, gridDim.x, tns)) { status = CPM_BARRIER_TIMEOUT; break; }
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    int st = status;
+#pragma unroll
+    for (int j = 0; j < NR; ++j) {
+      if (st == CPM_OK && active[j]) st = CPM_NOT_CONVERGED;
+      a.info->iters[j] = iters[j];
+      a.info->resid[j] = resid[j];
+    }
+    a.info->outer = outer;
+    set_status(a.info, st);
+  } else if (status != CPM_OK && threadIdx.x == 0) {
+    set_status(a.info, status);
+  }
+}
+
+// ------------------------------------------------------------------ launch
+struct Workspace {
+  GridBarrier *bar;
+  double *part;
+  double *r, *p0, *p1, *q;
+  float *r32, *pa32, *pb32, *q32, *d32;
+};
+
+static size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
+
+
+static size_t layout(int64_t n, int nrhs, int precision, char *base, Workspace *w) {
+  size_t off = 0;
+  auto take = [&](size_t bytes) -> char * {
+    char *p = base ? base + off : nullptr;
+    off += align256(bytes);
+    return p;
+  };
+  Workspace t{};
+  t.bar = (GridBarrier *)take(sizeof(GridBarrier));
+  t.part = (double *)take(sizeof(double) * 2 * kPartHalf);
+  const size_t nv = (size_t)n * nrhs;
+  if (precision == 0) {
+    t.r = (double *)take(8 * nv);
+    t.p0 = (double *)take(8 * nv);
+    t.p1 = (double *)take(8 * nv);
+    t.q = (double *)take(8 * nv);
+  } else {
+    t.r32 = (float *)take(4 * nv);
+    t.pa32 = (float *)take(4 * nv);
+    t.pb32 = (float *)take(4 * nv);
+    t.q32 = (float *)take(4 * nv);
+    t.d32 = (float *)take(4 * nv);
+  }
+  if (w) *w = t;
+  return off;
+}
+
+template <int NR, typename IT>
+static int launch_cg(const cpm_csr *A, const double *b, double *x, const cpm_cg_opts *o, Workspace &w,
+                     cpm_cg_info *info, cudaStream_t st) {
+  CGArgs<NR, IT> a{};
+  a.n = A->rows;
+  a.rp = (const IT *)A->indptr;
+  a.ci = A->indices;
+  a.av = A->vals;
+  a.av32 = A->vals32;
+  a.b = b;
+  a.x = x;
+  a.tol = o->tol;
+  a.maxiter = o->maxiter;
+  a.use_init_host = o->use_init_host;
+  a.use_init_dev = o->use_init_dev;
+  a.inner_tol = o->inner_tol > 0 ? o->inner_tol : 1e-5;
+  a.max_outer = o->max_outer > 0 ? o->max_outer : 50;
+  a.r = w.r;
+  a.p0 = w.p0;
+  a.p1 = w.p1;
+  a.q = w.q;
+  a.r32 = w.r32;
+  a.pa32 = w.pa32;
+  a.pb32 = w.pb32;
+  a.q32 = w.q32;
+  a.d32 = w.d32;
+  a.part = w.part;
+  a.bar = w.bar;
+  a.info = info;
+  const double tmo = o->barrier_timeout_s > 0 ? o->barrier_timeout_s : 2.0;
+  a.timeout_ns = (unsigned long long)(tmo * 1e9);
+
+  const void *fn = (o->precision == 0) ? (const void *)cg_fp64_kernel<NR, IT> : (const void *)cg_ir_kernel<NR, IT>;
+  static int cached_dev[2][2][2] = {};
+  static int cached_occ[2][2][2] = {};
+  const int dev = device_id();
+  const int pi = o->precision ? 1 : 0, ri = NR == 3, ii = sizeof(IT) == 8;
+  int &occ = cached_occ[pi][ri][ii];
+  int &occ_dev = cached_dev[pi][ri][ii];
+  if (occ == 0 || occ_dev != dev + 1) {
+    int blocks = 0;
+    CPM_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, fn, kCGThreads, 0));
+    occ = blocks;
+    occ_dev = dev + 1;
+  }
+  if (occ < 1) {
+    set_error("cg: kernel cannot be resident on an SM");
+    return CPM_CUDA_ERROR;
+  }
+  int64_t gmax = (int64_t)occ * sm_count();
+  if (gmax > kMaxGrid) gmax = kMaxGrid;
+  // at least ~64 rows per CTA so small systems do not pay for idle CTAs at barriers
+  int64_t G = (a.n + 63) / 64;
+  if (G > gmax) G = gmax;
+  if (G < 1) G = 1;
+  int64_t rpc = (a.n + G - 1) / G;
+  rpc = (rpc + 31) / 32 * 32;
+  G = (a.n + rpc - 1) / rpc;
+  if (G < 1) G = 1;
+  a.rows_per_cta = rpc;
+
+  CPM_TRY(cudaMemsetAsync(w.bar, 0, sizeof(GridBarrier), st));
+  CPM_TRY(cudaMemsetAsync(info, 0, sizeof(cpm_cg_info), st));
+  void *args[] = {&a};
+  CPM_TRY(cudaLaunchCooperativeKernel(fn, dim3((unsigned)G), dim3(kCGThreads), args, 0, st));
+  return CPM_OK;
+}
+
+}  // namespace cpm
+
+extern "C" size_t cpm_cg_workspace_bytes(int64_t n, int nrhs, int precision) {
+  return cpm::layout(n, nrhs, precision ? 1 : 0, nullptr, nullptr);
+}
+
+extern "C" int cpm_cg_solve(const cpm_csr *A, const double *b, double *x, int nrhs, const cpm_cg_opts *opts,
+                            void *workspace, size_t workspace_bytes, cpm_cg_info *info_dev, void *stream) {
+  using namespace cpm;
+  if (!A || !b || !x || !opts || !workspace || !info_dev) {
+    set_error("cpm_cg_solve: null argument");
+    return CPM_BAD_ARG;
+  }
+  if (nrhs != 1 && nrhs != 3) {
+    set_error("cpm_cg_solve: nrhs must be 1 or 3 (got %d)", nrhs);
+    return CPM_BAD_ARG;
+  }
+  if (A->rows != A->cols) {
+    set_error("cpm_cg_solve: matrix must be square (%lld x %lld)", (long long)A->rows, (long long)A->cols);
+    return CPM_BAD_ARG;
+  }
+  const int prec = opts->precision ? 1 : 0;
+  if (prec == 1 && !A->vals32) {
+    set_error("cpm_cg_solve: mixed precision needs the FP32 copy of the values (vals32)");
+    return CPM_BAD_ARG;
+  }
+  if (opts->maxiter < 0) {
+    set_error("cpm_cg_solve: maxiter must be >= 0");
+    return CPM_BAD_ARG;
+  }
+  const size_t need = layout(A->rows, nrhs, prec, nullptr, nullptr);
+  if (workspace_bytes < need) {
+    set_error("cpm_cg_solve: workspace too small (%zu < %zu bytes)", workspace_bytes, need);
+    return CPM_BAD_ARG;
+  }
+  if (A->rows == 0) return CPM_OK;
+  Workspace w;
+  layout(A->rows, nrhs, prec, (char *)workspace, &w);
+  cudaStream_t st = (cudaStream_t)stream;
+  if (A->indptr_is64) {
+    return nrhs == 1 ? launch_cg<1, int64_t>(A, b, x, opts, w, info_dev, st)
+                     : launch_cg<3, int64_t>(A, b, x, opts, w, info_dev, st);
+  }
+  return nrhs == 1 ? launch_cg<1, int32_t>(A, b, x, opts, w, info_dev, st)
+                   : launch_cg<3, int32_t>(A, b, x, opts, w, info_dev, st);
+}

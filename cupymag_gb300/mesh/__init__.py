@@ -1,0 +1,1 @@
+"""Subpackage of cupymag_gb300."""

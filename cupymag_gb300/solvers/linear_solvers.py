@@ -1,0 +1,133 @@
+"""Conjugate-gradient solves on the GPU (drop-in for cupymag/solvers/linear_solvers.py).
+
+``solve_cg`` keeps the reference signature and behaviour
+(linear_solvers.py:20-74): x0 is used only when ``use_init`` is true, the
+tolerance is relative to ||b||, a zero right-hand side returns b, and a solve
+that reaches ``maxiter`` raises ``RuntimeError`` with the same message text
+("Error! CG for {system} did not converge. info={info}, residual={rnorm}.").
+
+The work runs in one persistent cooperative kernel per solve (see
+csrc/cg.cu).  ``CGSolver`` keeps the workspace between solves so the LLG step
+allocates nothing per step; ``precision="IR"`` selects FP32 CG inside FP64
+iterative refinement.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+import torch
+
+from .. import _native as N
+from ..utils.device_csr import DeviceCSR
+
+PRECISIONS = {"DP": 0, "FP64": 0, "IR": 1, "MIXED": 1, "SP": 1}
+
+
+class CGSolver:
+    """Reusable solver state: workspace and the device info record."""
+
+    def __init__(self, device=None):
+        self.device = device or torch.device("cuda", torch.cuda.current_device())
+        self._ws = {}
+        self.barrier_timeout_s = 2.0
+        self.inner_tol = 1e-5
+        self.max_outer = 60
+
+    def workspace(self, n, nrhs, prec):
+        key = (n, nrhs, prec)
+        ws = self._ws.get(key)
+        if ws is None:
+            nbytes = N.lib().cpm_cg_workspace_bytes(n, nrhs, prec)
+            ws = torch.zeros(nbytes, dtype=torch.uint8, device=self.device)
+            self._ws[key] = ws
+        return ws
+
+    def launch(self, A: DeviceCSR, b: torch.Tensor, x: torch.Tensor, info: torch.Tensor, *, tol, maxiter,
+               use_init=False, use_init_dev: torch.Tensor = None, precision="DP"):
+        """Asynchronous solve; x is read as x0 when use_init, and overwritten."""
+        prec = PRECISIONS[precision] if isinstance(precision, str) else int(precision)
+        if prec == 1:
+            A.ensure_fp32()
+        n = A.shape[0]
+        nrhs = 1 if b.dim() == 1 else b.shape[1]
+        if b.shape[0] != n or x.shape != b.shape:
+            raise ValueError(f"solve shapes: A {A.shape}, b {tuple(b.shape)}, x {tuple(x.shape)}")
+        if not (b.is_contiguous() and x.is_contiguous()) or b.dtype != torch.float64 or x.dtype != torch.float64:
+            raise TypeError("b and x must be contiguous float64 device tensors")
+        ws = self.workspace(n, nrhs, prec)
+        o = N.CGOpts()
+        o.tol = float(tol)
+        o.maxiter = int(maxiter)
+        o.use_init_host = 1 if use_init else 0
+        o.use_init_dev = use_init_dev.data_ptr() if use_init_dev is not None else None
+        o.precision = prec
+        o.inner_tol = self.inner_tol
+        o.max_outer = self.max_outer
+        o.barrier_timeout_s = self.barrier_timeout_s
+        N.check(N.lib().cpm_cg_solve(A.struct(), b.data_ptr(), x.data_ptr(), nrhs, C.byref(o), ws.data_ptr(),
+                                     ws.numel(), info.data_ptr(), N.stream_ptr()), "cpm_cg_solve")
+
+
+def new_info(count=1, device=None) -> torch.Tensor:
+    """Device storage for `count` cpm_cg_info records."""
+    return torch.zeros((count, N.CG_INFO_BYTES), dtype=torch.uint8, device=device or "cuda")
+
+
+def decode_info(raw: np.ndarray) -> dict:
+    b = np.ascontiguousarray(raw).tobytes()
+    inf = N.CGInfo.from_buffer_copy(b)
+    return {"status": int(inf.status), "iters": list(inf.iters), "outer": int(inf.outer),
+            "resid": list(inf.resid), "bnorm": list(inf.bnorm)}
+
+
+_default = None
+
+
+def default_solver() -> CGSolver:
+    global _default
+    if _default is None:
+        N.require_cuda()
+        _default = CGSolver()
+    return _default
+
+
+def raise_for(info: dict, A, b, x, system=None, nrhs=1):
+    st = info["status"]
+    if st == N.CPM_OK:
+        return
+    if st == N.CPM_NOT_CONVERGED:
+        r = b - A.spmv(x)
+        rnorm = float(torch.linalg.norm(r))
+        its = info["iters"][0] if nrhs == 1 else info["iters"][:nrhs]
+        if system is not None:
+            msg = f"Error! CG for {system} did not converge. info={its}, residual={rnorm}."
+        else:
+            msg = f"Error! CG did not converge. info={its}, residual={rnorm}."
+        raise RuntimeError(msg)
+    raise RuntimeError(f"CG for {system or 'system'} failed: {N.STATUS_NAMES.get(st, st)}")
+
+
+def solve_cg(A, b, M=None, x0=None, tol=1e-7, maxiter=5000, use_init=False, system=None, precision="DP"):
+    """Solve A x = b (A: DeviceCSR or SciPy CSR, b: tensor or array); returns a float64 CUDA tensor.
+
+    Same contract as cupymag/solvers/linear_solvers.py:20-74.  b may hold 3
+    right-hand sides as an (n,3) array; they are solved together, each with
+    its own stopping test.
+    """
+    if M is not None:
+        raise NotImplementedError("preconditioned CG is not part of the reference path (M must be None)")
+    solver = default_solver()
+    if not isinstance(A, DeviceCSR):
+        A = DeviceCSR.from_scipy(A)
+    b = torch.as_tensor(b, dtype=torch.float64, device=A.device).contiguous()
+    if use_init and x0 is not None:
+        x = torch.as_tensor(x0, dtype=torch.float64, device=A.device).clone().contiguous()
+    else:
+        x = torch.zeros_like(b)
+    info = new_info(1, A.device)
+    solver.launch(A, b, x, info[0], tol=tol, maxiter=maxiter, use_init=bool(use_init and x0 is not None),
+                  precision=precision)
+    d = decode_info(info[0].cpu().numpy())
+    raise_for(d, A, b, x, system=system, nrhs=1 if b.dim() == 1 else b.shape[1])
+    return x

@@ -1,0 +1,172 @@
+/*
+ * cupymag_gb300 -- C-ABI of the GB300 (sm_103a) kernels for CuPyMag's
+ * Gauss-Seidel-projection LLG time step.
+ *
+ * Every function takes plain device pointers, sizes and a cudaStream_t passed
+ * as void*; launches are asynchronous on that stream.  Functions return a
+ * status code (cpm_status); on CPM_CUDA_ERROR / CPM_BAD_ARG the message is
+ * available from cpm_last_error_string() (per calling thread).  The library
+ * never allocates user-visible memory: solvers take a caller-owned workspace
+ * whose size is given by cpm_cg_workspace_bytes().
+ *
+ * Layouts (as in the reference): a 3-vector field (n,3) and a Voigt strain
+ * (n,6) are row-major "AoS" arrays; the elastic displacement u is the block
+ * vector [ux | uy | uz] of length 3n; the eigenstrain E0 is node-interleaved
+ * (6n).  CSR matrices use int32 column indices and int32 or int64 row
+ * pointers, FP64 values (plus an optional FP32 copy of the values for the
+ * mixed-precision solver).
+ */
+#ifndef CUPYMAG_GB300_H
+#define CUPYMAG_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+  CPM_OK = 0,
+  CPM_NOT_CONVERGED = 1,   /* maxiter reached (linear_solvers.py:64-74 raises) */
+  CPM_BARRIER_TIMEOUT = 2, /* a bounded grid-barrier wait ran out */
+  CPM_NONFINITE = 3,       /* NaN/Inf met in a CG scalar */
+  CPM_BAD_ARG = 4,
+  CPM_CUDA_ERROR = 5
+} cpm_status;
+
+/* Sparse matrix in CSR form (device pointers).  vals32 may be NULL. */
+typedef struct {
+  int64_t rows, cols, nnz;
+  const void *indptr;      /* int32_t[rows+1] or int64_t[rows+1] */
+  int32_t indptr_is64;
+  const int32_t *indices;  /* int32_t[nnz], sorted per row */
+  const double *vals;      /* double[nnz] */
+  const float *vals32;     /* float[nnz] or NULL */
+} cpm_csr;
+
+/* Per-solve result written by the solvers (device memory). */
+typedef struct {
+  int32_t status;          /* cpm_status of the solve */
+  int32_t iters[3];        /* CG iterations per right-hand side */
+  int32_t outer;           /* refinement sweeps (mixed precision) */
+  int32_t pad;
+  double resid[3];         /* final ||r|| per right-hand side */
+  double bnorm[3];         /* ||b|| per right-hand side */
+} cpm_cg_info;
+
+/* Solver controls. */
+typedef struct {
+  double tol;              /* stop when ||r|| <= tol * ||b||  (cupyx cg semantics) */
+  int32_t maxiter;
+  int32_t use_init_host;   /* x holds the initial guess (if use_init_dev is NULL) */
+  const int32_t *use_init_dev; /* device flag read at launch time, or NULL */
+  int32_t precision;       /* 0 = FP64 CG, 1 = FP32 CG inside FP64 refinement */
+  double inner_tol;        /* relative tolerance of each FP32 inner solve */
+  int32_t max_outer;       /* refinement sweep limit */
+  int32_t pad;
+  double barrier_timeout_s;/* bound on every grid-barrier wait (seconds) */
+} cpm_cg_opts;
+
+/* ---- library ---- */
+const char *cpm_version(void);
+const char *cpm_last_error_string(void);
+int cpm_device_sm_count(int device);
+
+/* ---- sparse matrix-vector products ----
+ * Replaces the cupyx CSR `A @ x` used throughout the step
+ * (cupymag/core/Micromagnetics.py:123,166,217-219,227,233,280-288).
+ * y[:, k] = alpha * A x[:, k] for k < nvec (nvec 1 or 3, (n,nvec) layout). */
+int cpm_spmv_csr(const cpm_csr *A, const double *x, double *y, double alpha, int nvec, void *stream);
+
+/* Same-pattern triple product (Fx, Fy, Fz share indptr/indices).
+ * mode 0 (cupymag/utils/compute_derivatives.py:36-58, compute_Hd_from_U):
+ *      y[i, k] = alpha * (A_k x)_i,  x (n,), y (n,3).
+ * mode 1 (cupymag/core/Micromagnetics.py:166-168, demag right-hand side):
+ *      y[i] = alpha * sum_k (A_k (x[:,k] - shift[k]))_i,  y[pin] = 0 if pin >= 0,
+ *      x (n,3), shift = device double[3] or NULL, y (n,). */
+int cpm_spmv_csr_multi(const cpm_csr *A, const double *vals_y, const double *vals_z, const double *x,
+                       double *y, double alpha, int mode, const double *shift, int64_t pin, void *stream);
+
+/* ---- conjugate gradient ----
+ * Replaces cupymag/solvers/linear_solvers.py:20-74 (cupyx cg): unpreconditioned
+ * CG, x0 used only when use_init, ||b|| == 0 returns b, stop on
+ * ||r|| <= tol ||b|| checked after each update, info != 0 at maxiter.
+ * One persistent cooperative launch does SpMV, dot products and vector updates
+ * for every iteration; nrhs 1 or 3 independent right-hand sides share A
+ * ((n,nrhs) layout), each with its own scalars and stopping test. */
+size_t cpm_cg_workspace_bytes(int64_t n, int nrhs, int precision);
+int cpm_cg_solve(const cpm_csr *A, const double *b, double *x, int nrhs, const cpm_cg_opts *opts,
+                 void *workspace, size_t workspace_bytes, cpm_cg_info *info_dev, void *stream);
+
+/* ---- LLG step kernels (cupymag/core/Micromagnetics.py:110-307) ---- */
+typedef struct {
+  double K1, elasC1, elasC2, elasC3, lambda100;
+  double Nd[3];            /* demagnetisation factors */
+  double Hext[3];          /* applied field (normalised) */
+  double R[9];             /* [100] -> [111] rotation, row-major; used when rot111 */
+  int32_t rot111;
+  int32_t has_E;           /* 0: strain is identically zero (ME off) */
+} cpm_field_params;
+
+/* Effective field of Micromagnetics.py:175-215 (rot111 variant :190-211) at
+ * magnetisation mm (n,3): anisotropy + magnetoelastic terms from the strain E
+ * (n,6, or NULL when has_E = 0), half of the demag field H~ (n,3) and of
+ * H_bar = -Nd * avg_m (avg_m: device double[3]), plus Hext.  Writes the field
+ * f (n,3) when f != NULL and t = f * dt + mm (n,3). */
+int cpm_llg_field(const cpm_field_params *P, int64_t n, const double *mm, const double *E, const double *Ht,
+                  const double *avg_m, double dt, double *f, double *t, void *stream);
+
+/* Gauss-Seidel star updates (Micromagnetics.py:225-237).  g (n,3) holds
+ * (g1n, g2n, g3n), f (n,3) the field from cpm_llg_field, mstar (n,3) the star
+ * magnetisation being built:
+ *   stage 1: m1* = m1 + g2n m3 - g3n m2,   out = f1 dt + m1*  (n)
+ *   stage 2: m2* = m2 + g3n m1* - g1* m3,  out = f2 dt + m2*  (n)
+ *   stage 3: m3* = m3 + g1* m2* - g2* m1*. */
+int cpm_gs_star(int stage, int64_t n, const double *m, const double *g, const double *g1star,
+                const double *g2star, const double *f, double dt, double *mstar, double *out, void *stream);
+
+/* Renormalisation step of Micromagnetics.py:292-307: m = mss / |mss| (0 where
+ * |mss| < 1e-14), m = 0 where defect_mask[i] (uint8, may be NULL),
+ * sumsq = sum (m - m_prev)^2, m_prev = m, *use_init_dev = sumsq < thresh (if
+ * not NULL), avg_out[3] = <m> = (w . m) / volume.  scratch: device doubles,
+ * cpm_volavg_scratch_doubles() of them, zero-initialised once. */
+int cpm_renorm_sumsq(int64_t n, const double *mss, const uint8_t *defect_mask, double *m, double *m_prev,
+                     const double *w, double volume, double thresh, double *sumsq_out, double *avg_out,
+                     int32_t *use_init_dev, double *scratch, void *stream);
+
+/* Volume average (cupymag/utils/volume_average.py:155-216) in per-DOF weight
+ * form: out[c] = (sum_i w_i f[i,c]) / volume for ncomp in {1,3,6} interleaved
+ * components; with R9 != NULL (ncomp = 3) the average of f R.  The weights fold
+ * the reference's quadrature (N at Gauss points times |detJ| w) per DOF.
+ * scratch as for cpm_renorm_sumsq. */
+size_t cpm_volavg_scratch_doubles(int ncomp);
+int cpm_volavg(int64_t n, int ncomp, const double *f, const double *w, double volume, const double *R9,
+               double *out, double *scratch, void *stream);
+
+/* Magnetostrictive eigenstrain E0 (6n, node-interleaved Voigt with doubled
+ * shears), cupymag/utils/final_assembly.py:208-266.  With R9/M36 (both or
+ * neither) it is built from m100 = m R and rotated per node by M^T
+ * (Micromagnetics.py:112-119). */
+int cpm_build_E0(int64_t n, const double *m, double lam100, double lam111, const double *R9,
+                 const double *M36, double *E0, void *stream);
+
+/* Strain from displacement (cupymag/utils/compute_derivatives.py:60-125): E
+ * (n,6) from the shared-pattern derivative matrices Fx (this CSR) and the
+ * value arrays of Fy, Fz applied to u = [ux|uy|uz]; R9 (row-major 3x3) or NULL. */
+int cpm_strain_from_u(const cpm_csr *Fx, const double *vals_y, const double *vals_z, const double *u,
+                      const double *R9, double *E, void *stream);
+
+/* Micromagnetics.py:132-162: E = (E - <E>) + E_bar, then E M^{-T} when rot111.
+ * E_bar is formed on the device from <m100> (or <m> without rotation; device
+ * double[3]), lam100, lam111 and S sigma (device double[6]), rotated by M when
+ * rot111.  avgE: device double[6]; M36, MinvT36: device row-major 6x6. */
+int cpm_strain_finalize(int64_t n, double *E, const double *avgE, const double *avg_m100, double lam100,
+                        double lam111, const double *Ebar_sigma6, const double *M36, const double *MinvT36,
+                        int rot111, void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

@@ -1,0 +1,120 @@
+"""GPU parity of the LLG step against the reference's own trajectories and the oracle.
+
+Tolerance: the plain FP64 method must match the reference's DP mode within
+1e-10 relative in m and <m> (max-norm over all DOFs and components, m is a
+unit vector so absolute == relative).
+"""
+import numpy as np
+import pytest
+import torch
+
+from . import _golden as G
+
+pytestmark = pytest.mark.gpu
+
+TOL_M = 1e-10
+
+
+def _ops(g, p, assembly="auto"):
+    from cupymag_gb300.core.assemble_simulation_operators import SimulationOperators
+    from cupymag_gb300.mesh.grids import TetraGrid
+    from cupymag_gb300.utils.defect_shapes import get_defect_shape_function
+    mesh = None
+    if p.grid_type == "Tet":
+        fn = get_defect_shape_function(p.defect_shape, (p.defect_parameters, p.defect_rotation))
+        mesh = TetraGrid(coords=g["tet_coords"], tets=g["tet_tets"], defect_shape=fn)
+    return SimulationOperators(p, assembly=assembly, mesh=mesh)
+
+
+@pytest.mark.parametrize("case", G.CASES)
+@pytest.mark.parametrize("assembly", ["auto", "coo"])
+def test_step_matches_reference_trajectory(case, assembly):
+    from cupymag_gb300.physics.llg import LLGSolver
+    g = G.load(case)
+    p = G.params(g)
+    if assembly == "coo" and p.grid_type == "Tet":
+        pytest.skip("tet meshes always use the COO path")
+    S = _ops(g, p, assembly)
+    L = LLGSolver(S, p)
+    m0 = g["m0"].copy()
+    m0[g["DefDOF"]] = 0.0
+    L.set_magnetization(torch.as_tensor(m0))
+    for k in range(g["step_m"].shape[0]):
+        L.step(p.Hext)
+        L.check()
+        its = [x for x in g["step_iters"][k] if x >= 0]
+        got = L.iterations()
+        assert max(abs(a - b) for a, b in zip(got, its)) <= 1, (k, got, its)
+        m = L.m.cpu().numpy()
+        err = np.abs(m - g["step_m"][k]).max()
+        assert err <= TOL_M, (case, k, err)
+        am = L.avg_m.cpu().numpy()
+        rel = np.abs(am - g["step_avg_m"][k]).max() / np.abs(g["step_avg_m"][k]).max()
+        assert rel <= TOL_M, (case, k, rel)
+
+
+@pytest.mark.parametrize("nx,me,rot,steps", [(16, False, False, 6), (12, True, True, 4), (10, True, False, 3)])
+def test_step_matches_oracle_midsize(nx, me, rot, steps):
+    """Larger meshes than the golden cases: product GPU step vs the oracle on the same operators."""
+    from oracle.llg import LLGState, llg_step
+    from oracle.volume_average import VolumeAverage as OVA
+    from cupymag_gb300.core.assemble_simulation_operators import SimulationOperators
+    from cupymag_gb300.physics.llg import LLGSolver
+    from cupymag_gb300.utils.magnetization_io import seeded_initial_m
+    g = G.load("hex_me_rot")
+    p = G.params(g).with_(Nx=nx, Ny=nx, Nz=nx, Ndx=nx // 4, Ndy=nx // 4, Ndz=nx // 4, ME=me, rot111=rot)
+    S = SimulationOperators(p)
+    ops = S.host_operators()
+    Avg = OVA(S.node_coords_np, S.elements_np, S.global_id_np)
+    m0 = seeded_initial_m(S.n_dof, S.DefDOF, seed=5)
+    L = LLGSolver(S, p)
+    L.set_magnetization(torch.as_tensor(m0))
+    O = LLGState(m0, Avg.average)
+    for k in range(steps):
+        L.step(p.Hext)
+        L.check()
+        O.iters = []
+        llg_step(O, ops, Avg.average, p, p.Hext, S.DefDOF)
+        err = np.abs(L.m.cpu().numpy() - O.m).max()
+        assert err <= TOL_M, (k, err)
+        got = L.iterations()
+        assert max(abs(a - b) for a, b in zip(got, O.iters)) <= 1, (got, O.iters)
+
+
+def test_mixed_precision_step_error_bound():
+    """FP32 CG inside FP64 refinement: max |m - m_FP64| <= 1e-6 (stated bound), same stopping test."""
+    from cupymag_gb300.core.assemble_simulation_operators import SimulationOperators
+    from cupymag_gb300.physics.llg import LLGSolver
+    from cupymag_gb300.utils.magnetization_io import seeded_initial_m
+    g = G.load("hex_me_rot")
+    p = G.params(g).with_(Nx=16, Ny=16, Nz=16, Ndx=4, Ndy=4, Ndz=4)
+    S = SimulationOperators(p)
+    m0 = torch.as_tensor(seeded_initial_m(S.n_dof, S.DefDOF, seed=3))
+    A = LLGSolver(S, p, precision="DP")
+    B = LLGSolver(S, p, precision="IR")
+    A.set_magnetization(m0)
+    B.set_magnetization(m0)
+    for _ in range(5):
+        A.step(p.Hext)
+        B.step(p.Hext)
+        A.check()
+        B.check()
+    err = (A.m - B.m).abs().max().item()
+    rel_avg = ((A.avg_m - B.avg_m).abs().max() / A.avg_m.abs().max()).item()
+    assert err <= 1e-6 and rel_avg <= 1e-6, (err, rel_avg)
+
+
+def test_step_deterministic():
+    from cupymag_gb300.physics.llg import LLGSolver
+    g = G.load("hex_me_rot")
+    p = G.params(g)
+    S = _ops(g, p)
+    outs = []
+    for _ in range(2):
+        L = LLGSolver(S, p)
+        L.set_magnetization(torch.as_tensor(g["m0"]))
+        for _ in range(3):
+            L.step(p.Hext)
+        L.check()
+        outs.append(L.m.cpu().numpy())
+    assert np.array_equal(outs[0], outs[1])

@@ -1,0 +1,188 @@
+"""CPU tests of the host side: config loader, parameters, mesh, assembly, C-ABI exports."""
+import os
+import re
+
+import numpy as np
+import pytest
+
+from . import _golden as G
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+# ------------------------------------------------------------------ YAML subset / parameters
+def test_yaml_subset_pyyaml_resolution():
+    from cupymag_gb300.core.config_loader import safe_load
+    d = safe_load(
+        "a: 1.25e+6  # float\nb: 1e6\nc: 1.0e6\nd: 10.0e-9\ne: [[1.0, 0.0], [0, 1]]\nf: yes\ng: 'q # x'\n"
+        "h:\n  - 1\n  - k: 2\n    l: 3\ni: ~\nj: \"s\"\nk: .5\nl: -0.95\nm: 0x1f\n")
+    assert d["a"] == 1.25e6 and d["b"] == "1e6" and d["c"] == "1.0e6" and d["d"] == 10.0e-9
+    assert d["e"] == [[1.0, 0.0], [0, 1]] and d["f"] is True and d["g"] == "q # x"
+    assert d["h"] == [1, {"k": 2, "l": 3}] and d["i"] is None and d["j"] == "s" and d["k"] == 0.5
+    assert d["l"] == -0.95 and d["m"] == 31
+
+
+def test_example_config_parses(tmp_path):
+    from cupymag_gb300.core.parameters import load_parameters
+    cfg = """
+physics:
+  magnetic:
+    ms: 1.25e+6
+    exchange_stiffness: 1.0e-11
+    anisotropy_k1: 958.0
+  elastic: {c11: 240.0e+9, c12: 89.0e+9, c44: 76.0e+9}
+  magnetostriction:
+    lambda100: 10.0e-6
+    lambda111: 30.9e-6
+  demagnetization: {n_x: 0.0, n_y: 0.0, n_z: 1.0}
+  external_field: {hext1: 200.0, dhext1: 20.0, hext2: 0.01}
+  external_stress: {sigma11: 0.0}
+  rotation_111: false
+  magnetoelastic_coupling: true
+  characteristic_length: 10.0e-9
+grid:
+  type: "Hex"
+  cubic_mesh: {nx: 8, ny: 8, nz: 4, ndx: 2, ndy: 2, ndz: 2}
+simulation:
+  precision: "DP"
+  llg: {timestep: 3.0e-12, alpha_damping: 0.15, llg_accuracy_factor: 5.0e-10}
+  solver: {tolerance: 1.0e-7, max_iterations: 5000, initial_factor: 100.0}
+  restart: false
+  initial_magnetization: [1.0, 0.0, 0.0]
+  stop_condition:
+    direction: [0.8, 0.6, 0.0]
+    value: -0.95
+output:
+  directory: "out"
+"""
+    p = tmp_path / "c.yaml"
+    p.write_text(cfg)
+    P = load_parameters(p)
+    assert P.Nx == 8 and P.Nz == 4 and P.ME and not P.rot111
+    np.testing.assert_allclose(P.stop_direction, (0.8, 0.6, 0.0))
+    assert P.output_dir == str((tmp_path / "out").resolve())
+    assert P.dt == pytest.approx(3e-12 * 1.25663706127e-6 * 1.76e11 * 1.25e6 / (1 + 0.15 ** 2), rel=1e-15)
+
+
+def test_parameter_validation():
+    from cupymag_gb300.core.parameters import SimParams
+    with pytest.raises(ValueError, match="Saturation magnetization must be positive"):
+        SimParams(ms=0.0).finalize()
+    with pytest.raises(ValueError, match="Timestep must be positive"):
+        SimParams(timestep=0.0).finalize()
+
+
+@pytest.mark.parametrize("case", G.CASES)
+def test_parameters_match_reference(case):
+    g = G.load(case)
+    p = G.params(g)
+    for k in ["dt", "alpha", "K1", "elasC1", "elasC2", "elasC3", "s11", "s12", "s44"]:
+        assert getattr(p, k) == g["param_" + k], k
+
+
+# ------------------------------------------------------------------ mesh / assembly
+@pytest.mark.parametrize("case", G.CASES)
+def test_mesh_and_coo_assembly_match_reference(case):
+    from cupymag_gb300.mesh.grids import HexGrid, TetraGrid, extract_defect_dofs
+    from cupymag_gb300.physics.assembly import assemble_coo, stiffness_voigt
+    from cupymag_gb300.utils.defect_shapes import get_defect_shape_function
+    from cupymag_gb300.utils.rot_111_matrices import get_M_matrix
+    g = G.load(case)
+    p = G.params(g)
+    if p.grid_type == "Hex":
+        grid = HexGrid(p.Nx, p.Ny, p.Nz, p.Ndx, p.Ndy, p.Ndz, p.defect_center)
+    else:
+        fn = get_defect_shape_function(p.defect_shape, (p.defect_parameters, p.defect_rotation))
+        grid = TetraGrid(coords=g["tet_coords"], tets=g["tet_tets"], defect_shape=fn)
+    coords, el = grid.std_fem_mesh()
+    gid = grid.build_periodic_node_map(coords)
+    np.testing.assert_array_equal(coords, g["node_coords"])
+    np.testing.assert_array_equal(el, g["elements"])
+    np.testing.assert_array_equal(gid, g["global_id"])
+    D = extract_defect_dofs(el, gid)
+    np.testing.assert_array_equal(D, g["DefDOF"])
+    if p.grid_type == "Hex":
+        np.testing.assert_array_equal(grid.defect_dofs(), D)
+    C = stiffness_voigt(p.c11, p.c12, p.c44, get_M_matrix() if p.rot111 else None)
+    ops = assemble_coo(coords, el, gid, int(gid.max()) + 1, D, p.alpha1, p.alpha2, p.ME, C)
+    for k, A in G.matrices(g).items():
+        B = ops[k]
+        np.testing.assert_array_equal(A.indptr, B.indptr, err_msg=k)
+        np.testing.assert_array_equal(A.indices, B.indices, err_msg=k)
+        np.testing.assert_allclose(B.data, A.data, rtol=0, atol=1e-14 * np.abs(A.data).max(), err_msg=k)
+
+
+@pytest.mark.parametrize("case", ["hex_plain", "hex_me_rot", "hex_me_norot"])
+def test_structured_hex_assembly_matches_reference(case):
+    from cupymag_gb300.core.assemble_simulation_operators import SimulationOperators
+    g = G.load(case)
+    p = G.params(g)
+    ops = SimulationOperators(p, device="cpu", assembly="structured").host_operators()
+    for k, A in G.matrices(g).items():
+        B = ops[k]
+        np.testing.assert_array_equal(A.indptr, B.indptr, err_msg=k)
+        np.testing.assert_array_equal(A.indices, B.indices, err_msg=k)
+        np.testing.assert_allclose(B.data, A.data, rtol=0, atol=2e-15 * np.abs(A.data).max(), err_msg=k)
+
+
+def test_structured_equals_coo_on_larger_grid():
+    from cupymag_gb300.core.assemble_simulation_operators import SimulationOperators
+    p = G.params(G.load("hex_me_rot")).with_(Nx=7, Ny=5, Nz=9, Ndx=3, Ndy=2, Ndz=4)
+    a = SimulationOperators(p, device="cpu", assembly="structured").host_operators()
+    b = SimulationOperators(p, device="cpu", assembly="coo").host_operators()
+    for k in a:
+        np.testing.assert_array_equal(a[k].indptr, b[k].indptr, err_msg=k)
+        np.testing.assert_array_equal(a[k].indices, b[k].indices, err_msg=k)
+        np.testing.assert_allclose(a[k].data, b[k].data, rtol=0, atol=2e-15 * np.abs(b[k].data).max(), err_msg=k)
+
+
+def test_periodic_map_matches_reference_loop():
+    from oracle.mesh import tet_periodic_map
+    from cupymag_gb300.mesh.grids import TetraGrid, kuhn_tet_cube
+    coords, tets = kuhn_tet_cube(4, jitter=0.2, seed=3)
+    np.testing.assert_array_equal(TetraGrid(coords=coords, tets=tets).build_periodic_node_map(),
+                                  tet_periodic_map(coords))
+
+
+def test_nas_roundtrip(tmp_path):
+    from cupymag_gb300.mesh.grids import kuhn_tet_cube, read_nas, write_nas
+    coords, tets = kuhn_tet_cube(3, jitter=0.2, seed=1)
+    f = tmp_path / "m.nas"
+    write_nas(f, coords, tets)
+    ids, c2, eids, t2 = read_nas(f)
+    np.testing.assert_array_equal(c2, coords)
+    np.testing.assert_array_equal(t2, tets)
+    p = coords[tets]
+    assert (np.linalg.det(p[:, 1:] - p[:, :1]) > 0).all()
+
+
+def test_volume_average_weights_match_reference():
+    from cupymag_gb300.utils.volume_average import dof_weights
+    for case in G.CASES:
+        g = G.load(case)
+        w, V = dof_weights(g["node_coords"], g["elements"], g["global_id"], int(g["n"]))
+        np.testing.assert_allclose(w @ g["in_f3"] / V, g["out_avg_f3"], rtol=1e-12, atol=1e-15)
+        w2, V2 = dof_weights(g["node_coords"], g["elements"], g["global_id"], int(g["n"]),
+                             defect_flag=g["elements"][:, -1])
+        np.testing.assert_allclose(w2 @ g["in_f3"] / V2, g["out_avg_f3_nodefect"], rtol=1e-12, atol=1e-15)
+
+
+# ------------------------------------------------------------------ C-ABI
+def _header_functions():
+    txt = open(os.path.join(ROOT, "include", "cupymag_gb300.h")).read()
+    txt = re.sub(r"/\*.*?\*/", "", txt, flags=re.S)
+    return sorted(set(re.findall(r"\b(cpm_[a-z0-9_]+)\s*\(", txt)))
+
+
+def test_library_exports_every_header_symbol():
+    from cupymag_gb300 import _native as N
+    from cupymag_gb300.build import build
+    build()
+    lib = N.load()
+    names = _header_functions()
+    assert names, "no functions parsed from the header"
+    for nm in names:
+        assert hasattr(lib, nm), nm
+    assert set(names) <= set(N.EXPORTED) | {"cpm_device_sm_count"}
+    assert lib.cpm_version().startswith(b"cupymag_gb300")
+    assert lib.cpm_cg_workspace_bytes(1000, 3, 1) > lib.cpm_cg_workspace_bytes(10, 1, 1)
