@@ -26,7 +26,7 @@ dbl = C.c_double
 
 class CSR(C.Structure):
     _fields_ = [("rows", i64), ("cols", i64), ("nnz", i64), ("indptr", vp), ("indptr_is64", i32),
-                ("indices", vp), ("vals", vp), ("vals32", vp)]
+                ("indices", vp), ("vals", vp), ("vals32", vp), ("max_row_nnz", i64)]
 
 
 class CGInfo(C.Structure):

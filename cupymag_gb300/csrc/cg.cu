@@ -30,6 +30,7 @@
 #include <cstdio>
 
 #include "cpm_common.cuh"
+#include "csr_tile.cuh"
 
 namespace cpm {
 
@@ -61,6 +62,7 @@ struct CGArgs {
   cpm_cg_info *info;
   unsigned long long timeout_ns;
   int64_t rows_per_cta;
+  int group;                               // threads per row in the staged SpMV
 };
 
 // Block-wide sum of NV values per thread, deterministic; result broadcast.
@@ -120,41 +122,43 @@ __device__ __forceinline__ void set_status(cpm_cg_info *info, int st) {
 }
 
 // ------------------------------------------------------------------ FP64 CG
+// Three phases per iteration, each ended by a grid barrier:
+//   1. q = A p over staged tiles (one FP64 FMA per non-zero), partial p.q;
+//   2. x += alpha p, r -= alpha q, partial r.r;
+//   3. p = r + beta p for the CTA's own rows.
+// Forming p in its own pass (instead of r + beta p_old inside the gather)
+// keeps the FP64 work of the SpMV at one FMA per non-zero, which is what the
+// FP64 pipes of GB300 can sustain at HBM speed.
 template <int NR, typename IT>
 __global__ void __launch_bounds__(kCGThreads) cg_fp64_kernel(CGArgs<NR, IT> a) {
   __shared__ double s_red[2 * NR][kCGWarps];
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  extern __shared__ __align__(16) unsigned char s_tile[];
+  const TileSmem tile = tile_smem(s_tile);
+  const int G = a.group;
+  const int R = kCGThreads / G;
+  const bool lead = (threadIdx.x % G) == 0;
   const int64_t r0 = min(a.n, (int64_t)blockIdx.x * a.rows_per_cta);
   const int64_t r1 = min(a.n, r0 + a.rows_per_cta);
   const bool use_init = a.use_init_dev ? (__ldcg(a.use_init_dev) != 0) : (a.use_init_host != 0);
   const unsigned long long tns = a.timeout_ns;
   int par = 0;
+  double *p = a.p0;
 
-  // ---- prologue: r = b - A x (or r = b, x = 0), ||b||^2, ||r||^2
+  // ---- prologue: r = b - A x (or r = b, x = 0), p = r, ||b||^2, ||r||^2
   double v[2 * NR];
 #pragma unroll
   for (int j = 0; j < 2 * NR; ++j) v[j] = 0.0;
   if (use_init) {
-    for (int64_t row = r0 + warp; row < r1; row += kCGWarps) {
-      int64_t s, e;
-      row_range(a.rp, row, s, e);
+    for (int64_t t0 = r0; t0 < r1; t0 += R) {
       double acc[NR];
-#pragma unroll
-      for (int j = 0; j < NR; ++j) acc[j] = 0.0;
-      for (int64_t k = s + lane; k < e; k += kWarp) {
-        const double av = ld_stream(a.av + k);
-        const int c = ld_stream(a.ci + k);
-#pragma unroll
-        for (int j = 0; j < NR; ++j) acc[j] = fma(av, a.x[(int64_t)c * NR + j], acc[j]);
-      }
-#pragma unroll
-      for (int j = 0; j < NR; ++j) acc[j] = warp_sum(acc[j]);
-      if (lane == 0) {
+      const int64_t row = tile_rows<NR, IT>(a.rp, a.ci, a.av, a.x, t0, min(r1, t0 + R), G, tile, acc);
+      if (row >= 0 && lead) {
 #pragma unroll
         for (int j = 0; j < NR; ++j) {
           const double bj = a.b[row * NR + j];
           const double rj = bj - acc[j];
           a.r[row * NR + j] = rj;
+          p[row * NR + j] = rj;
           v[j] = fma(bj, bj, v[j]);
           v[NR + j] = fma(rj, rj, v[NR + j]);
         }
@@ -166,6 +170,7 @@ __global__ void __launch_bounds__(kCGThreads) cg_fp64_kernel(CGArgs<NR, IT> a) {
       for (int j = 0; j < NR; ++j) {
         const double bj = a.b[row * NR + j];
         a.r[row * NR + j] = bj;
+        p[row * NR + j] = bj;
         a.x[row * NR + j] = 0.0;
         v[j] = fma(bj, bj, v[j]);
         v[NR + j] = fma(bj, bj, v[NR + j]);
@@ -176,7 +181,7 @@ __global__ void __launch_bounds__(kCGThreads) cg_fp64_kernel(CGArgs<NR, IT> a) {
     set_status(a.info, CPM_BARRIER_TIMEOUT);
     return;
   }
-  double atol[NR], rho[NR], rho_old[NR], resid[NR];
+  double atol[NR], rho[NR], resid[NR];
   int active[NR], iters[NR];
   bool any = false;
 #pragma unroll
@@ -184,7 +189,6 @@ __global__ void __launch_bounds__(kCGThreads) cg_fp64_kernel(CGArgs<NR, IT> a) {
     const double bn = sqrt(v[j]);
     atol[j] = a.tol * bn;
     rho[j] = v[NR + j];
-    rho_old[j] = 1.0;
     resid[j] = sqrt(v[NR + j]);
     active[j] = bn != 0.0;
     iters[j] = 0;
@@ -198,51 +202,21 @@ __global__ void __launch_bounds__(kCGThreads) cg_fp64_kernel(CGArgs<NR, IT> a) {
 
   int status = CPM_OK;
   for (int k = 0; any && k < a.maxiter; ++k) {
-    double beta[NR];
+    // ---- phase 1: q = A p, partial p.q
+    double pq[NR];
 #pragma unroll
-    for (int j = 0; j < NR; ++j) beta[j] = (k == 0 || !active[j]) ? 0.0 : rho[j] / rho_old[j];
-    const double *pin = (k & 1) ? a.p1 : a.p0;
-    double *pout = (k & 1) ? a.p0 : a.p1;
-
-    // ---- phase 1: q = A (r + beta p_old), p_new, partial p.q
-#pragma unroll
-    for (int j = 0; j < NR; ++j) v[j] = 0.0;
-    for (int64_t row = r0 + warp; row < r1; row += kCGWarps) {
-      int64_t s, e;
-      row_range(a.rp, row, s, e);
+    for (int j = 0; j < NR; ++j) pq[j] = 0.0;
+    for (int64_t t0 = r0; t0 < r1; t0 += R) {
       double acc[NR];
-#pragma unroll
-      for (int j = 0; j < NR; ++j) acc[j] = 0.0;
-      if (k == 0) {
-        for (int64_t kk = s + lane; kk < e; kk += kWarp) {
-          const double av = ld_stream(a.av + kk);
-          const int64_t c = ld_stream(a.ci + kk);
-#pragma unroll
-          for (int j = 0; j < NR; ++j) acc[j] = fma(av, a.r[c * NR + j], acc[j]);
-        }
-      } else {
-        for (int64_t kk = s + lane; kk < e; kk += kWarp) {
-          const double av = ld_stream(a.av + kk);
-          const int64_t c = ld_stream(a.ci + kk);
-#pragma unroll
-          for (int j = 0; j < NR; ++j) acc[j] = fma(av, __fma_rn(beta[j], pin[c * NR + j], a.r[c * NR + j]), acc[j]);
-        }
-      }
-#pragma unroll
-      for (int j = 0; j < NR; ++j) acc[j] = warp_sum(acc[j]);
-      if (lane == 0) {
+      const int64_t row = tile_rows<NR, IT>(a.rp, a.ci, a.av, p, t0, min(r1, t0 + R), G, tile, acc);
+      if (row >= 0 && lead) {
 #pragma unroll
         for (int j = 0; j < NR; ++j) {
-          const double pn = (k == 0) ? a.r[row * NR + j] : __fma_rn(beta[j], pin[row * NR + j], a.r[row * NR + j]);
-          pout[row * NR + j] = pn;
           a.q[row * NR + j] = acc[j];
-          v[j] = fma(pn, acc[j], v[j]);
+          pq[j] = fma(p[row * NR + j], acc[j], pq[j]);
         }
       }
     }
-    double pq[NR];
-#pragma unroll
-    for (int j = 0; j < NR; ++j) pq[j] = v[j];
     if (!grid_sum<NR>(pq, a.part, par, a.bar, tns, s_red)) { status = CPM_BARRIER_TIMEOUT; break; }
     double alpha[NR];
     bool bad = false;
@@ -260,8 +234,9 @@ __global__ void __launch_bounds__(kCGThreads) cg_fp64_kernel(CGArgs<NR, IT> a) {
     for (int64_t row = r0 + threadIdx.x; row < r1; row += kCGThreads) {
 #pragma unroll
       for (int j = 0; j < NR; ++j) {
+        if (!active[j]) continue;
         const int64_t i = row * NR + j;
-        a.x[i] = __fma_rn(alpha[j], pout[i], a.x[i]);
+        a.x[i] = __fma_rn(alpha[j], p[i], a.x[i]);
         const double rn = __fma_rn(-alpha[j], a.q[i], a.r[i]);
         a.r[i] = rn;
         rr[j] = fma(rn, rn, rr[j]);
@@ -269,18 +244,32 @@ __global__ void __launch_bounds__(kCGThreads) cg_fp64_kernel(CGArgs<NR, IT> a) {
     }
     if (!grid_sum<NR>(rr, a.part, par, a.bar, tns, s_red)) { status = CPM_BARRIER_TIMEOUT; break; }
     any = false;
+    double beta[NR];
 #pragma unroll
     for (int j = 0; j < NR; ++j) {
+      beta[j] = 0.0;
       if (!active[j]) continue;
       if (!isfinite(rr[j])) bad = true;
       iters[j] += 1;
-      rho_old[j] = rho[j];
+      beta[j] = rr[j] / rho[j];
       rho[j] = rr[j];
       resid[j] = sqrt(rr[j]);
       if (resid[j] <= atol[j]) active[j] = 0;
       any |= active[j] != 0;
     }
     if (bad) { status = CPM_NONFINITE; break; }
+    if (!any || k + 1 >= a.maxiter) break;
+
+    // ---- phase 3: p = r + beta p (own rows)
+    for (int64_t row = r0 + threadIdx.x; row < r1; row += kCGThreads) {
+#pragma unroll
+      for (int j = 0; j < NR; ++j) {
+        if (!active[j]) continue;
+        const int64_t i = row * NR + j;
+        p[i] = __fma_rn(beta[j], p[i], a.r[i]);
+      }
+    }
+    if (!grid_sync(a.bar, gridDim.x, tns)) { status = CPM_BARRIER_TIMEOUT; break; }
   }
   if (blockIdx.x == 0 && threadIdx.x == 0) {
     int st = status;
@@ -584,7 +573,9 @@ static int launch_cg(const cpm_csr *A, const double *b, double *x, const cpm_cg_
   const double tmo = o->barrier_timeout_s > 0 ? o->barrier_timeout_s : 2.0;
   a.timeout_ns = (unsigned long long)(tmo * 1e9);
 
-  const void *fn = (o->precision == 0) ? (const void *)cg_fp64_kernel<NR, IT> : (const void *)cg_ir_kernel<NR, IT>;
+  const bool fp64 = o->precision == 0;
+  const void *fn = fp64 ? (const void *)cg_fp64_kernel<NR, IT> : (const void *)cg_ir_kernel<NR, IT>;
+  const int smem = fp64 ? kTileSmemBytes : 0;
   static int cached_dev[2][2][2] = {};
   static int cached_occ[2][2][2] = {};
   const int dev = device_id();
@@ -592,8 +583,9 @@ static int launch_cg(const cpm_csr *A, const double *b, double *x, const cpm_cg_
   int &occ = cached_occ[pi][ri][ii];
   int &occ_dev = cached_dev[pi][ri][ii];
   if (occ == 0 || occ_dev != dev + 1) {
+    if (smem) CPM_TRY(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
     int blocks = 0;
-    CPM_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, fn, kCGThreads, 0));
+    CPM_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, fn, kCGThreads, smem));
     occ = blocks;
     occ_dev = dev + 1;
   }
@@ -601,6 +593,8 @@ static int launch_cg(const cpm_csr *A, const double *b, double *x, const cpm_cg_
     set_error("cg: kernel cannot be resident on an SM");
     return CPM_CUDA_ERROR;
   }
+  int64_t maxrow = A->max_row_nnz > 0 ? A->max_row_nnz : (A->nnz + A->rows - 1) / (A->rows > 0 ? A->rows : 1);
+  a.group = group_size(maxrow, kCGThreads);
   int64_t gmax = (int64_t)occ * sm_count();
   if (gmax > kMaxGrid) gmax = kMaxGrid;
   // at least ~64 rows per CTA so small systems do not pay for idle CTAs at barriers
@@ -616,7 +610,7 @@ static int launch_cg(const cpm_csr *A, const double *b, double *x, const cpm_cg_
   CPM_TRY(cudaMemsetAsync(w.bar, 0, sizeof(GridBarrier), st));
   CPM_TRY(cudaMemsetAsync(info, 0, sizeof(cpm_cg_info), st));
   void *args[] = {&a};
-  CPM_TRY(cudaLaunchCooperativeKernel(fn, dim3((unsigned)G), dim3(kCGThreads), args, 0, st));
+  CPM_TRY(cudaLaunchCooperativeKernel(fn, dim3((unsigned)G), dim3(kCGThreads), args, smem, st));
   return CPM_OK;
 }
 

@@ -11,6 +11,7 @@
 // given n and GPU, fixed-order block trees, and the last CTA to finish sums the
 // per-CTA partials in CTA order.
 #include "cpm_common.cuh"
+#include "csr_tile.cuh"
 
 namespace cpm {
 
@@ -299,34 +300,37 @@ __global__ void __launch_bounds__(kEwThreads) e0_kernel(int64_t n, const double 
 // ------------------------------------------------------------ strain from u
 // compute_derivatives.py:60-125: nine products D_a u_b from the shared-pattern
 // matrices (Fx, Fy, Fz), combined into Voigt strain (optionally rotated by R).
+// Staged tiles, G threads per row, nine FP64 FMAs per non-zero.
+constexpr int kStrainThreads = 256;
+
 template <typename IT>
-__global__ void __launch_bounds__(kEwThreads) strain_kernel(int64_t n, const IT *__restrict__ rp,
-                                                            const int *__restrict__ ci,
-                                                            const double *__restrict__ ax,
-                                                            const double *__restrict__ ay,
-                                                            const double *__restrict__ az,
-                                                            const double *__restrict__ u, const double *R9,
-                                                            double *__restrict__ E) {
-  const int lane = threadIdx.x & 31;
-  const int64_t w0 = (int64_t)blockIdx.x * (kEwThreads / kWarp) + (threadIdx.x >> 5);
-  const int64_t ws = (int64_t)gridDim.x * (kEwThreads / kWarp);
-  for (int64_t row = w0; row < n; row += ws) {
-    const int64_t s = (int64_t)__ldg(rp + row), e = (int64_t)__ldg(rp + row + 1);
+__global__ void __launch_bounds__(kStrainThreads) strain_kernel(int64_t n, const IT *__restrict__ rp,
+                                                                const int *__restrict__ ci,
+                                                                const double *__restrict__ ax,
+                                                                const double *__restrict__ ay,
+                                                                const double *__restrict__ az,
+                                                                const double *__restrict__ u, const double *R9,
+                                                                double *__restrict__ E, int G) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  const MultiTile<3> t = multi_tile_smem<3>(smem);
+  const int R = kStrainThreads / G;
+  const double *vals[3] = {ax, ay, az};
+  const int64_t ntiles = (n + R - 1) / R;
+  for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+    const int64_t t0 = tile * R, t1 = min(n, t0 + R);
     double d[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};  // d[a][b] = (D_a u_b)_row
-    for (int64_t k = s + lane; k < e; k += kWarp) {
-      const int64_t c = ld_stream(ci + k);
-      const double v[3] = {ld_stream(ax + k), ld_stream(ay + k), ld_stream(az + k)};
+    const int64_t row = visit_tile<3, IT>(rp, ci, vals, t0, t1, G, t, [&](const double (&v)[3], int64_t c) {
       const double uu[3] = {__ldg(u + c), __ldg(u + n + c), __ldg(u + 2 * n + c)};
 #pragma unroll
       for (int a = 0; a < 3; ++a)
 #pragma unroll
         for (int b = 0; b < 3; ++b) d[a][b] = __fma_rn(v[a], uu[b], d[a][b]);
-    }
+    });
 #pragma unroll
     for (int a = 0; a < 3; ++a)
 #pragma unroll
-      for (int b = 0; b < 3; ++b) d[a][b] = warp_sum(d[a][b]);
-    if (lane == 0) {
+      for (int b = 0; b < 3; ++b) d[a][b] = group_sum(d[a][b], G);
+    if (row >= 0 && (threadIdx.x % G) == 0) {
       double out[6];
       if (!R9) {
         out[0] = d[0][0];
@@ -350,6 +354,7 @@ __global__ void __launch_bounds__(kEwThreads) strain_kernel(int64_t n, const IT 
 #pragma unroll
       for (int c = 0; c < 6; ++c) E[6 * row + c] = out[c];
     }
+    __syncthreads();
   }
 }
 
@@ -501,16 +506,28 @@ extern "C" int cpm_strain_from_u(const cpm_csr *Fx, const double *vals_y, const 
   }
   const int64_t n = Fx->rows;
   if (n <= 0) return CPM_OK;
-  int64_t g = (n + (kEwThreads / kWarp) - 1) / (kEwThreads / kWarp);
-  const int64_t cap = (int64_t)sm_count() * 16;
-  if (g > cap) g = cap;
+  const int64_t mr = Fx->max_row_nnz > 0 ? Fx->max_row_nnz : (Fx->nnz + n - 1) / n;
+  const int G = group_size_cap(mr, kStrainThreads, multi_cap<3>());
+  const int64_t tiles = (n + kStrainThreads / G - 1) / (kStrainThreads / G);
   cudaStream_t st = (cudaStream_t)stream;
+  const void *fn = Fx->indptr_is64 ? (const void *)strain_kernel<int64_t> : (const void *)strain_kernel<int32_t>;
+  static int occ = 0;
+  if (occ == 0) {
+    cudaFuncSetAttribute((const void *)strain_kernel<int64_t>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         kTileSmemBytes);
+    cudaFuncSetAttribute((const void *)strain_kernel<int32_t>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         kTileSmemBytes);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fn, kStrainThreads, kTileSmemBytes);
+    if (occ < 1) occ = 1;
+  }
+  int64_t g = (int64_t)occ * sm_count();
+  if (g > tiles) g = tiles;
   if (Fx->indptr_is64)
-    strain_kernel<int64_t><<<(int)g, kEwThreads, 0, st>>>(n, (const int64_t *)Fx->indptr, Fx->indices, Fx->vals,
-                                                          vals_y, vals_z, u, R9, E);
+    strain_kernel<int64_t><<<(int)g, kStrainThreads, kTileSmemBytes, st>>>(
+        n, (const int64_t *)Fx->indptr, Fx->indices, Fx->vals, vals_y, vals_z, u, R9, E, G);
   else
-    strain_kernel<int32_t><<<(int)g, kEwThreads, 0, st>>>(n, (const int32_t *)Fx->indptr, Fx->indices, Fx->vals,
-                                                          vals_y, vals_z, u, R9, E);
+    strain_kernel<int32_t><<<(int)g, kStrainThreads, kTileSmemBytes, st>>>(
+        n, (const int32_t *)Fx->indptr, Fx->indices, Fx->vals, vals_y, vals_z, u, R9, E, G);
   return check_launch("cpm_strain_from_u");
 }
 

@@ -59,6 +59,12 @@ class DeviceCSR:
         return self
 
     @property
+    def max_row_nnz(self) -> int:
+        if getattr(self, "_max_row", None) is None:
+            self._max_row = int((self.indptr[1:] - self.indptr[:-1]).max().item()) if self.shape[0] else 0
+        return self._max_row
+
+    @property
     def nnz(self) -> int:
         return int(self.data.numel())
 
@@ -83,6 +89,7 @@ class DeviceCSR:
             s.indices = self.indices.data_ptr()
             s.vals = self.data.data_ptr()
             s.vals32 = self.data32.data_ptr() if self.data32 is not None else None
+            s.max_row_nnz = self.max_row_nnz
             self._struct = s
         return self._struct
 

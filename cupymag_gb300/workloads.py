@@ -46,6 +46,7 @@ def hex_params(n, defect, ME, rot111, **kw) -> SimParams:
 WORKLOADS = {
     "hex32_plain": dict(n=32, defect=4, ME=False, rot111=False, steps=500, B0=0.1),
     "hex128_me": dict(n=128, defect=16, ME=True, rot111=True, steps=500, B0=0.1),
+    "hex64_me": dict(n=64, defect=8, ME=True, rot111=True, steps=500, B0=0.1),
     "hex256_plain": dict(n=256, defect=32, ME=False, rot111=True, steps=200, B0=0.1),
     "hex192_me": dict(n=192, defect=24, ME=True, rot111=True, steps=200, B0=0.1),
 }

@@ -43,6 +43,7 @@ typedef struct {
   const int32_t *indices;  /* int32_t[nnz], sorted per row */
   const double *vals;      /* double[nnz] */
   const float *vals32;     /* float[nnz] or NULL */
+  int64_t max_row_nnz;     /* longest row (0: unknown; sets the rows-per-thread-group split) */
 } cpm_csr;
 
 /* Per-solve result written by the solvers (device memory). */

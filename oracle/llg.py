@@ -234,3 +234,35 @@ def fixed_sweep_fields(p, steps, B0):
         H1 = (B0 - 2.0 * B0 * frac) / from_mu0
         out.append((H1 / p.ms, 0.0, 0.0))
     return out
+
+
+def run_driver(p, ops, Avg, defect, m0, max_steps=100000):
+    """The reference's convergence-driven field sweep (Micromagnetics.py:76-347).
+
+    Returns the hysteresis rows [Hext1, Hext2, Hext3, <m1>, <m2>, <m3>] (H in
+    A/m) written at every convergence/save event and at the end, and the final m.
+    """
+    n = m0.shape[0]
+    S = LLGState(m0, Avg)
+    llg_min_step = 10 if p.ME else 100
+    LLG_accuracy = n * p.LLG_accuracy_factor
+    Hext = list(p.Hext)
+    dH = list(p.dHext)
+    stop = np.asarray(p.stop_direction, dtype=np.float64)
+    rows = []
+    nstep = 0
+    total = 0
+    while S.avg_m @ stop > p.stop_value and total < max_steps:
+        nstep += 1
+        total += 1
+        llg_step(S, ops, Avg, p, tuple(Hext), defect)
+        conv = S.sumsq < LLG_accuracy and nstep > llg_min_step
+        if conv or nstep % p.save_frequency == 0:
+            rows.append([float(f"{Hext[0] * p.ms:.1f}"), float(f"{Hext[1] * p.ms:.1f}"),
+                         float(f"{Hext[2] * p.ms:.1f}"), *S.avg_m])
+        if conv:
+            Hext = [h - d for h, d in zip(Hext, dH)]
+            nstep = 0
+    rows.append([float(f"{Hext[0] * p.ms:.1f}"), float(f"{Hext[1] * p.ms:.1f}"), float(f"{Hext[2] * p.ms:.1f}"),
+                 *S.avg_m])
+    return np.array(rows), S.m, total

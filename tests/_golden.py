@@ -7,6 +7,7 @@ import scipy.sparse as sp
 
 GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 CASES = ["hex_plain", "hex_me_rot", "hex_me_norot", "tet_me_rot"]
+DRIVER = "hex_driver"
 
 
 def load(name):

@@ -118,3 +118,18 @@ def test_step_deterministic():
         L.check()
         outs.append(L.m.cpu().numpy())
     assert np.array_equal(outs[0], outs[1])
+
+
+def test_driver_sweep_matches_reference_main(tmp_path):
+    """GPU run of the reference's convergence-driven field sweep (4^3, to the stop condition)."""
+    from cupymag_gb300.core.Micromagnetics import run
+    g = G.load(G.DRIVER)
+    p = G.params(g).with_(output_dir=str(tmp_path))
+    res = run(p, verbose=False)
+    rows = np.loadtxt(tmp_path / "hysteresis.txt", skiprows=1)
+    ref = g["hysteresis"]
+    assert rows.shape == ref.shape
+    np.testing.assert_array_equal(rows[:, :3], ref[:, :3])
+    # stable branches track to rounding; the last row follows the switching event
+    np.testing.assert_allclose(rows[:-1, 3:], ref[:-1, 3:], rtol=0, atol=1e-10)
+    np.testing.assert_allclose(rows[-1, 3:], ref[-1, 3:], rtol=0, atol=1e-6)

@@ -131,3 +131,21 @@ def test_llg_steps(case):
         assert err <= 1e-14, (k, err)
         np.testing.assert_allclose(S.avg_m, g["step_avg_m"][k], rtol=0, atol=1e-13)
         np.testing.assert_allclose(S.E, g["step_E"][k], rtol=0, atol=1e-12 * max(1.0, np.abs(g["step_E"][k]).max()))
+
+
+def test_driver_sweep_matches_reference_main():
+    """The reference's own convergence-driven sweep (main() run to its stop condition)."""
+    from oracle.llg import run_driver
+    g = G.load("hex_driver")
+    p = G.params(g)
+    ops = G.matrices(g)
+    coords, el, gid = oracle_mesh(g, p)
+    Avg = VolumeAverage(coords, el, gid)
+    n = int(g["n"])
+    v = np.asarray(p.initial_magnetization, dtype=np.float64)
+    m0 = np.tile(v / np.linalg.norm(v), (n, 1))
+    m0[g["DefDOF"]] = 0.0
+    rows, m, steps = run_driver(p, ops, Avg.average, g["DefDOF"], m0)
+    np.testing.assert_array_equal(rows[:, :3], g["hysteresis"][:, :3])
+    np.testing.assert_allclose(rows[:, 3:], g["hysteresis"][:, 3:], rtol=0, atol=1e-14)
+    np.testing.assert_allclose(m, g["final_m"], rtol=0, atol=1e-14)
