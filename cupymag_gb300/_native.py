@@ -54,6 +54,7 @@ _PROTOS = {
     "cpm_spmv_csr_multi": (C.c_int, [C.POINTER(CSR), vp, vp, vp, vp, dbl, C.c_int, vp, i64, vp]),
     "cpm_cg_workspace_bytes": (C.c_size_t, [i64, C.c_int, C.c_int]),
     "cpm_cg_solve": (C.c_int, [C.POINTER(CSR), vp, vp, C.c_int, C.POINTER(CGOpts), vp, C.c_size_t, vp, vp]),
+    "cpm_cg_solve_noalloc": (C.c_int, [C.POINTER(CSR), vp, vp, C.c_int, C.POINTER(CGOpts), vp, vp]),
     "cpm_llg_field": (C.c_int, [C.POINTER(FieldParams), i64, vp, vp, vp, vp, dbl, vp, vp, vp]),
     "cpm_gs_star": (C.c_int, [C.c_int, i64, vp, vp, vp, vp, vp, dbl, vp, vp, vp]),
     "cpm_renorm_sumsq": (C.c_int, [i64, vp, vp, vp, vp, vp, dbl, dbl, vp, vp, vp, vp, vp]),

@@ -28,6 +28,7 @@
 // inner_tol relative, x += d, until ||b - A64 x|| <= tol ||b||.
 #include <cmath>
 #include <cstdio>
+#include <mutex>
 
 #include "cpm_common.cuh"
 #include "csr_tile.cuh"
@@ -620,33 +621,34 @@ extern "C" size_t cpm_cg_workspace_bytes(int64_t n, int nrhs, int precision) {
   return cpm::layout(n, nrhs, precision ? 1 : 0, nullptr, nullptr);
 }
 
-extern "C" int cpm_cg_solve(const cpm_csr *A, const double *b, double *x, int nrhs, const cpm_cg_opts *opts,
-                            void *workspace, size_t workspace_bytes, cpm_cg_info *info_dev, void *stream) {
-  using namespace cpm;
+namespace cpm {
+
+static int solve_impl(const cpm_csr *A, const double *b, double *x, int nrhs, const cpm_cg_opts *opts,
+                      void *workspace, size_t workspace_bytes, cpm_cg_info *info_dev, void *stream, const char *who) {
   if (!A || !b || !x || !opts || !workspace || !info_dev) {
-    set_error("cpm_cg_solve: null argument");
+    set_error("%s: null argument", who);
     return CPM_BAD_ARG;
   }
   if (nrhs != 1 && nrhs != 3) {
-    set_error("cpm_cg_solve: nrhs must be 1 or 3 (got %d)", nrhs);
+    set_error("%s: nrhs must be 1 or 3 (got %d)", who, nrhs);
     return CPM_BAD_ARG;
   }
   if (A->rows != A->cols) {
-    set_error("cpm_cg_solve: matrix must be square (%lld x %lld)", (long long)A->rows, (long long)A->cols);
+    set_error("%s: matrix must be square (%lld x %lld)", who, (long long)A->rows, (long long)A->cols);
     return CPM_BAD_ARG;
   }
   const int prec = opts->precision ? 1 : 0;
   if (prec == 1 && !A->vals32) {
-    set_error("cpm_cg_solve: mixed precision needs the FP32 copy of the values (vals32)");
+    set_error("%s: mixed precision needs the FP32 copy of the values (vals32)", who);
     return CPM_BAD_ARG;
   }
   if (opts->maxiter < 0) {
-    set_error("cpm_cg_solve: maxiter must be >= 0");
+    set_error("%s: maxiter must be >= 0", who);
     return CPM_BAD_ARG;
   }
   const size_t need = layout(A->rows, nrhs, prec, nullptr, nullptr);
   if (workspace_bytes < need) {
-    set_error("cpm_cg_solve: workspace too small (%zu < %zu bytes)", workspace_bytes, need);
+    set_error("%s: workspace too small (%zu < %zu bytes)", who, workspace_bytes, need);
     return CPM_BAD_ARG;
   }
   if (A->rows == 0) return CPM_OK;
@@ -659,4 +661,66 @@ extern "C" int cpm_cg_solve(const cpm_csr *A, const double *b, double *x, int nr
   }
   return nrhs == 1 ? launch_cg<1, int32_t>(A, b, x, opts, w, info_dev, st)
                    : launch_cg<3, int32_t>(A, b, x, opts, w, info_dev, st);
+}
+
+// ---------------------------------------------------------------- no-allocation variant
+// Scratch of cpm_cg_solve_noalloc: a fixed array in device memory that exists
+// in every context that loads this library, for the life of the process.
+// 32 MiB holds the FP64 solver's four vectors for n * nrhs up to about 1.03
+// million (FP32-refinement form: five float vectors, about 1.65 million).
+constexpr size_t kNoAllocScratchBytes = size_t(32) << 20;
+static __device__ __align__(256) unsigned char g_cg_noalloc_scratch[kNoAllocScratchBytes];
+
+constexpr int kMaxDevices = 64;
+static std::mutex g_noalloc_mu;
+static void *g_noalloc_ptr[kMaxDevices] = {};
+
+// Device address of the scratch array on the current device.  The first call
+// on a device resolves it with cudaGetSymbolAddress (with that device current)
+// and caches it; later calls only read the cache.
+static int noalloc_scratch(void **out) {
+  int dev = 0;
+  CPM_TRY(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= kMaxDevices) {
+    set_error("cpm_cg_solve_noalloc: device ordinal %d out of range", dev);
+    return CPM_BAD_ARG;
+  }
+  std::lock_guard<std::mutex> lock(g_noalloc_mu);
+  if (g_noalloc_ptr[dev] == nullptr) {
+    void *ptr = nullptr;
+    const cudaError_t e = cudaGetSymbolAddress(&ptr, g_cg_noalloc_scratch);
+    if (e != cudaSuccess || ptr == nullptr) {
+      set_error("cpm_cg_solve_noalloc: cudaGetSymbolAddress failed: %s", cudaGetErrorString(e));
+      return CPM_CUDA_ERROR;
+    }
+    g_noalloc_ptr[dev] = ptr;
+  }
+  *out = g_noalloc_ptr[dev];
+  return CPM_OK;
+}
+
+}  // namespace cpm
+
+extern "C" int cpm_cg_solve(const cpm_csr *A, const double *b, double *x, int nrhs, const cpm_cg_opts *opts,
+                            void *workspace, size_t workspace_bytes, cpm_cg_info *info_dev, void *stream) {
+  return cpm::solve_impl(A, b, x, nrhs, opts, workspace, workspace_bytes, info_dev, stream, "cpm_cg_solve");
+}
+
+extern "C" int cpm_cg_solve_noalloc(const cpm_csr *A, const double *b, double *x, int nrhs, const cpm_cg_opts *opts,
+                                    cpm_cg_info *info_dev, void *stream) {
+  using namespace cpm;
+  if (!A || !opts) {
+    set_error("cpm_cg_solve_noalloc: null argument");
+    return CPM_BAD_ARG;
+  }
+  const size_t need = layout(A->rows, nrhs == 3 ? 3 : 1, opts->precision ? 1 : 0, nullptr, nullptr);
+  if (need > kNoAllocScratchBytes) {
+    set_error("cpm_cg_solve_noalloc: this solve needs %zu bytes of scratch but the built-in array holds %zu "
+              "(n * nrhs up to about 1.03 million in FP64); use cpm_cg_solve with a workspace instead",
+              need, kNoAllocScratchBytes);
+    return CPM_BAD_ARG;
+  }
+  void *ws = nullptr;
+  if (int s = noalloc_scratch(&ws)) return s;
+  return solve_impl(A, b, x, nrhs, opts, ws, kNoAllocScratchBytes, info_dev, stream, "cpm_cg_solve_noalloc");
 }

@@ -100,6 +100,25 @@ size_t cpm_cg_workspace_bytes(int64_t n, int nrhs, int precision);
 int cpm_cg_solve(const cpm_csr *A, const double *b, double *x, int nrhs, const cpm_cg_opts *opts,
                  void *workspace, size_t workspace_bytes, cpm_cg_info *info_dev, void *stream);
 
+/* Same solve as cpm_cg_solve, for callers that cannot allocate device memory:
+ * code that runs while another component owns all allocation (a fixed memory
+ * arena or pool handed out by a host application, an embedding that forbids
+ * cudaMalloc after start-up), or that must not add allocation calls to a path
+ * it has already sized.  It takes no workspace: its scratch is a fixed 32 MiB
+ * array in device memory, built into this library, which every GPU that loads
+ * the library holds until the process exits.  It calls no cudaMalloc,
+ * cudaFree or allocating library routine.  The limit is about 1.03 million
+ * values of n * nrhs in FP64 (1.65 million in the FP32-refinement form); larger
+ * solves are rejected with CPM_BAD_ARG and a message.  The first call on each
+ * device looks up the array's device address (cudaGetSymbolAddress) with that
+ * device current; make that first call before any stream capture.  All calls
+ * share the one array and it keeps the last call's contents (the solver clears
+ * what must start at zero), so calls whose kernels overlap on the GPU -- on
+ * different streams or different host threads -- race and give wrong results.
+ * No counterpart in the reference. */
+int cpm_cg_solve_noalloc(const cpm_csr *A, const double *b, double *x, int nrhs, const cpm_cg_opts *opts,
+                         cpm_cg_info *info_dev, void *stream);
+
 /* ---- LLG step kernels (cupymag/core/Micromagnetics.py:110-307) ---- */
 typedef struct {
   double K1, elasC1, elasC2, elasC3, lambda100;
