@@ -117,6 +117,19 @@ def spmv_bytes(A, nvec):
     return A.nnz * (8 + 4) + (A.shape[0] + 1) * ip + nvec * (A.shape[1] * 8 + A.shape[0] * 8)
 
 
+def stencil_launch_bytes(A, nvec, iters, outer, fp32):
+    """Algorithmic bytes of a matrix-free CG launch: vector passes only (flags and coefficients are cached).
+
+    FP64 CG: 88 B per unknown and iteration (q = A p: read p, write q; x, r update: read 4, write 2;
+    p update: read 2, write 1).  FP32 inner iterations: 44 B; each FP64 refinement sweep: 48 B
+    (residual: read x, b, write r, p, d in FP32; x += d).
+    """
+    u = A.shape[0] * nvec
+    if fp32:
+        return u * (44 * iters + 48 * max(outer, 1))
+    return u * (88 * iters + 24)
+
+
 def cg_launch_bytes(A, nvec, iters, warm):
     n = A.shape[0]
     per_it = spmv_bytes(A, nvec) + 6 * n * 8 * nvec
@@ -188,7 +201,8 @@ def run_ours(args):
     p, w = workload(args.workload)
     t_setup = time.perf_counter()
     S = SimulationOperators(p)
-    L = LLGSolver(S, p, precision=args.precision)
+    ops_kind = args.operators or ("csr" if args.precision == "DP" else "stencil")
+    L = LLGSolver(S, p, precision=args.precision, operators=ops_kind)
     torch.cuda.synchronize()
     t_setup = time.perf_counter() - t_setup
     m0 = seeded_m0(S.n_dof, S.DefDOF, seed=1234 + rank)
@@ -251,7 +265,10 @@ def run_ours(args):
         inf = decode_info(info_hist[s][k].cpu().numpy())
         warm = bool(warm_hist[s].item())
         its = max(inf["iters"][:nv])
-        b = cg_launch_bytes(A, nv, its, warm)
+        if hasattr(A, "ncomp"):
+            b = stencil_launch_bytes(A, nv, its, inf["outer"], args.precision != "DP")
+        else:
+            b = cg_launch_bytes(A, nv, its, warm)
         d = e0.elapsed_time(e1)
         tot_bytes += b
         tot_ms += d
@@ -269,7 +286,9 @@ def run_ours(args):
     its_mean = [float(np.mean([r[j] for r in its_step])) for j in range(len(its_step[0]))]
     peak, peak_kind = peaks()
     achieved = tot_bytes / (tot_ms / 1e3) / 1e9
-    roof = {"kernel": "cg_fp64_kernel" if args.precision == "DP" else "cg_ir_kernel", "bound": "hbm",
+    kname = {("csr", "DP"): "cg_fp64_kernel", ("csr", "IR"): "cg_ir_kernel",
+             ("stencil", "DP"): "cg_stencil_fp64_kernel", ("stencil", "IR"): "cg_stencil_ir_kernel"}[(ops_kind, args.precision)]
+    roof = {"kernel": kname, "bound": "hbm",
             "achieved": round(achieved, 1), "peak": peak, "peak_kind": peak_kind, "unit": "GB/s",
             "frac": round(achieved / peak, 4), "traffic": None,
             "share_of_step": round(tot_ms / ms, 4),
@@ -316,11 +335,11 @@ def run_ours(args):
             "data": "synthetic (seeded m0 = normalise((1,0,0)+N(0,1e-3)), fixed field sweep)",
             "config": {"workload": args.workload, "mesh": f"hex {w['n']}^3 periodic, defect {w['defect']}^3",
                        "n_dof": S.n_dof, "magnetoelastic": w["ME"], "rot111": w["rot111"],
-                       "precision": args.precision, "tol": p.tol, "sweep": f"+{w['B0']} T -> -{w['B0']} T over "
+                       "precision": args.precision, "operators": ops_kind, "tol": p.tol, "sweep": f"+{w['B0']} T -> -{w['B0']} T over "
                        f"{w['steps']} steps", "timed_steps": f"{args.warmup}..{args.warmup + args.steps - 1}",
                        "l2": "inputs larger than L2 (operators %.1f GB resident)" % (
-                           sum(x.nbytes() for x in [L.A_demag, L.A1, L.A2, L.F1, L.Fx] +
-                               ([L.A_el, L.F_el] if L.ME else [])) / 1e9),
+                           sum(x.nbytes() for x in [L.A_demag, L.A1, L.A2, L.F1, L.Fx, L.F_el] +
+                               ([L.A_el] if L.ME else []) if hasattr(x, "nbytes")) / 1e9),
                        "parallelism": f"replicas x{world}", "setup_s": round(t_setup, 1),
                        "cg_iterations_per_step": [round(x, 1) for x in its_mean]},
             "e2e": {"value": round(e2e_value, 4), "unit": "steps/s",
@@ -380,6 +399,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--workload", default="hex128_me")
     ap.add_argument("--precision", default="DP", choices=["DP", "IR"])
+    ap.add_argument("--operators", default=None, choices=["csr", "stencil"],
+                    help="solved operators as CSR or matrix-free stencils (default: csr for DP, stencil for IR)")
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()

@@ -29,6 +29,11 @@ class CSR(C.Structure):
                 ("indices", vp), ("vals", vp), ("vals32", vp), ("max_row_nnz", i64)]
 
 
+class Stencil(C.Structure):
+    _fields_ = [("nx", i32), ("ny", i32), ("nz", i32), ("ncomp", i32), ("coef", vp), ("coef32", vp),
+                ("flags", vp)]
+
+
 class CGInfo(C.Structure):
     _fields_ = [("status", i32), ("iters", i32 * 3), ("outer", i32), ("pad", i32), ("resid", dbl * 3),
                 ("bnorm", dbl * 3)]
@@ -55,6 +60,9 @@ _PROTOS = {
     "cpm_cg_workspace_bytes": (C.c_size_t, [i64, C.c_int, C.c_int]),
     "cpm_cg_solve": (C.c_int, [C.POINTER(CSR), vp, vp, C.c_int, C.POINTER(CGOpts), vp, C.c_size_t, vp, vp]),
     "cpm_cg_solve_noalloc": (C.c_int, [C.POINTER(CSR), vp, vp, C.c_int, C.POINTER(CGOpts), vp, vp]),
+    "cpm_stencil_apply": (C.c_int, [C.POINTER(Stencil), vp, vp, dbl, C.c_int, vp]),
+    "cpm_cg_solve_stencil": (C.c_int, [C.POINTER(Stencil), vp, vp, C.c_int, C.POINTER(CGOpts), vp, C.c_size_t, vp,
+                                       vp]),
     "cpm_llg_field": (C.c_int, [C.POINTER(FieldParams), i64, vp, vp, vp, vp, dbl, vp, vp, vp]),
     "cpm_gs_star": (C.c_int, [C.c_int, i64, vp, vp, vp, vp, vp, dbl, vp, vp, vp]),
     "cpm_renorm_sumsq": (C.c_int, [i64, vp, vp, vp, vp, vp, dbl, dbl, vp, vp, vp, vp, vp]),

@@ -77,7 +77,7 @@ def run(params, fields=None, max_steps=None, precision=None, verbose=True, devic
         if converged or nstep % p.save_frequency == 0:
             count += 1
             hyst.write(f"{Hext[0] * p.ms:.1f}\t{Hext[1] * p.ms:.1f}\t{Hext[2] * p.ms:.1f}\t"
-                       f"{avg_m[0]!r}\t{avg_m[1]!r}\t{avg_m[2]!r}\n")
+                       f"{float(avg_m[0])!r}\t{float(avg_m[1])!r}\t{float(avg_m[2])!r}\n")
             if p.write_m:
                 write_array(L.m, os.path.join(out_dir, "last_m.h5"))
             if nstep >= 5000 and verbose:
@@ -90,7 +90,7 @@ def run(params, fields=None, max_steps=None, precision=None, verbose=True, devic
             nstep = 0
             count = 0
     hyst.write(f"{Hext[0] * p.ms:.1f}\t{Hext[1] * p.ms:.1f}\t{Hext[2] * p.ms:.1f}\t"
-               f"{avg_m[0]!r}\t{avg_m[1]!r}\t{avg_m[2]!r}\n")
+               f"{float(avg_m[0])!r}\t{float(avg_m[1])!r}\t{float(avg_m[2])!r}\n")
     hyst.close()
     if p.write_m:
         write_array(L.m, os.path.join(out_dir, "last_m.h5"))

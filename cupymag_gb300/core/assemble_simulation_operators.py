@@ -149,6 +149,25 @@ class SimulationOperators:
         ops = self._coo()
         return DeviceCSR.from_scipy(ops["A_el"], self.device), DeviceCSR.from_scipy(ops["F_el"], self.device)
 
+    def stencil_operators(self):
+        """Matrix-free forms of A_demag, A1, A2, F1 (and A_el with ME) for structured hex grids."""
+        from ..utils.stencil_operator import COL_EXCLUDED, ROW_IDENTITY, ROW_ZERO, StencilOperator
+        if not self.structured:
+            raise ValueError("stencil operators need a structured hex grid (at least 3 cells per axis)")
+        g, e, n = self.fem_grid, self._cell(), self.n_dof
+        st = lambda K: SH.stencil_from_element(K).reshape(-1)  # noqa: E731
+        mk = lambda coef, flags=None: StencilOperator(g.Nx, g.Ny, g.Nz, coef, flags, self.device)  # noqa: E731
+        pin = StencilOperator.flags_for(n, [0], ROW_IDENTITY | COL_EXCLUDED)
+        dfl = StencilOperator.flags_for(n, self.DefDOF, ROW_IDENTITY | COL_EXCLUDED) if len(self.DefDOF) else None
+        frow = StencilOperator.flags_for(n, self.DefDOF, ROW_ZERO) if len(self.DefDOF) else None
+        out = {"A_demag": mk(st(e["K"]), pin),
+               "A1": mk(st(e["K"] * self.alpha1 + e["M"]), dfl),
+               "A2": mk(st(e["K"] * self.alpha2 + e["M"]), dfl),
+               "F1": mk(st(e["M"]), frow)}
+        if self.p.ME:
+            out["A_el"] = mk(SH.stencil_from_element(e["Kel"], 3, 3).reshape(-1), pin)
+        return out
+
     def volume_average(self):
         return VolumeAverage(self.node_coords_np, self.elements_np, self.global_id_np, device=self.device)
 

@@ -46,7 +46,7 @@ SOLVE_NAMES = ["elasticity", "demag", "Gauss-Seidel g1n/g2n/g3n", "Gauss-Seidel 
 class LLGSolver:
     """Device-resident state and operators of one LLG run."""
 
-    def __init__(self, sim_ops, params, precision="DP", device=None, ops=None):
+    def __init__(self, sim_ops, params, precision="DP", device=None, ops=None, operators="csr"):
         self.p = params
         self.precision = "DP" if precision == "DP" else "IR"
         self.dev = device or sim_ops.device
@@ -59,6 +59,14 @@ class LLGSolver:
             Avg = sim_ops.volume_average()
         else:
             A_demag, Fx, Fy, Fz, Deriv, A1, A2, F1, A_el, F_el, Avg = ops
+        self.operators = operators
+        if operators == "stencil":
+            # matrix-free forms of the solved operators and of F1 (structured hex grids)
+            so = sim_ops.stencil_operators()
+            A_demag, A1, A2, F1 = so["A_demag"], so["A1"], so["A2"], so["F1"]
+            A_el = so.get("A_el")
+            if Fx is not None and F_el is None and params.ME:
+                raise ValueError("magnetoelastic run without F_el")
         self.A_demag, self.Fx, self.Fy, self.Fz, self.Deriv = A_demag, Fx, Fy, Fz, Deriv
         self.A1, self.A2, self.F1, self.A_el, self.F_el, self.Avg = A1, A2, F1, A_el, F_el, Avg
         if self.precision == "IR":

@@ -31,7 +31,7 @@ class CGSolver:
         self.device = device or torch.device("cuda", torch.cuda.current_device())
         self._ws = {}
         self.barrier_timeout_s = 2.0
-        self.inner_tol = 1e-5
+        self.inner_tol = 1e-4
         self.max_outer = 60
 
     def workspace(self, n, nrhs, prec):
@@ -56,6 +56,7 @@ class CGSolver:
         if not (b.is_contiguous() and x.is_contiguous()) or b.dtype != torch.float64 or x.dtype != torch.float64:
             raise TypeError("b and x must be contiguous float64 device tensors")
         ws = self.workspace(n, nrhs, prec)
+        stencil = hasattr(A, "ncomp")
         o = N.CGOpts()
         o.tol = float(tol)
         o.maxiter = int(maxiter)
@@ -65,8 +66,9 @@ class CGSolver:
         o.inner_tol = self.inner_tol
         o.max_outer = self.max_outer
         o.barrier_timeout_s = self.barrier_timeout_s
-        N.check(N.lib().cpm_cg_solve(A.struct(), b.data_ptr(), x.data_ptr(), nrhs, C.byref(o), ws.data_ptr(),
-                                     ws.numel(), info.data_ptr(), N.stream_ptr()), "cpm_cg_solve")
+        fn = N.lib().cpm_cg_solve_stencil if stencil else N.lib().cpm_cg_solve
+        N.check(fn(A.struct(), b.data_ptr(), x.data_ptr(), nrhs, C.byref(o), ws.data_ptr(), ws.numel(),
+                   info.data_ptr(), N.stream_ptr()), "cpm_cg_solve")
 
 
 def new_info(count=1, device=None) -> torch.Tensor:
@@ -118,7 +120,7 @@ def solve_cg(A, b, M=None, x0=None, tol=1e-7, maxiter=5000, use_init=False, syst
     if M is not None:
         raise NotImplementedError("preconditioned CG is not part of the reference path (M must be None)")
     solver = default_solver()
-    if not isinstance(A, DeviceCSR):
+    if not (isinstance(A, DeviceCSR) or hasattr(A, "ncomp")):
         A = DeviceCSR.from_scipy(A)
     b = torch.as_tensor(b, dtype=torch.float64, device=A.device).contiguous()
     if use_init and x0 is not None:

@@ -1,0 +1,67 @@
+"""Matrix-free periodic hex operators (see csrc/stencil.cu).
+
+A ``StencilOperator`` holds the 27-point coefficients of one structured hex
+operator (exactly the values of its CSR rows) plus per-DOF flags for the
+anchor and defect rows/columns, and applies it through the C-ABI
+(``cpm_stencil_apply``, ``cpm_cg_solve_stencil``) without a matrix stream.
+"""
+from __future__ import annotations
+
+import numpy as np
+import torch
+
+from .. import _native as N
+
+ROW_IDENTITY, ROW_ZERO, COL_EXCLUDED = 1, 2, 4
+
+
+class StencilOperator:
+    def __init__(self, nx, ny, nz, coef, flags=None, device=None):
+        self.nx, self.ny, self.nz = int(nx), int(ny), int(nz)
+        coef = np.asarray(coef, dtype=np.float64).reshape(-1)
+        self.ncomp = {27: 1, 243: 3}[coef.size]
+        dev = device or torch.device("cuda", torch.cuda.current_device())
+        self.coef = torch.as_tensor(coef, device=dev)
+        self.coef32 = self.coef.to(torch.float32)
+        self.flags = None if flags is None else torch.as_tensor(np.asarray(flags, dtype=np.uint8), device=dev)
+        self.n = self.nx * self.ny * self.nz
+        self.shape = (self.n * self.ncomp, self.n * self.ncomp)
+        self._struct = None
+
+    @property
+    def device(self):
+        return self.coef.device
+
+    def ensure_fp32(self):
+        return self
+
+    def struct(self) -> N.Stencil:
+        if self._struct is None:
+            s = N.Stencil()
+            s.nx, s.ny, s.nz, s.ncomp = self.nx, self.ny, self.nz, self.ncomp
+            s.coef = self.coef.data_ptr()
+            s.coef32 = self.coef32.data_ptr()
+            s.flags = None if self.flags is None else self.flags.data_ptr()
+            self._struct = s
+        return self._struct
+
+    def spmv(self, x: torch.Tensor, out: torch.Tensor = None, alpha: float = 1.0) -> torch.Tensor:
+        x = x.contiguous()
+        nvec = 1 if x.dim() == 1 else x.shape[1]
+        if x.shape[0] != self.shape[1] or nvec not in (1, 3) or (self.ncomp == 3 and nvec != 1):
+            raise ValueError(f"shape mismatch: {self.shape} @ {tuple(x.shape)}")
+        if out is None:
+            out = torch.empty_like(x)
+        N.check(N.lib().cpm_stencil_apply(self.struct(), x.data_ptr(), out.data_ptr(), float(alpha), nvec,
+                                          N.stream_ptr()), "cpm_stencil_apply")
+        return out
+
+    def __matmul__(self, x):
+        return self.spmv(x)
+
+    # the same operator with unit (and excluded) rows at the given DOFs
+    @staticmethod
+    def flags_for(n, dofs, bits):
+        f = np.zeros(n, dtype=np.uint8)
+        f[np.asarray(dofs, dtype=np.int64)] = bits
+        return f

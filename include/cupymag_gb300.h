@@ -119,6 +119,33 @@ int cpm_cg_solve(const cpm_csr *A, const double *b, double *x, int nrhs, const c
 int cpm_cg_solve_noalloc(const cpm_csr *A, const double *b, double *x, int nrhs, const cpm_cg_opts *opts,
                          cpm_cg_info *info_dev, void *stream);
 
+/* ---- matrix-free periodic hex operators ----
+ * The structured hex grid's operators are 27-point periodic stencils; these
+ * entry points apply them (and run the same CG on them) without streaming
+ * CSR values.  coef[(a*ncomp + b)*27 + d], d = (dx+1)*9 + (dy+1)*3 + (dz+1),
+ * is the coefficient between component a of DOF p and component b of DOF
+ * p + (dx,dy,dz) (wrapped), DOF = (i*ny + j)*nz + k -- exactly the values of
+ * the CSR rows built by structured assembly (assemble_demag.py:186-233,
+ * assemble_Gauss_Seidel.py:163-214, assemble_elasticity.py:350-459).
+ * flags (uint8 per DOF, may be NULL): 1 = unit row (anchors, defect DOFs of
+ * A1/A2), 2 = empty row (defect rows of the mass matrix), 4 = the DOF's
+ * column is dropped from every other row (final_assembly.py:59-158). */
+typedef struct {
+  int32_t nx, ny, nz;      /* cells per axis (>= 3), n = nx*ny*nz DOFs */
+  int32_t ncomp;           /* 1: scalar operator; 3: elastic operator on [ux|uy|uz] */
+  const double *coef;      /* 27*ncomp*ncomp FP64 coefficients */
+  const float *coef32;     /* the same in FP32 (mixed precision), or NULL */
+  const uint8_t *flags;    /* per-DOF row/column flags, or NULL */
+} cpm_stencil;
+
+/* y = alpha * A x (FP64); nvec 1 or 3 ((n,nvec) layout) for ncomp = 1. */
+int cpm_stencil_apply(const cpm_stencil *S, const double *x, double *y, double alpha, int nvec, void *stream);
+
+/* cpm_cg_solve on a stencil operator: same semantics, options and info;
+ * workspace size cpm_cg_workspace_bytes(n * ncomp, nrhs, precision). */
+int cpm_cg_solve_stencil(const cpm_stencil *S, const double *b, double *x, int nrhs, const cpm_cg_opts *opts,
+                         void *workspace, size_t workspace_bytes, cpm_cg_info *info_dev, void *stream);
+
 /* ---- LLG step kernels (cupymag/core/Micromagnetics.py:110-307) ---- */
 typedef struct {
   double K1, elasC1, elasC2, elasC3, lambda100;
