@@ -30,8 +30,7 @@ class CSR(C.Structure):
 
 
 class Stencil(C.Structure):
-    _fields_ = [("nx", i32), ("ny", i32), ("nz", i32), ("ncomp", i32), ("coef", vp), ("coef32", vp),
-                ("flags", vp)]
+    _fields_ = [("nx", i32), ("ny", i32), ("nz", i32), ("ncomp", i32), ("coef", dbl * 243), ("flags", vp)]
 
 
 class CGInfo(C.Structure):

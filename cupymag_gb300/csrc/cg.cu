@@ -24,8 +24,7 @@
 // stopping test, so each result equals the single-system solve.
 //
 // precision = 1: FP32 CG (FP32 values and vectors, FP64 dot accumulation)
-// inside FP64 iterative refinement: r = b - A64 x in FP64, solve A32 d = r to
-// inner_tol relative, x += d, until ||b - A64 x|| <= tol ||b||.
+// with FP64 reliable updates of x and of the residual b - A64 x.
 #include <cmath>
 #include <cstdio>
 #include <mutex>
@@ -232,44 +231,82 @@ __global__ void __launch_bounds__(kCGThreads) cg_fp64_kernel(CGArgs<NR, IT> a) {
   }
 }
 
-// ------------------------------------------------ FP32 CG in FP64 refinement
+// ------------------------------------------ FP32 CG with FP64 reliable updates
+// Mixed-precision CG with reliable updates (Sleijpen & van der Vorst, 1996),
+// as in csrc/stencil.cu: FP32 values and vectors (p, q, correction d,
+// recursive residual r32) with FP64 dot accumulation; when the recursive
+// residual has dropped by inner_tol below the last true residual (or below the
+// stopping threshold), x += d in FP64 and r is replaced by b - A64 x computed
+// with the FP64 values (staged tiles).  The search direction survives the
+// update, so the iteration count stays close to plain FP64 CG; convergence is
+// only ever decided on the FP64 residual.
 template <int NR, typename IT>
 __global__ void __launch_bounds__(kCGThreads) cg_ir_kernel(CGArgs<NR, IT> a) {
   __shared__ double s_red[2 * NR][kCGWarps];
+  extern __shared__ __align__(16) unsigned char s_tile[];
+  const TileSmem tile = tile_smem(s_tile);
+  const int G = a.group;
+  const int R = kCGThreads / G;
+  const bool lead = (threadIdx.x % G) == 0;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int64_t r0 = min(a.n, (int64_t)blockIdx.x * a.rows_per_cta);
   const int64_t r1 = min(a.n, r0 + a.rows_per_cta);
   const bool use_init = a.use_init_dev ? (__ldcg(a.use_init_dev) != 0) : (a.use_init_host != 0);
   const unsigned long long tns = a.timeout_ns;
+  const double delta = a.inner_tol;
   int par = 0;
 
-  // ---- ||b||, x0
+  // ---- prologue: r = b - A64 x (or b), r32 = p32 = r, d = 0
   double v[2 * NR];
 #pragma unroll
   for (int j = 0; j < 2 * NR; ++j) v[j] = 0.0;
-  for (int64_t row = r0 + threadIdx.x; row < r1; row += kCGThreads) {
+  if (use_init) {
+    for (int64_t t0 = r0; t0 < r1; t0 += R) {
+      double acc[NR];
+      const int64_t row = tile_rows<NR, IT>(a.rp, a.ci, a.av, a.x, t0, min(r1, t0 + R), G, tile, acc);
+      if (row >= 0 && lead) {
 #pragma unroll
-    for (int j = 0; j < NR; ++j) {
-      const double bj = a.b[row * NR + j];
-      if (!use_init) a.x[row * NR + j] = 0.0;
-      v[j] = fma(bj, bj, v[j]);
+        for (int j = 0; j < NR; ++j) {
+          const double bj = a.b[row * NR + j];
+          const double rj = bj - acc[j];
+          const float rf = (float)rj;
+          a.r32[row * NR + j] = rf;
+          a.pa32[row * NR + j] = rf;
+          a.d32[row * NR + j] = 0.0f;
+          v[j] = fma(bj, bj, v[j]);
+          v[NR + j] = fma(rj, rj, v[NR + j]);
+        }
+      }
+    }
+  } else {
+    for (int64_t row = r0 + threadIdx.x; row < r1; row += kCGThreads) {
+#pragma unroll
+      for (int j = 0; j < NR; ++j) {
+        const double bj = a.b[row * NR + j];
+        const float rf = (float)bj;
+        a.x[row * NR + j] = 0.0;
+        a.r32[row * NR + j] = rf;
+        a.pa32[row * NR + j] = rf;
+        a.d32[row * NR + j] = 0.0f;
+        v[j] = fma(bj, bj, v[j]);
+        v[NR + j] = fma(bj, bj, v[NR + j]);
+      }
     }
   }
-  double bb[NR];
-#pragma unroll
-  for (int j = 0; j < NR; ++j) bb[j] = v[j];
-  if (!grid_sum<NR>(bb, a.part, par, a.bar, tns, s_red)) {
+  if (!grid_sum<2 * NR>(v, a.part, par, a.bar, tns, s_red)) {
     set_status(a.info, CPM_BARRIER_TIMEOUT);
     return;
   }
-  double atol[NR], resid[NR];
+  double atol[NR], resid[NR], rho[NR], rlast[NR];
   int active[NR], iters[NR];
   bool any = false;
 #pragma unroll
   for (int j = 0; j < NR; ++j) {
-    const double bn = sqrt(bb[j]);
+    const double bn = sqrt(v[j]);
     atol[j] = a.tol * bn;
-    resid[j] = bn;
+    rho[j] = v[NR + j];
+    resid[j] = sqrt(v[NR + j]);
+    rlast[j] = resid[j];
     active[j] = bn != 0.0;
     iters[j] = 0;
     any |= active[j] != 0;
@@ -278,161 +315,136 @@ __global__ void __launch_bounds__(kCGThreads) cg_ir_kernel(CGArgs<NR, IT> a) {
     if (blockIdx.x == 0 && threadIdx.x == 0) a.info->bnorm[j] = bn;
   }
   int status = CPM_OK;
-  int outer = 0;
-  int total = 0;
-  while (any) {
-    // ---- outer residual r = b - A64 x in FP64; FP32 copy; d = 0
-    double rr64[NR], rr32[NR];
+  int updates = 0;
+  float *p32 = a.pa32;
+  for (int k = 0; any && k < a.maxiter; ++k) {
+    if (k > 0 && !grid_sync(a.bar, gridDim.x, tns)) { status = CPM_BARRIER_TIMEOUT; break; }
+    // ---- phase 1: q32 = A32 p32 (warp per row, FP32 products, FP64 row sum), partial p.q
+    double pq[NR];
 #pragma unroll
-    for (int j = 0; j < NR; ++j) { rr64[j] = 0.0; rr32[j] = 0.0; }
+    for (int j = 0; j < NR; ++j) pq[j] = 0.0;
     for (int64_t row = r0 + warp; row < r1; row += kCGWarps) {
       int64_t s, e;
       row_range(a.rp, row, s, e);
-      double acc[NR];
+      float acc[NR];
 #pragma unroll
-      for (int j = 0; j < NR; ++j) acc[j] = 0.0;
+      for (int j = 0; j < NR; ++j) acc[j] = 0.0f;
       for (int64_t kk = s + lane; kk < e; kk += kWarp) {
-        const double av = ld_stream(a.av + kk);
-        const int64_t c = ld_stream(a.ci + kk);
+        const float av = ld_stream(a.av32 + kk);
+        const int64_t cc = ld_stream(a.ci + kk);
 #pragma unroll
-        for (int j = 0; j < NR; ++j) acc[j] = fma(av, a.x[c * NR + j], acc[j]);
+        for (int j = 0; j < NR; ++j) acc[j] = fmaf(av, p32[cc * NR + j], acc[j]);
       }
+      double accd[NR];
 #pragma unroll
-      for (int j = 0; j < NR; ++j) acc[j] = warp_sum(acc[j]);
+      for (int j = 0; j < NR; ++j) accd[j] = warp_sum((double)acc[j]);
       if (lane == 0) {
 #pragma unroll
         for (int j = 0; j < NR; ++j) {
-          const double rj = a.b[row * NR + j] - acc[j];
-          const float rf = (float)rj;
-          a.r32[row * NR + j] = rf;
-          a.d32[row * NR + j] = 0.0f;
-          rr64[j] = fma(rj, rj, rr64[j]);
-          rr32[j] = fma((double)rf, (double)rf, rr32[j]);
+          const float qf = (float)accd[j];
+          a.q32[row * NR + j] = qf;
+          pq[j] = fma((double)p32[row * NR + j], (double)qf, pq[j]);
         }
       }
     }
-    double red[2 * NR];
-#pragma unroll
-    for (int j = 0; j < NR; ++j) { red[j] = rr64[j]; red[NR + j] = rr32[j]; }
-    if (!grid_sum<2 * NR>(red, a.part, par, a.bar, tns, s_red)) { status = CPM_BARRIER_TIMEOUT; break; }
-    any = false;
-    double rho[NR], rho_old[NR], iatol[NR];
-    int iact[NR];
-    bool iany = false;
+    if (!grid_sum<NR>(pq, a.part, par, a.bar, tns, s_red)) { status = CPM_BARRIER_TIMEOUT; break; }
+    double alpha[NR];
+    bool bad = false;
 #pragma unroll
     for (int j = 0; j < NR; ++j) {
-      if (active[j]) {
-        resid[j] = sqrt(red[j]);
-        if (!(resid[j] > atol[j])) active[j] = 0;
-      }
-      any |= active[j] != 0;
-      rho[j] = red[NR + j];
-      rho_old[j] = 1.0;
-      iact[j] = active[j];
-      iatol[j] = a.inner_tol * sqrt(red[NR + j]);
-      iany |= iact[j] != 0;
+      alpha[j] = active[j] ? rho[j] / pq[j] : 0.0;
+      if (active[j] && !isfinite(alpha[j])) bad = true;
     }
-    if (!any) break;
-    if (outer >= a.max_outer || total >= a.maxiter) break;
-    ++outer;
-
-    // ---- inner FP32 CG on A32 d = r32
-    int kin = 0;
-    while (iany && total < a.maxiter) {
-      double beta[NR];
+    if (bad) { status = CPM_NONFINITE; break; }
+    // ---- phase 2: d += alpha p, r32 -= alpha q
+    double rr[NR];
 #pragma unroll
-      for (int j = 0; j < NR; ++j) beta[j] = (kin == 0 || !iact[j]) ? 0.0 : rho[j] / rho_old[j];
-      const float *pin = (kin & 1) ? a.pb32 : a.pa32;
-      float *pout = (kin & 1) ? a.pa32 : a.pb32;
-      float fb[NR];
-#pragma unroll
-      for (int j = 0; j < NR; ++j) fb[j] = (float)beta[j];
-#pragma unroll
-      for (int j = 0; j < NR; ++j) v[j] = 0.0;
-      for (int64_t row = r0 + warp; row < r1; row += kCGWarps) {
-        int64_t s, e;
-        row_range(a.rp, row, s, e);
-        float acc[NR];
-#pragma unroll
-        for (int j = 0; j < NR; ++j) acc[j] = 0.0f;
-        if (kin == 0) {
-          for (int64_t kk = s + lane; kk < e; kk += kWarp) {
-            const float av = ld_stream(a.av32 + kk);
-            const int64_t c = ld_stream(a.ci + kk);
-#pragma unroll
-            for (int j = 0; j < NR; ++j) acc[j] = fmaf(av, a.r32[c * NR + j], acc[j]);
-          }
-        } else {
-          for (int64_t kk = s + lane; kk < e; kk += kWarp) {
-            const float av = ld_stream(a.av32 + kk);
-            const int64_t c = ld_stream(a.ci + kk);
-#pragma unroll
-            for (int j = 0; j < NR; ++j) acc[j] = fmaf(av, __fmaf_rn(fb[j], pin[c * NR + j], a.r32[c * NR + j]), acc[j]);
-          }
-        }
-        double accd[NR];
-#pragma unroll
-        for (int j = 0; j < NR; ++j) accd[j] = warp_sum((double)acc[j]);
-        if (lane == 0) {
-#pragma unroll
-          for (int j = 0; j < NR; ++j) {
-            const float pn = (kin == 0) ? a.r32[row * NR + j] : __fmaf_rn(fb[j], pin[row * NR + j], a.r32[row * NR + j]);
-            const float qf = (float)accd[j];
-            pout[row * NR + j] = pn;
-            a.q32[row * NR + j] = qf;
-            v[j] = fma((double)pn, (double)qf, v[j]);
-          }
-        }
-      }
-      double pq[NR];
-#pragma unroll
-      for (int j = 0; j < NR; ++j) pq[j] = v[j];
-      if (!grid_sum<NR>(pq, a.part, par, a.bar, tns, s_red)) { status = CPM_BARRIER_TIMEOUT; break; }
-      double alpha[NR];
-      bool bad = false;
-#pragma unroll
-      for (int j = 0; j < NR; ++j) {
-        alpha[j] = iact[j] ? rho[j] / pq[j] : 0.0;
-        if (iact[j] && !isfinite(alpha[j])) bad = true;
-      }
-      if (bad) { status = CPM_NONFINITE; break; }
-      double rr[NR];
-#pragma unroll
-      for (int j = 0; j < NR; ++j) rr[j] = 0.0;
-      for (int64_t row = r0 + threadIdx.x; row < r1; row += kCGThreads) {
-#pragma unroll
-        for (int j = 0; j < NR; ++j) {
-          const int64_t i = row * NR + j;
-          a.d32[i] = (float)fma(alpha[j], (double)pout[i], (double)a.d32[i]);
-          const float rn = (float)fma(-alpha[j], (double)a.q32[i], (double)a.r32[i]);
-          a.r32[i] = rn;
-          rr[j] = fma((double)rn, (double)rn, rr[j]);
-        }
-      }
-      if (!grid_sum<NR>(rr, a.part, par, a.bar, tns, s_red)) { status = CPM_BARRIER_TIMEOUT; break; }
-      iany = false;
-#pragma unroll
-      for (int j = 0; j < NR; ++j) {
-        if (!iact[j]) continue;
-        if (!isfinite(rr[j])) bad = true;
-        iters[j] += 1;
-        rho_old[j] = rho[j];
-        rho[j] = rr[j];
-        if (sqrt(rr[j]) <= iatol[j]) iact[j] = 0;
-        iany |= iact[j] != 0;
-      }
-      if (bad) { status = CPM_NONFINITE; break; }
-      ++kin;
-      ++total;
-    }
-    if (status != CPM_OK) break;
-    // ---- x += d (FP64)
+    for (int j = 0; j < NR; ++j) rr[j] = 0.0;
     for (int64_t row = r0 + threadIdx.x; row < r1; row += kCGThreads) {
 #pragma unroll
-      for (int j = 0; j < NR; ++j)
-        if (active[j]) a.x[row * NR + j] += (double)a.d32[row * NR + j];
+      for (int j = 0; j < NR; ++j) {
+        if (!active[j]) continue;
+        const int64_t i = row * NR + j;
+        const float af = (float)alpha[j];
+        a.d32[i] = fmaf(af, p32[i], a.d32[i]);
+        const float rn = fmaf(-af, a.q32[i], a.r32[i]);
+        a.r32[i] = rn;
+        rr[j] = fma((double)rn, (double)rn, rr[j]);
+      }
     }
-    if (!grid_sync(a.bar, gridDim.x, tns)) { status = CPM_BARRIER_TIMEOUT; break; }
+    if (!grid_sum<NR>(rr, a.part, par, a.bar, tns, s_red)) { status = CPM_BARRIER_TIMEOUT; break; }
+    bool upd = false;
+    int need[NR];
+#pragma unroll
+    for (int j = 0; j < NR; ++j) {
+      need[j] = 0;
+      if (!active[j]) continue;
+      if (!isfinite(rr[j])) bad = true;
+      iters[j] += 1;
+      const double rn = sqrt(rr[j]);
+      need[j] = (rn < delta * rlast[j]) || (rn <= atol[j]) || (k + 1 >= a.maxiter);
+      upd |= need[j] != 0;
+    }
+    if (bad) { status = CPM_NONFINITE; break; }
+    double rnew[NR];
+#pragma unroll
+    for (int j = 0; j < NR; ++j) rnew[j] = rr[j];
+    if (upd) {
+      ++updates;
+      for (int64_t row = r0 + threadIdx.x; row < r1; row += kCGThreads)
+#pragma unroll
+        for (int j = 0; j < NR; ++j) {
+          if (!need[j]) continue;
+          const int64_t i = row * NR + j;
+          a.x[i] += (double)a.d32[i];
+          a.d32[i] = 0.0f;
+        }
+      if (!grid_sync(a.bar, gridDim.x, tns)) { status = CPM_BARRIER_TIMEOUT; break; }
+      double tr[NR];
+#pragma unroll
+      for (int j = 0; j < NR; ++j) tr[j] = 0.0;
+      for (int64_t t0 = r0; t0 < r1; t0 += R) {
+        double acc[NR];
+        const int64_t row = tile_rows<NR, IT>(a.rp, a.ci, a.av, a.x, t0, min(r1, t0 + R), G, tile, acc);
+        if (row >= 0 && lead) {
+#pragma unroll
+          for (int j = 0; j < NR; ++j) {
+            if (!need[j]) continue;
+            const double rj = a.b[row * NR + j] - acc[j];
+            a.r32[row * NR + j] = (float)rj;
+            tr[j] = fma(rj, rj, tr[j]);
+          }
+        }
+      }
+      if (!grid_sum<NR>(tr, a.part, par, a.bar, tns, s_red)) { status = CPM_BARRIER_TIMEOUT; break; }
+#pragma unroll
+      for (int j = 0; j < NR; ++j) {
+        if (!need[j]) continue;
+        resid[j] = sqrt(tr[j]);
+        rlast[j] = resid[j];
+        rnew[j] = tr[j];
+        if (resid[j] <= atol[j]) active[j] = 0;
+      }
+    }
+    any = false;
+    float beta[NR];
+#pragma unroll
+    for (int j = 0; j < NR; ++j) {
+      beta[j] = 0.0f;
+      if (!active[j]) continue;
+      beta[j] = (float)(rnew[j] / rho[j]);
+      rho[j] = rnew[j];
+      any = true;
+    }
+    if (!any || k + 1 >= a.maxiter) break;
+    // ---- phase 3: p = r32 + beta p
+    for (int64_t row = r0 + threadIdx.x; row < r1; row += kCGThreads)
+#pragma unroll
+      for (int j = 0; j < NR; ++j) {
+        if (!active[j]) continue;
+        const int64_t i = row * NR + j;
+        p32[i] = fmaf(beta[j], p32[i], a.r32[i]);
+      }
   }
   if (blockIdx.x == 0 && threadIdx.x == 0) {
     int st = status;
@@ -442,7 +454,7 @@ __global__ void __launch_bounds__(kCGThreads) cg_ir_kernel(CGArgs<NR, IT> a) {
       a.info->iters[j] = iters[j];
       a.info->resid[j] = resid[j];
     }
-    a.info->outer = outer;
+    a.info->outer = updates;
     set_status(a.info, st);
   } else if (status != CPM_OK && threadIdx.x == 0) {
     set_status(a.info, status);
@@ -464,7 +476,7 @@ static int launch_cg(const cpm_csr *A, const double *b, double *x, const cpm_cg_
   a.maxiter = o->maxiter;
   a.use_init_host = o->use_init_host;
   a.use_init_dev = o->use_init_dev;
-  a.inner_tol = o->inner_tol > 0 ? o->inner_tol : 1e-5;
+  a.inner_tol = o->inner_tol > 0 ? o->inner_tol : 0.1;
   a.max_outer = o->max_outer > 0 ? o->max_outer : 50;
   a.r = w.r;
   a.p0 = w.p0;
@@ -483,7 +495,7 @@ static int launch_cg(const cpm_csr *A, const double *b, double *x, const cpm_cg_
 
   const bool fp64 = o->precision == 0;
   const void *fn = fp64 ? (const void *)cg_fp64_kernel<NR, IT> : (const void *)cg_ir_kernel<NR, IT>;
-  const int smem = fp64 ? kTileSmemBytes : 0;
+  const int smem = kTileSmemBytes;
   static int cached_dev[2][2][2] = {};
   static int cached_occ[2][2][2] = {};
   const int dev = device_id();

@@ -20,8 +20,13 @@
 
 namespace cpm {
 
-constexpr int kTileCap = 7168;                          // non-zeros per staged tile
+// Single-value tiles are sized so four 256-thread CTAs fit on an SM (43 KB each):
+// while one CTA waits for its copies the others compute.
+constexpr int kTileCap = 3584;                          // non-zeros per staged tile
 constexpr int kTileSmemBytes = kTileCap * 8 + 16 + (kTileCap + 4) * 4 + 16;
+// Tiles of three value arrays (Fx, Fy, Fz) are larger so 27-entry rows keep
+// small thread groups.
+constexpr int kMultiSmemBytes = 86064;
 
 struct TileSmem {
   double *v;  // kTileCap + 2 values (offset so 16-byte copies land aligned)
@@ -126,7 +131,12 @@ namespace cpm {
 // once and NV value streams.  Capacity in non-zeros for NV value arrays.
 template <int NV>
 __host__ __device__ constexpr int multi_cap() {
-  return NV == 1 ? kTileCap : ((kTileSmemBytes - 64) / (8 * NV + 4)) / 4 * 4 - 4;
+  return NV == 1 ? kTileCap : ((kMultiSmemBytes - 64) / (8 * NV + 4)) / 4 * 4 - 4;
+}
+
+template <int NV>
+__host__ __device__ constexpr int multi_smem() {
+  return NV == 1 ? kTileSmemBytes : kMultiSmemBytes;
 }
 
 template <int NV>

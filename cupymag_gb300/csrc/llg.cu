@@ -514,19 +514,19 @@ extern "C" int cpm_strain_from_u(const cpm_csr *Fx, const double *vals_y, const 
   static int occ = 0;
   if (occ == 0) {
     cudaFuncSetAttribute((const void *)strain_kernel<int64_t>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         kTileSmemBytes);
+                         multi_smem<3>());
     cudaFuncSetAttribute((const void *)strain_kernel<int32_t>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         kTileSmemBytes);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fn, kStrainThreads, kTileSmemBytes);
+                         multi_smem<3>());
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fn, kStrainThreads, multi_smem<3>());
     if (occ < 1) occ = 1;
   }
   int64_t g = (int64_t)occ * sm_count();
   if (g > tiles) g = tiles;
   if (Fx->indptr_is64)
-    strain_kernel<int64_t><<<(int)g, kStrainThreads, kTileSmemBytes, st>>>(
+    strain_kernel<int64_t><<<(int)g, kStrainThreads, multi_smem<3>(), st>>>(
         n, (const int64_t *)Fx->indptr, Fx->indices, Fx->vals, vals_y, vals_z, u, R9, E, G);
   else
-    strain_kernel<int32_t><<<(int)g, kStrainThreads, kTileSmemBytes, st>>>(
+    strain_kernel<int32_t><<<(int)g, kStrainThreads, multi_smem<3>(), st>>>(
         n, (const int32_t *)Fx->indptr, Fx->indices, Fx->vals, vals_y, vals_z, u, R9, E, G);
   return check_launch("cpm_strain_from_u");
 }

@@ -15,15 +15,15 @@ constexpr int kSpThreads = 256;
 
 // Staged thread-group-per-row kernels (see csr_tile.cuh): one FP64 FMA per
 // non-zero and value, tiles of rows handed out grid-stride.
-static int tile_grid(int64_t tiles, const void *fn) {
+static int tile_grid(int64_t tiles, const void *fn, int smem) {
   static int occ_cache[8] = {};
   static const void *fn_cache[8] = {};
   int occ = 0;
   for (int i = 0; i < 8; ++i)
     if (fn_cache[i] == fn) occ = occ_cache[i];
   if (occ == 0) {
-    cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, kTileSmemBytes);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fn, kSpThreads, kTileSmemBytes);
+    cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fn, kSpThreads, smem);
     if (occ < 1) occ = 1;
     for (int i = 0; i < 8; ++i)
       if (fn_cache[i] == nullptr) {
@@ -155,7 +155,7 @@ extern "C" int cpm_spmv_csr(const cpm_csr *A, const double *x, double *y, double
 #define CPM_SP1(IT, NV)                                                                                          \
   do {                                                                                                           \
     const void *fn = (const void *)spmv_kernel<IT, NV>;                                                          \
-    spmv_kernel<IT, NV><<<tile_grid(tiles, fn), kSpThreads, kTileSmemBytes, st>>>(                               \
+    spmv_kernel<IT, NV><<<tile_grid(tiles, fn, multi_smem<1>()), kSpThreads, multi_smem<1>(), st>>>(           \
         A->rows, (const IT *)A->indptr, A->indices, A->vals, x, y, alpha, G);                                    \
   } while (0)
   if (A->indptr_is64) {
@@ -183,7 +183,7 @@ extern "C" int cpm_spmv_csr_multi(const cpm_csr *A, const double *vals_y, const 
 #define CPM_SP3(IT, M)                                                                                         \
   do {                                                                                                         \
     const void *fn = (const void *)spmv3_kernel<IT, M>;                                                        \
-    spmv3_kernel<IT, M><<<tile_grid(tiles, fn), kSpThreads, kTileSmemBytes, st>>>(                             \
+    spmv3_kernel<IT, M><<<tile_grid(tiles, fn, multi_smem<3>()), kSpThreads, multi_smem<3>(), st>>>(         \
         A->rows, (const IT *)A->indptr, A->indices, A->vals, vals_y, vals_z, x, y, alpha, shift, pin, G);      \
   } while (0)
   if (A->indptr_is64) {

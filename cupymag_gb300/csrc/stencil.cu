@@ -18,138 +18,17 @@
 //
 // The solver is the same cupyx-semantics CG as csrc/cg.cu (three phases per
 // iteration, bounded grid barriers, fixed-order reductions), in FP64
-// (precision 0) or as FP32 CG inside FP64 iterative refinement (precision 1):
-// the refinement residual b - A x applies the FP64 coefficients to the FP64
-// x, so the stopping test ||b - A x|| <= tol ||b|| is the FP64 one, while the
-// inner iterations run on FP32 vectors with FP32 coefficients and FP64 dot
-// accumulation.  GB300 issues FP32 FMAs at many times its FP64 rate, so the
-// FP32 inner iterations are bound by the vectors' L2/HBM traffic alone.
+// (precision 0) or in FP32 with FP64 reliable updates (precision 1): the
+// residual is periodically replaced by b - A x computed with the FP64
+// coefficients and the FP64 x, so the stopping test ||b - A x|| <= tol ||b||
+// is the FP64 one, while the iterations run on FP32 vectors with FP32
+// coefficients and FP64 dot accumulation.  GB300 issues FP32 FMAs at many
+// times its FP64 rate, so the FP32 iterations are bound by vector traffic.
 #include <cmath>
 
-#include "cg_common.cuh"
+#include "stencil_ops.cuh"
 
 namespace cpm {
-
-enum : uint8_t { kRowIdentity = 1, kRowZero = 2, kColExcluded = 4 };
-
-struct StencilOp {
-  int nx, ny, nz;
-  int64_t n;
-  const double *c64;
-  const float *c32;
-  const uint8_t *flags;
-};
-
-// Wrapped neighbour offsets of a DOF along each axis (index 0: -1, 1: 0, 2: +1).
-struct Nbr {
-  int64_t xi[3];
-  int yj[3];
-  int zk[3];
-};
-
-__device__ __forceinline__ Nbr neighbours(const StencilOp &S, int64_t dof) {
-  const int64_t nyz = (int64_t)S.ny * S.nz;
-  const int i = (int)(dof / nyz);
-  const int64_t rem = dof - (int64_t)i * nyz;
-  const int j = (int)(rem / S.nz);
-  const int k = (int)(rem - (int64_t)j * S.nz);
-  Nbr b;
-  b.xi[0] = (int64_t)(i == 0 ? S.nx - 1 : i - 1) * nyz;
-  b.xi[1] = (int64_t)i * nyz;
-  b.xi[2] = (int64_t)(i == S.nx - 1 ? 0 : i + 1) * nyz;
-  b.yj[0] = (j == 0 ? S.ny - 1 : j - 1) * S.nz;
-  b.yj[1] = j * S.nz;
-  b.yj[2] = (j == S.ny - 1 ? 0 : j + 1) * S.nz;
-  b.zk[0] = k == 0 ? S.nz - 1 : k - 1;
-  b.zk[1] = k;
-  b.zk[2] = k == S.nz - 1 ? 0 : k + 1;
-  return b;
-}
-
-// y = A x at one DOF for a scalar operator (nc = 1), nr interleaved vectors.
-// Accumulates in T (FP64 for the FP64 products, FP32 for the inner solve).
-template <typename T, int NR>
-__device__ __forceinline__ void apply_scalar(const StencilOp &S, const T *c, const T *x, int64_t dof, T (&y)[NR]) {
-#pragma unroll
-  for (int r = 0; r < NR; ++r) y[r] = T(0);
-  const uint8_t f = S.flags ? S.flags[dof] : 0;
-  if (f & kRowIdentity) {
-#pragma unroll
-    for (int r = 0; r < NR; ++r) y[r] = x[dof * NR + r];
-    return;
-  }
-  if (f & kRowZero) return;
-  const Nbr b = neighbours(S, dof);
-#pragma unroll
-  for (int a = 0; a < 3; ++a)
-#pragma unroll
-    for (int bb = 0; bb < 3; ++bb)
-#pragma unroll
-      for (int cc = 0; cc < 3; ++cc) {
-        const int64_t q = b.xi[a] + b.yj[bb] + b.zk[cc];
-        if (S.flags && (S.flags[q] & kColExcluded)) continue;
-        const T w = c[(a * 3 + bb) * 3 + cc];
-#pragma unroll
-        for (int r = 0; r < NR; ++r) y[r] = fma(w, x[q * NR + r], y[r]);
-      }
-}
-
-// y = A x at one DOF for the elastic operator (nc = 3, block vectors).
-template <typename T>
-__device__ __forceinline__ void apply_elastic(const StencilOp &S, const T *c, const T *x, int64_t dof, T (&y)[3]) {
-  const int64_t n = S.n;
-  y[0] = y[1] = y[2] = T(0);
-  const uint8_t f = S.flags ? S.flags[dof] : 0;
-  if (f & kRowIdentity) {
-    y[0] = x[dof];
-    y[1] = x[n + dof];
-    y[2] = x[2 * n + dof];
-    return;
-  }
-  if (f & kRowZero) return;
-  const Nbr b = neighbours(S, dof);
-#pragma unroll
-  for (int a = 0; a < 3; ++a)
-#pragma unroll
-    for (int bb = 0; bb < 3; ++bb)
-#pragma unroll
-      for (int cc = 0; cc < 3; ++cc) {
-        const int64_t q = b.xi[a] + b.yj[bb] + b.zk[cc];
-        if (S.flags && (S.flags[q] & kColExcluded)) continue;
-        const int d = (a * 3 + bb) * 3 + cc;
-        const T u0 = x[q], u1 = x[n + q], u2 = x[2 * n + q];
-#pragma unroll
-        for (int r = 0; r < 3; ++r) {
-          T acc = y[r];
-          acc = fma(c[(r * 3 + 0) * 27 + d], u0, acc);
-          acc = fma(c[(r * 3 + 1) * 27 + d], u1, acc);
-          acc = fma(c[(r * 3 + 2) * 27 + d], u2, acc);
-          y[r] = acc;
-        }
-      }
-}
-
-// Unknown index of (dof, component) for the NC/NR layouts.
-template <int NC, int NR>
-__device__ __forceinline__ int64_t uidx(int64_t n, int64_t dof, int comp) {
-  return NC == 1 ? dof * NR + comp : (int64_t)comp * n + dof;
-}
-
-// y at one DOF (all NC*NR components) in T.
-template <typename T, int NC, int NR>
-__device__ __forceinline__ void apply(const StencilOp &S, const T *c, const T *x, int64_t dof, T (&y)[NC * NR]) {
-  if (NC == 1) {
-    T t[NR];
-    apply_scalar<T, NR>(S, c, x, dof, t);
-#pragma unroll
-    for (int r = 0; r < NR; ++r) y[r] = t[r];
-  } else {
-    T t[3];
-    apply_elastic<T>(S, c, x, dof, t);
-#pragma unroll
-    for (int r = 0; r < 3; ++r) y[r] = t[r];
-  }
-}
 
 struct StencilCG {
   StencilOp S;
@@ -177,22 +56,12 @@ __host__ __device__ constexpr int n_systems() { return NC == 1 ? NR : 1; }
 template <int NC, int NR>
 __device__ __forceinline__ int sys_of(int comp) { return NC == 1 ? comp : 0; }
 
-// Coefficients staged in shared memory (27 * NC * NC values).
-template <typename T, int NC>
-__device__ __forceinline__ const T *stage_coef(const T *c, T *smem) {
-  for (int i = threadIdx.x; i < 27 * NC * NC; i += blockDim.x) smem[i] = c[i];
-  __syncthreads();
-  return smem;
-}
-
 // ---------------------------------------------------------------- FP64 stencil CG
 template <int NC, int NR>
-__global__ void __launch_bounds__(kCGThreads) cg_stencil_fp64_kernel(StencilCG a) {
+__global__ void __launch_bounds__(kCGThreads) cg_stencil_fp64_kernel(const __grid_constant__ StencilCG a) {
   constexpr int U = NC * NR;
   constexpr int NS = n_systems<NC, NR>();
   __shared__ double s_red[2 * 3][kCGWarps];
-  __shared__ double s_c[27 * NC * NC];
-  const double *c = stage_coef<double, NC>(a.S.c64, s_c);
   const int64_t n = a.S.n;
   const int64_t d0 = min(n, (int64_t)blockIdx.x * a.dofs_per_cta);
   const int64_t d1 = min(n, d0 + a.dofs_per_cta);
@@ -205,7 +74,7 @@ __global__ void __launch_bounds__(kCGThreads) cg_stencil_fp64_kernel(StencilCG a
   for (int j = 0; j < 2 * NS; ++j) v[j] = 0.0;
   for (int64_t dof = d0 + threadIdx.x; dof < d1; dof += kCGThreads) {
     double y[U];
-    if (use_init) apply<double, NC, NR>(a.S, c, a.x, dof, y);
+    if (use_init) apply<double, NC, NR>(a.S, a.x, (int)dof, y);
 #pragma unroll
     for (int u = 0; u < U; ++u) {
       const int64_t i = uidx<NC, NR>(n, dof, u);
@@ -250,7 +119,7 @@ __global__ void __launch_bounds__(kCGThreads) cg_stencil_fp64_kernel(StencilCG a
     for (int j = 0; j < NS; ++j) pq[j] = 0.0;
     for (int64_t dof = d0 + threadIdx.x; dof < d1; dof += kCGThreads) {
       double y[U];
-      apply<double, NC, NR>(a.S, c, a.p, dof, y);
+      apply<double, NC, NR>(a.S, a.p, (int)dof, y);
 #pragma unroll
       for (int u = 0; u < U; ++u) {
         const int64_t i = uidx<NC, NR>(n, dof, u);
@@ -324,46 +193,66 @@ __global__ void __launch_bounds__(kCGThreads) cg_stencil_fp64_kernel(StencilCG a
   }
 }
 
-// ---------------------------------------------------------------- FP32 CG in FP64 refinement
+// ---------------------------------------------------------------- FP32 CG with FP64 reliable updates
+// Mixed-precision CG with reliable updates (Sleijpen & van der Vorst, 1996):
+// the iteration runs on FP32 vectors (p, q, the correction d and the
+// recursive residual r) with FP64 dot accumulation.  Whenever the recursive
+// residual has dropped by a factor delta (inner_tol) below the last true
+// residual -- or below the stopping threshold -- x += d in FP64 and the
+// residual is replaced by the true FP64 residual b - A x (FP64 coefficients,
+// FP64 x).  The search direction is kept across updates, so the Krylov
+// convergence of plain CG is retained (unlike restarted refinement), and the
+// stopping test ||b - A x|| <= tol ||b|| is only ever decided on the FP64
+// residual.  info->outer counts the reliable updates.
 template <int NC, int NR>
-__global__ void __launch_bounds__(kCGThreads) cg_stencil_ir_kernel(StencilCG a) {
+__global__ void __launch_bounds__(kCGThreads) cg_stencil_ir_kernel(const __grid_constant__ StencilCG a) {
   constexpr int U = NC * NR;
   constexpr int NS = n_systems<NC, NR>();
   __shared__ double s_red[2 * 3][kCGWarps];
-  __shared__ double s_c[27 * NC * NC];
-  __shared__ float s_c32[27 * NC * NC];
-  const double *c = stage_coef<double, NC>(a.S.c64, s_c);
-  const float *c32 = stage_coef<float, NC>(a.S.c32, s_c32);
   const int64_t n = a.S.n;
   const int64_t d0 = min(n, (int64_t)blockIdx.x * a.dofs_per_cta);
   const int64_t d1 = min(n, d0 + a.dofs_per_cta);
   const bool use_init = a.use_init_dev ? (__ldcg(a.use_init_dev) != 0) : (a.use_init_host != 0);
   const unsigned long long tns = a.timeout_ns;
+  const double delta = a.inner_tol;
   int par = 0;
 
-  double bb[NS];
+  // ---- prologue: r = b - A x (FP64), r32 = p32 = r, d = 0; ||b||, ||r||
+  double v[2 * NS];
 #pragma unroll
-  for (int j = 0; j < NS; ++j) bb[j] = 0.0;
-  for (int64_t dof = d0 + threadIdx.x; dof < d1; dof += kCGThreads)
+  for (int j = 0; j < 2 * NS; ++j) v[j] = 0.0;
+  for (int64_t dof = d0 + threadIdx.x; dof < d1; dof += kCGThreads) {
+    double y[U];
+    if (use_init) apply<double, NC, NR>(a.S, a.x, (int)dof, y);
 #pragma unroll
     for (int u = 0; u < U; ++u) {
       const int64_t i = uidx<NC, NR>(n, dof, u);
       const double bi = a.b[i];
+      const double ri = use_init ? bi - y[u] : bi;
       if (!use_init) a.x[i] = 0.0;
-      bb[sys_of<NC, NR>(u)] = fma(bi, bi, bb[sys_of<NC, NR>(u)]);
+      const float rf = (float)ri;
+      a.r32[i] = rf;
+      a.p32[i] = rf;
+      a.d32[i] = 0.0f;
+      const int s = sys_of<NC, NR>(u);
+      v[s] = fma(bi, bi, v[s]);
+      v[NS + s] = fma(ri, ri, v[NS + s]);
     }
-  if (!grid_sum<NS>(bb, a.part, par, a.bar, tns, s_red)) {
+  }
+  if (!grid_sum<2 * NS>(v, a.part, par, a.bar, tns, s_red)) {
     set_status(a.info, CPM_BARRIER_TIMEOUT);
     return;
   }
-  double atol[NS], resid[NS];
+  double atol[NS], resid[NS], rho[NS], r0[NS];
   int active[NS], iters[NS];
   bool any = false;
 #pragma unroll
   for (int j = 0; j < NS; ++j) {
-    const double bn = sqrt(bb[j]);
+    const double bn = sqrt(v[j]);
     atol[j] = a.tol * bn;
-    resid[j] = bn;
+    rho[j] = v[NS + j];
+    resid[j] = sqrt(v[NS + j]);
+    r0[j] = resid[j];
     active[j] = bn != 0.0;
     iters[j] = 0;
     any |= active[j] != 0;
@@ -376,124 +265,136 @@ __global__ void __launch_bounds__(kCGThreads) cg_stencil_ir_kernel(StencilCG a) 
         if (!active[sys_of<NC, NR>(u)]) a.x[uidx<NC, NR>(n, dof, u)] = a.b[uidx<NC, NR>(n, dof, u)];
   }
   int status = CPM_OK;
-  int outer = 0, total = 0;
-  while (any) {
-    // ---- refinement residual in FP64: r = b - A x; FP32 copies; d = 0
-    if (!grid_sync(a.bar, gridDim.x, tns)) { status = CPM_BARRIER_TIMEOUT; break; }
-    double red[2 * NS];
+  int updates = 0;
+  for (int k = 0; any && k < a.maxiter; ++k) {
+    if (k > 0 && !grid_sync(a.bar, gridDim.x, tns)) { status = CPM_BARRIER_TIMEOUT; break; }
+    // ---- phase 1: q = A32 p, partial p.q
+    // per-thread partials in FP32 (a thread owns a few dozen DOFs), summed in FP64 across threads
+    float pqf[NS];
 #pragma unroll
-    for (int j = 0; j < 2 * NS; ++j) red[j] = 0.0;
+    for (int j = 0; j < NS; ++j) pqf[j] = 0.0f;
     for (int64_t dof = d0 + threadIdx.x; dof < d1; dof += kCGThreads) {
-      double y[U];
-      apply<double, NC, NR>(a.S, c, a.x, dof, y);
+      float y[U];
+      apply<float, NC, NR>(a.S, a.p32, (int)dof, y);
 #pragma unroll
       for (int u = 0; u < U; ++u) {
         const int64_t i = uidx<NC, NR>(n, dof, u);
-        const double ri = a.b[i] - y[u];
-        const float rf = (float)ri;
-        a.r32[i] = rf;
-        a.p32[i] = rf;
-        a.d32[i] = 0.0f;
+        a.q32[i] = y[u];
         const int s = sys_of<NC, NR>(u);
-        red[s] = fma(ri, ri, red[s]);
-        red[NS + s] = fma((double)rf, (double)rf, red[NS + s]);
+        pqf[s] = fmaf(a.p32[i], y[u], pqf[s]);
       }
     }
-    if (!grid_sum<2 * NS>(red, a.part, par, a.bar, tns, s_red)) { status = CPM_BARRIER_TIMEOUT; break; }
-    any = false;
-    double rho[NS], iatol[NS];
-    int iact[NS];
-    bool iany = false;
+    double pq[NS];
+#pragma unroll
+    for (int j = 0; j < NS; ++j) pq[j] = (double)pqf[j];
+    if (!grid_sum<NS>(pq, a.part, par, a.bar, tns, s_red)) { status = CPM_BARRIER_TIMEOUT; break; }
+    double alpha[NS];
+    bool bad = false;
 #pragma unroll
     for (int j = 0; j < NS; ++j) {
-      if (active[j]) {
-        resid[j] = sqrt(red[j]);
-        if (!(resid[j] > atol[j])) active[j] = 0;
-      }
-      any |= active[j] != 0;
-      rho[j] = red[NS + j];
-      iact[j] = active[j];
-      iatol[j] = a.inner_tol * sqrt(red[NS + j]);
-      iany |= iact[j] != 0;
+      alpha[j] = active[j] ? rho[j] / pq[j] : 0.0;
+      if (active[j] && !isfinite(alpha[j])) bad = true;
     }
-    if (!any || outer >= a.max_outer || total >= a.maxiter) break;
-    ++outer;
-    // ---- inner FP32 CG on A d = r
-    for (int kin = 0; iany && total < a.maxiter; ++kin, ++total) {
-      if (kin > 0 && !grid_sync(a.bar, gridDim.x, tns)) { status = CPM_BARRIER_TIMEOUT; break; }
-      double pq[NS];
+    if (bad) { status = CPM_NONFINITE; break; }
+    // ---- phase 2: d += alpha p, r32 -= alpha q, partial r32.r32
+    float rrf[NS], af[NS];
 #pragma unroll
-      for (int j = 0; j < NS; ++j) pq[j] = 0.0;
-      for (int64_t dof = d0 + threadIdx.x; dof < d1; dof += kCGThreads) {
-        float y[U];
-        apply<float, NC, NR>(a.S, c32, a.p32, dof, y);
-#pragma unroll
-        for (int u = 0; u < U; ++u) {
-          const int64_t i = uidx<NC, NR>(n, dof, u);
-          a.q32[i] = y[u];
-          const int s = sys_of<NC, NR>(u);
-          pq[s] = fma((double)a.p32[i], (double)y[u], pq[s]);
-        }
-      }
-      if (!grid_sum<NS>(pq, a.part, par, a.bar, tns, s_red)) { status = CPM_BARRIER_TIMEOUT; break; }
-      double alpha[NS];
-      bool bad = false;
-#pragma unroll
-      for (int j = 0; j < NS; ++j) {
-        alpha[j] = iact[j] ? rho[j] / pq[j] : 0.0;
-        if (iact[j] && !isfinite(alpha[j])) bad = true;
-      }
-      if (bad) { status = CPM_NONFINITE; break; }
-      double rr[NS];
-#pragma unroll
-      for (int j = 0; j < NS; ++j) rr[j] = 0.0;
-      for (int64_t dof = d0 + threadIdx.x; dof < d1; dof += kCGThreads) {
-#pragma unroll
-        for (int u = 0; u < U; ++u) {
-          const int s = sys_of<NC, NR>(u);
-          if (!iact[s]) continue;
-          const int64_t i = uidx<NC, NR>(n, dof, u);
-          const float af = (float)alpha[s];
-          a.d32[i] = fmaf(af, a.p32[i], a.d32[i]);
-          const float rn = fmaf(-af, a.q32[i], a.r32[i]);
-          a.r32[i] = rn;
-          rr[s] = fma((double)rn, (double)rn, rr[s]);
-        }
-      }
-      if (!grid_sum<NS>(rr, a.part, par, a.bar, tns, s_red)) { status = CPM_BARRIER_TIMEOUT; break; }
-      iany = false;
-      float beta[NS];
-#pragma unroll
-      for (int j = 0; j < NS; ++j) {
-        beta[j] = 0.0f;
-        if (!iact[j]) continue;
-        if (!isfinite(rr[j])) bad = true;
-        iters[j] += 1;
-        beta[j] = (float)(rr[j] / rho[j]);
-        rho[j] = rr[j];
-        if (sqrt(rr[j]) <= iatol[j]) iact[j] = 0;
-        iany |= iact[j] != 0;
-      }
-      if (bad) { status = CPM_NONFINITE; break; }
-      if (!iany) break;
-      for (int64_t dof = d0 + threadIdx.x; dof < d1; dof += kCGThreads) {
-#pragma unroll
-        for (int u = 0; u < U; ++u) {
-          const int s = sys_of<NC, NR>(u);
-          if (!iact[s]) continue;
-          const int64_t i = uidx<NC, NR>(n, dof, u);
-          a.p32[i] = fmaf(beta[s], a.p32[i], a.r32[i]);
-        }
-      }
+    for (int j = 0; j < NS; ++j) {
+      rrf[j] = 0.0f;
+      af[j] = (float)alpha[j];
     }
-    if (status != CPM_OK) break;
-    // ---- x += d (own DOFs only; the next residual pass starts with a barrier)
-    for (int64_t dof = d0 + threadIdx.x; dof < d1; dof += kCGThreads)
+    for (int64_t dof = d0 + threadIdx.x; dof < d1; dof += kCGThreads) {
 #pragma unroll
       for (int u = 0; u < U; ++u) {
+        const int s = sys_of<NC, NR>(u);
+        if (!active[s]) continue;
         const int64_t i = uidx<NC, NR>(n, dof, u);
-        if (active[sys_of<NC, NR>(u)]) a.x[i] += (double)a.d32[i];
+        a.d32[i] = fmaf(af[s], a.p32[i], a.d32[i]);
+        const float rn = fmaf(-af[s], a.q32[i], a.r32[i]);
+        a.r32[i] = rn;
+        rrf[s] = fmaf(rn, rn, rrf[s]);
       }
+    }
+    double rr[NS];
+#pragma unroll
+    for (int j = 0; j < NS; ++j) rr[j] = (double)rrf[j];
+    if (!grid_sum<NS>(rr, a.part, par, a.bar, tns, s_red)) { status = CPM_BARRIER_TIMEOUT; break; }
+    bool upd = false;
+    int need[NS];
+#pragma unroll
+    for (int j = 0; j < NS; ++j) {
+      need[j] = 0;
+      if (!active[j]) continue;
+      if (!isfinite(rr[j])) bad = true;
+      iters[j] += 1;
+      const double rn = sqrt(rr[j]);
+      need[j] = (rn < delta * r0[j]) || (rn <= atol[j]) || (k + 1 >= a.maxiter);
+      upd |= need[j] != 0;
+    }
+    if (bad) { status = CPM_NONFINITE; break; }
+    double rnew[NS];
+#pragma unroll
+    for (int j = 0; j < NS; ++j) rnew[j] = rr[j];
+    if (upd) {
+      // ---- reliable update: x += d (FP64), d = 0 (own DOFs), then r = b - A64 x
+      ++updates;
+      for (int64_t dof = d0 + threadIdx.x; dof < d1; dof += kCGThreads)
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+          const int s = sys_of<NC, NR>(u);
+          if (!need[s]) continue;
+          const int64_t i = uidx<NC, NR>(n, dof, u);
+          a.x[i] += (double)a.d32[i];
+          a.d32[i] = 0.0f;
+        }
+      if (!grid_sync(a.bar, gridDim.x, tns)) { status = CPM_BARRIER_TIMEOUT; break; }
+      double tr[NS];
+#pragma unroll
+      for (int j = 0; j < NS; ++j) tr[j] = 0.0;
+      for (int64_t dof = d0 + threadIdx.x; dof < d1; dof += kCGThreads) {
+        double y[U];
+        apply<double, NC, NR>(a.S, a.x, (int)dof, y);
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+          const int s = sys_of<NC, NR>(u);
+          if (!need[s]) continue;
+          const int64_t i = uidx<NC, NR>(n, dof, u);
+          const double ri = a.b[i] - y[u];
+          a.r32[i] = (float)ri;
+          tr[s] = fma(ri, ri, tr[s]);
+        }
+      }
+      if (!grid_sum<NS>(tr, a.part, par, a.bar, tns, s_red)) { status = CPM_BARRIER_TIMEOUT; break; }
+#pragma unroll
+      for (int j = 0; j < NS; ++j) {
+        if (!need[j]) continue;
+        resid[j] = sqrt(tr[j]);
+        r0[j] = resid[j];
+        rnew[j] = tr[j];
+        if (resid[j] <= atol[j]) active[j] = 0;
+      }
+    }
+    any = false;
+    float beta[NS];
+#pragma unroll
+    for (int j = 0; j < NS; ++j) {
+      beta[j] = 0.0f;
+      if (!active[j]) continue;
+      beta[j] = (float)(rnew[j] / rho[j]);
+      rho[j] = rnew[j];
+      any = true;
+    }
+    if (!any || k + 1 >= a.maxiter) break;
+    // ---- phase 3: p = r32 + beta p
+    for (int64_t dof = d0 + threadIdx.x; dof < d1; dof += kCGThreads) {
+#pragma unroll
+      for (int u = 0; u < U; ++u) {
+        const int s = sys_of<NC, NR>(u);
+        if (!active[s]) continue;
+        const int64_t i = uidx<NC, NR>(n, dof, u);
+        a.p32[i] = fmaf(beta[s], a.p32[i], a.r32[i]);
+      }
+    }
   }
   if (blockIdx.x == 0 && threadIdx.x == 0) {
     int st = status;
@@ -503,7 +404,7 @@ __global__ void __launch_bounds__(kCGThreads) cg_stencil_ir_kernel(StencilCG a) 
       a.info->iters[j] = iters[j];
       a.info->resid[j] = resid[j];
     }
-    a.info->outer = outer;
+    a.info->outer = updates;
     set_status(a.info, st);
   } else if (status != CPM_OK && threadIdx.x == 0) {
     set_status(a.info, status);
@@ -512,13 +413,11 @@ __global__ void __launch_bounds__(kCGThreads) cg_stencil_ir_kernel(StencilCG a) 
 
 // ---------------------------------------------------------------- y = alpha A x (FP64)
 template <int NC, int NR>
-__global__ void __launch_bounds__(256) stencil_apply_kernel(StencilOp S, const double *x, double *y, double alpha) {
-  __shared__ double s_c[27 * NC * NC];
-  const double *c = stage_coef<double, NC>(S.c64, s_c);
+__global__ void __launch_bounds__(256) stencil_apply_kernel(const __grid_constant__ StencilOp S, const double *x, double *y, double alpha) {
   for (int64_t dof = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; dof < S.n;
        dof += (int64_t)gridDim.x * blockDim.x) {
     double t[NC * NR];
-    apply<double, NC, NR>(S, c, x, dof, t);
+    apply<double, NC, NR>(S, x, (int)dof, t);
 #pragma unroll
     for (int u = 0; u < NC * NR; ++u) y[uidx<NC, NR>(S.n, dof, u)] = alpha * t[u];
   }
@@ -529,16 +428,20 @@ static StencilOp to_op(const cpm_stencil *s) {
   S.nx = s->nx;
   S.ny = s->ny;
   S.nz = s->nz;
-  S.n = (int64_t)s->nx * s->ny * s->nz;
-  S.c64 = s->coef;
-  S.c32 = s->coef32;
+  S.n = s->nx * s->ny * s->nz;
   S.flags = s->flags;
+  const int nc = 27 * s->ncomp * s->ncomp;
+  for (int i = 0; i < 243; ++i) {
+    S.c64[i] = i < nc ? s->coef[i] : 0.0;
+    S.c32[i] = (float)S.c64[i];
+  }
   return S;
 }
 
 static int check_stencil(const cpm_stencil *s, const char *who) {
-  if (!s || !s->coef || s->nx < 3 || s->ny < 3 || s->nz < 3 || (s->ncomp != 1 && s->ncomp != 3)) {
-    set_error("%s: bad stencil (needs coefficients, at least 3 cells per axis, ncomp 1 or 3)", who);
+  if (!s || s->nx < 3 || s->ny < 3 || s->nz < 3 || (s->ncomp != 1 && s->ncomp != 3) ||
+      (int64_t)s->nx * s->ny * s->nz * s->ncomp >= (int64_t)1 << 31) {
+    set_error("%s: bad stencil (at least 3 cells per axis, ncomp 1 or 3, fewer than 2^31 unknowns)", who);
     return CPM_BAD_ARG;
   }
   return CPM_OK;
@@ -555,7 +458,7 @@ static int launch_stencil_cg(const cpm_stencil *s, const double *b, double *x, c
   a.maxiter = o->maxiter;
   a.use_init_host = o->use_init_host;
   a.use_init_dev = o->use_init_dev;
-  a.inner_tol = o->inner_tol > 0 ? o->inner_tol : 1e-4;
+  a.inner_tol = o->inner_tol > 0 ? o->inner_tol : 0.1;
   a.max_outer = o->max_outer > 0 ? o->max_outer : 60;
   a.r = w.r;
   a.p = w.p0;
@@ -606,10 +509,6 @@ extern "C" int cpm_cg_solve_stencil(const cpm_stencil *S, const double *b, doubl
     return CPM_BAD_ARG;
   }
   const int prec = opts->precision ? 1 : 0;
-  if (prec && !S->coef32) {
-    set_error("cpm_cg_solve_stencil: mixed precision needs the FP32 coefficients");
-    return CPM_BAD_ARG;
-  }
   const int64_t n = (int64_t)S->nx * S->ny * S->nz;
   const int64_t unknowns = n * S->ncomp;
   const size_t need = layout(unknowns, nrhs, prec, nullptr, nullptr);

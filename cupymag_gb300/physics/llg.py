@@ -131,8 +131,21 @@ class LLGSolver:
         self.solver.launch(A, b, x, self.info[k], tol=self.p.tol, maxiter=self.p.maxiter,
                            use_init_dev=self.use_init, precision=self.precision)
 
+    def cg_request(self, A, b, x, k):
+        """A solve of this step, for an executor that batches solves of several runs."""
+        return CGRequest(self, A, b, x, k)
+
+    @staticmethod
+    def _run(gen):
+        for req in gen:
+            req.execute()
+
     def magnetoelastic_strain(self):
         """E from mechanical equilibrium at the current m (Micromagnetics.py:114-164)."""
+        self._run(self._me_gen())
+        return self.E
+
+    def _me_gen(self):
         L, s = N.lib(), N.stream_ptr()
         n, p = self.n, self.p
         R9 = self.R9_dev.data_ptr() if self.rot else None
@@ -141,7 +154,7 @@ class LLGSolver:
                 "cpm_build_E0")
         self.F_el.spmv(self.E0, out=self.b_el)
         self.launches += 5 + (1 if self.rot else 0)
-        self._cg(self.A_el, self.b_el, self.u, 0)
+        yield self.cg_request(self.A_el, self.b_el, self.u, 0)
         self.Deriv.strain_into(self.u, self.E, self.R9_dev if self.rot else None)
         self.Avg.average_into(self.E, self.avgE)
         if self.rot:
@@ -152,15 +165,17 @@ class LLGSolver:
         N.check(L.cpm_strain_finalize(n, self.E.data_ptr(), self.avgE.data_ptr(), am.data_ptr(), p.lambda100,
                                       p.lambda111, self.Es_dev.data_ptr(), self.M36_dev.data_ptr(),
                                       self.MinvT36_dev.data_ptr(), 1 if self.rot else 0, s), "cpm_strain_finalize")
-        return self.E
 
     def demag_field(self):
         """H~ = -F U with U from the pinned demag Poisson solve (Micromagnetics.py:166-171)."""
+        self._run(self._demag_gen())
+        return self.Ht
+
+    def _demag_gen(self):
         self.Deriv.demag_rhs_into(self.m, self.avg_m, self.bdemag, pin=0)
         self.launches += 2
-        self._cg(self.A_demag, self.bdemag, self.U, 1)
+        yield self.cg_request(self.A_demag, self.bdemag, self.U, 1)
         self.Deriv.hd_into(self.U, self.Ht)
-        return self.Ht
 
     def effective_field(self, mm, dt, Hext, f_out=None, t_out=None):
         """f(mm) and t = f dt + mm (Micromagnetics.py:175-215 / :239-278)."""
@@ -174,26 +189,29 @@ class LLGSolver:
 
     def gs_projection_step(self, Hext):
         """Gauss-Seidel projection with the current fields, then renormalisation (:213-307)."""
+        self._run(self._gs_gen(Hext))
+
+    def _gs_gen(self, Hext):
         L, s, n, p = N.lib(), N.stream_ptr(), self.n, self.p
         dt = p.dt
         self.effective_field(self.m, dt, Hext, f_out=self.f, t_out=self.t)
         self.launches += 8  # 4 SpMV, 3 star updates, 1 renormalisation (fields and CGs count themselves)
         self.F1.spmv(self.t, out=self.b3)
-        self._cg(self.A1, self.b3, self.g, 2)
+        yield self.cg_request(self.A1, self.b3, self.g, 2)
         mp, gp = self.m.data_ptr(), self.g.data_ptr()
         N.check(L.cpm_gs_star(1, n, mp, gp, None, None, self.f.data_ptr(), dt, self.mstar.data_ptr(),
                               self.t1.data_ptr(), s), "cpm_gs_star")
         self.F1.spmv(self.t1, out=self.b1)
-        self._cg(self.A1, self.b1, self.g1s, 3)
+        yield self.cg_request(self.A1, self.b1, self.g1s, 3)
         N.check(L.cpm_gs_star(2, n, mp, gp, self.g1s.data_ptr(), None, self.f.data_ptr(), dt,
                               self.mstar.data_ptr(), self.t1.data_ptr(), s), "cpm_gs_star")
         self.F1.spmv(self.t1, out=self.b1)
-        self._cg(self.A1, self.b1, self.g2s, 4)
+        yield self.cg_request(self.A1, self.b1, self.g2s, 4)
         N.check(L.cpm_gs_star(3, n, mp, gp, self.g1s.data_ptr(), self.g2s.data_ptr(), None, dt,
                               self.mstar.data_ptr(), None, s), "cpm_gs_star")
         self.effective_field(self.mstar, dt * p.alpha_damp, Hext, t_out=self.t)
         self.F1.spmv(self.t, out=self.b3)
-        self._cg(self.A2, self.b3, self.mss, 5)
+        yield self.cg_request(self.A2, self.b3, self.mss, 5)
         w, V = self.Avg.weights()
         N.check(L.cpm_renorm_sumsq(n, self.mss.data_ptr(), self.defect.data_ptr(), self.m.data_ptr(),
                                    self.m_prev.data_ptr(), w.data_ptr(), V, self.thresh, self.sumsq.data_ptr(),
@@ -202,10 +220,18 @@ class LLGSolver:
 
     def step(self, Hext):
         """One GSPM step at applied field Hext (normalised by Ms); asynchronous."""
+        self._run(self.step_gen(Hext))
+
+    def step_gen(self, Hext):
+        """The step as a generator that yields each linear solve (CGRequest) before it is needed.
+
+        The caller executes every yielded request before resuming; a batching
+        executor can collect the requests of several runs and solve them in
+        one launch."""
         if self.ME:
-            self.magnetoelastic_strain()
-        self.demag_field()
-        self.gs_projection_step(Hext)
+            yield from self._me_gen()
+        yield from self._demag_gen()
+        yield from self._gs_gen(Hext)
         self.nstep += 1
 
     # ------------------------------------------------------------------ results
@@ -238,6 +264,22 @@ class LLGSolver:
             nrhs = 3 if k in (2, 5) else 1
             raise_for(inf[k], A, b, x, system=SOLVE_NAMES[k], nrhs=nrhs)
         return inf
+
+
+class CGRequest:
+    """One linear solve of an LLG step: A x = b with the solver's tolerances and warm-start flag."""
+
+    __slots__ = ("run", "A", "b", "x", "k")
+
+    def __init__(self, run, A, b, x, k):
+        self.run, self.A, self.b, self.x, self.k = run, A, b, x, k
+
+    @property
+    def kind(self):
+        return (getattr(self.A, "ncomp", 0), 1 if self.b.dim() == 1 else self.b.shape[1], self.k)
+
+    def execute(self):
+        self.run._cg(self.A, self.b, self.x, self.k)
 
 
 def effective_field(solver: LLGSolver, m, Hext, dt=None):

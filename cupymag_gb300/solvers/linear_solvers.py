@@ -31,7 +31,7 @@ class CGSolver:
         self.device = device or torch.device("cuda", torch.cuda.current_device())
         self._ws = {}
         self.barrier_timeout_s = 2.0
-        self.inner_tol = 1e-4
+        self.inner_tol = 0.1   # reliable-update factor of the mixed-precision solver
         self.max_outer = 60
 
     def workspace(self, n, nrhs, prec):

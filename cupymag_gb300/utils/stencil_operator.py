@@ -12,7 +12,7 @@ import torch
 
 from .. import _native as N
 
-ROW_IDENTITY, ROW_ZERO, COL_EXCLUDED = 1, 2, 4
+ROW_IDENTITY, ROW_ZERO, COL_EXCLUDED, NEAR_EXCLUDED = 1, 2, 4, 8
 
 
 class StencilOperator:
@@ -21,16 +21,29 @@ class StencilOperator:
         coef = np.asarray(coef, dtype=np.float64).reshape(-1)
         self.ncomp = {27: 1, 243: 3}[coef.size]
         dev = device or torch.device("cuda", torch.cuda.current_device())
-        self.coef = torch.as_tensor(coef, device=dev)
-        self.coef32 = self.coef.to(torch.float32)
-        self.flags = None if flags is None else torch.as_tensor(np.asarray(flags, dtype=np.uint8), device=dev)
+        self.coef_host = coef.copy()
+        self._dev = torch.device(dev)
         self.n = self.nx * self.ny * self.nz
+        if flags is not None:
+            flags = self.mark_neighbours(np.asarray(flags, dtype=np.uint8).copy())
+        self.flags = None if flags is None else torch.as_tensor(flags, device=dev)
         self.shape = (self.n * self.ncomp, self.n * self.ncomp)
         self._struct = None
 
     @property
     def device(self):
-        return self.coef.device
+        return self._dev
+
+    def mark_neighbours(self, f):
+        """Set NEAR_EXCLUDED on every DOF that has an excluded column among its 27 neighbours."""
+        ex = (f & COL_EXCLUDED).astype(bool).reshape(self.nx, self.ny, self.nz)
+        near = np.zeros_like(ex)
+        for dx in (-1, 0, 1):
+            for dy in (-1, 0, 1):
+                for dz in (-1, 0, 1):
+                    near |= np.roll(ex, (dx, dy, dz), axis=(0, 1, 2))
+        f[near.reshape(-1)] |= NEAR_EXCLUDED
+        return f
 
     def ensure_fp32(self):
         return self
@@ -39,8 +52,7 @@ class StencilOperator:
         if self._struct is None:
             s = N.Stencil()
             s.nx, s.ny, s.nz, s.ncomp = self.nx, self.ny, self.nz, self.ncomp
-            s.coef = self.coef.data_ptr()
-            s.coef32 = self.coef32.data_ptr()
+            s.coef[:self.coef_host.size] = tuple(float(v) for v in self.coef_host)
             s.flags = None if self.flags is None else self.flags.data_ptr()
             self._struct = s
         return self._struct

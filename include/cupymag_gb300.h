@@ -50,7 +50,7 @@ typedef struct {
 typedef struct {
   int32_t status;          /* cpm_status of the solve */
   int32_t iters[3];        /* CG iterations per right-hand side */
-  int32_t outer;           /* refinement sweeps (mixed precision) */
+  int32_t outer;           /* reliable updates (mixed precision) */
   int32_t pad;
   double resid[3];         /* final ||r|| per right-hand side */
   double bnorm[3];         /* ||b|| per right-hand side */
@@ -62,9 +62,9 @@ typedef struct {
   int32_t maxiter;
   int32_t use_init_host;   /* x holds the initial guess (if use_init_dev is NULL) */
   const int32_t *use_init_dev; /* device flag read at launch time, or NULL */
-  int32_t precision;       /* 0 = FP64 CG, 1 = FP32 CG inside FP64 refinement */
-  double inner_tol;        /* relative tolerance of each FP32 inner solve */
-  int32_t max_outer;       /* refinement sweep limit */
+  int32_t precision;       /* 0 = FP64 CG, 1 = FP32 CG with FP64 reliable updates */
+  double inner_tol;        /* reliable update when the FP32 residual fell by this factor (default 0.1) */
+  int32_t max_outer;       /* unused (kept for layout) */
   int32_t pad;
   double barrier_timeout_s;/* bound on every grid-barrier wait (seconds) */
 } cpm_cg_opts;
@@ -126,15 +126,18 @@ int cpm_cg_solve_noalloc(const cpm_csr *A, const double *b, double *x, int nrhs,
  * is the coefficient between component a of DOF p and component b of DOF
  * p + (dx,dy,dz) (wrapped), DOF = (i*ny + j)*nz + k -- exactly the values of
  * the CSR rows built by structured assembly (assemble_demag.py:186-233,
- * assemble_Gauss_Seidel.py:163-214, assemble_elasticity.py:350-459).
- * flags (uint8 per DOF, may be NULL): 1 = unit row (anchors, defect DOFs of
- * A1/A2), 2 = empty row (defect rows of the mass matrix), 4 = the DOF's
- * column is dropped from every other row (final_assembly.py:59-158). */
+ * assemble_Gauss_Seidel.py:163-214, assemble_elasticity.py:350-459).  The
+ * coefficients are host values (this struct lives in host memory); the
+ * kernels receive them as launch parameters.
+ * flags (device uint8 per DOF, may be NULL): 1 = unit row (anchors, defect
+ * DOFs of A1/A2), 2 = empty row (defect rows of the mass matrix), 4 = the
+ * DOF's column is dropped from every other row (final_assembly.py:59-158),
+ * 8 = some neighbour of this DOF carries flag 4 (its row takes the checked
+ * path; all other rows skip the per-neighbour flag tests). */
 typedef struct {
   int32_t nx, ny, nz;      /* cells per axis (>= 3), n = nx*ny*nz DOFs */
   int32_t ncomp;           /* 1: scalar operator; 3: elastic operator on [ux|uy|uz] */
-  const double *coef;      /* 27*ncomp*ncomp FP64 coefficients */
-  const float *coef32;     /* the same in FP32 (mixed precision), or NULL */
+  double coef[243];        /* 27*ncomp*ncomp FP64 coefficients (FP32 copies are rounded from these) */
   const uint8_t *flags;    /* per-DOF row/column flags, or NULL */
 } cpm_stencil;
 
