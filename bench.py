@@ -40,8 +40,9 @@ METRIC = "LLG steps/s & SpMV HBM GB/s vs plain FP64 at |m| err<=1e-6; serving p5
 # g1n, g2n, g3n, g1*, g2*, m1**, m2**, m3**), measured on the GPU; used only to
 # extrapolate the CPU sample of --impl reference, which cannot afford the
 # full solves (a full CPU step takes tens of minutes).
-REFERENCE_ITERS = {"hex128_me": [200, 60, 12, 12, 12, 12, 12, 14, 14, 14],
-                   "hex32_plain": [60, 12, 12, 12, 12, 12, 14, 14, 14]}
+REFERENCE_ITERS = {"hex128_me": [1930, 375, 22, 30, 30, 22, 29, 30, 44, 44],
+                   "hex64_me": [960, 190, 22, 30, 30, 22, 29, 30, 44, 44],
+                   "hex32_plain": [95, 22, 30, 30, 22, 29, 30, 44, 44]}
 
 
 def peaks():
@@ -180,6 +181,66 @@ def cpu_sample(p, S, iters_per_solve, cap=3):
             "per_iter_s": per_it, "cores": cores, "blas_threads": blas}
 
 
+# ------------------------------------------------------------------ plain FP64 beside the precision form
+def fp64_check(args, S, p, L, m0, fields):
+    """The same steps from the same m0 with every solve in FP64 (stencil operators); returns (solver, ms)."""
+    import torch
+    from cupymag_gb300.physics.llg import LLGSolver
+    ops = (None, L.Fx, L.Fy, L.Fz, L.Deriv, None, None, None, None, L.F_el, L.Avg)
+    R = LLGSolver(S, p, precision="DP", operators="stencil", ops=ops)
+    R.set_magnetization(torch.as_tensor(m0))
+    for s in range(args.warmup):
+        R.step(fields[s])
+        R.check()
+    stream = torch.cuda.current_stream()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for s in range(args.warmup, args.warmup + args.steps):
+        R.step(fields[s])
+    e1.record(stream)
+    torch.cuda.synchronize()
+    R.check()
+    return R, e0.elapsed_time(e1)
+
+
+# ------------------------------------------------------------------ serving sample
+def serving_sample(args):
+    """The first K requests of the serving stream through the engine (FP32 + FP64 refinement, real-time
+    Poisson arrivals), beside the same requests run one at a time in plain FP64 (each for its first few
+    steps, extrapolated to the full sweep with its own setup time)."""
+    import numpy as np
+    from cupymag_gb300.serving import ServingEngine, run_sequential, serving_requests
+    reqs = serving_requests()[:args.serve_requests]
+    res, st = ServingEngine("IR", hbm_budget_gb=args.hbm_budget_gb).serve(reqs, realtime=True)
+    seq, _ = run_sequential(reqs, precision="DP", max_steps=args.seq_steps)
+    t_seq, steps, errs = 0.0, 0, []
+    for r in reqs:
+        q = seq[r.rid]
+        t_steps = q.completed - q.admitted - q.setup_s
+        t_seq += q.setup_s + t_steps * r.steps / max(q.steps, 1)
+        steps += r.steps
+        a, b = res[r.rid].hist[:q.steps, :3], q.hist[:, :3]
+        if len(a) == len(b) and len(b):
+            errs.append(float(np.abs(a - b).max() / np.abs(b).max()))
+    seq_sps = steps / t_seq if t_seq > 0 else None
+    edges = [r.edge for r in reqs]
+    return {"requests": len(reqs), "arrivals": "Poisson 20/s", "edges": f"{min(edges)}..{max(edges)}",
+            "magnetoelastic": sum(r.ME for r in reqs), "steps_per_request": reqs[0].steps,
+            "precision": "f32+f64", "makespan_s": round(st.makespan_s, 3), "steps_per_s": round(st.steps_per_s, 2),
+            "latency_p50_s": round(st.latency_p50_s, 3), "latency_p99_s": round(st.latency_p99_s, 3),
+            "failed": st.failed, "mean_batch": round(st.mean_batch, 2), "max_batch": st.max_batch,
+            "graph_steps": st.graph_steps, "eager_steps": st.eager_steps, "captures": st.captures,
+            "graph_error": st.graph_error, "blockdiag_launches": st.blockdiag_launches,
+            "peak_budget_gb": round(st.peak_budget_gb, 2), "hbm_budget_gb": args.hbm_budget_gb,
+            "sequential_fp64_steps_per_s": None if seq_sps is None else round(seq_sps, 3),
+            "speedup_vs_sequential": None if not seq_sps else round(st.steps_per_s / seq_sps, 2),
+            "sequential_sample": (f"each request alone in plain FP64 (stencil operators, host check per step) for "
+                                  f"its first {args.seq_steps} steps, time per step x {reqs[0].steps} + setup"),
+            "avg_m_rel_err_vs_fp64_first_steps": max(errs) if errs else None}
+
+
 # ------------------------------------------------------------------ our arm
 def run_ours(args):
     import numpy as np
@@ -247,6 +308,7 @@ def run_ours(args):
     L._cg = orig_cg
     launches = L.launches - launches0
     L.check()
+    m_timed, avg_timed = L.m.clone(), L.avg_m.clone()
     ms = t0.elapsed_time(t1)
     # max over ranks
     t_tensor = torch.tensor([ms], device="cuda")
@@ -314,8 +376,27 @@ def run_ours(args):
         dist.all_reduce(e2e_t, op=dist.ReduceOp.MAX)
     e2e_value = world * args.steps / float(e2e_t.item())
 
+    fp64 = None
+    if args.precision != "DP" and not args.no_fp64_check:
+        R, ms64 = fp64_check(args, S, p, L, m0, fields)
+        v64 = args.steps / (ms64 / 1e3)
+        err_m = float((m_timed - R.m).abs().max())
+        err_avg = float((avg_timed - R.avg_m).abs().max() / R.avg_m.abs().max())
+        fp64 = {"steps_per_s": round(v64, 4), "ms_per_step": round(ms64 / args.steps, 3), "operators": "stencil",
+                "speedup": round(value / world / v64, 3), "max_abs_m_err": err_m, "avg_m_rel_err": err_avg,
+                "after_steps": args.warmup + args.steps, "bound": 1e-6}
+        del R
+        torch.cuda.empty_cache()
+
+    op_gb = sum(x.nbytes() for x in [L.A_demag, L.A1, L.A2, L.F1, L.Fx, L.F_el] + ([L.A_el] if L.ME else [])
+                if hasattr(x, "nbytes")) / 1e9
     line = None
     if rank == 0:
+        serving = None
+        if world == 1 and args.serve_requests > 0:
+            del L
+            torch.cuda.empty_cache()
+            serving = serving_sample(args)
         cpu = None
         if world == 1 and not args.no_cpu_baseline:
             try:
@@ -337,14 +418,14 @@ def run_ours(args):
                        "n_dof": S.n_dof, "magnetoelastic": w["ME"], "rot111": w["rot111"],
                        "precision": args.precision, "operators": ops_kind, "tol": p.tol, "sweep": f"+{w['B0']} T -> -{w['B0']} T over "
                        f"{w['steps']} steps", "timed_steps": f"{args.warmup}..{args.warmup + args.steps - 1}",
-                       "l2": "inputs larger than L2 (operators %.1f GB resident)" % (
-                           sum(x.nbytes() for x in [L.A_demag, L.A1, L.A2, L.F1, L.Fx, L.F_el] +
-                               ([L.A_el] if L.ME else []) if hasattr(x, "nbytes")) / 1e9),
+                       "l2": "inputs larger than L2 (operators %.1f GB resident)" % op_gb,
                        "parallelism": f"replicas x{world}", "setup_s": round(t_setup, 1),
                        "cg_iterations_per_step": [round(x, 1) for x in its_mean]},
             "e2e": {"value": round(e2e_value, 4), "unit": "steps/s",
                     "h2d_bytes_per_step": S.n_dof * 3 * 8, "d2h_bytes_per_step": S.n_dof * 3 * 8 + 24},
             "gpu_launches": launches,
+            "fp64": fp64,
+            "serving": serving,
             "roofline": roof,
             "cpu_baseline": cpu,
             "clocks": clk.summary(),
@@ -398,11 +479,17 @@ def main():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--workload", default="hex128_me")
-    ap.add_argument("--precision", default="DP", choices=["DP", "IR"])
+    ap.add_argument("--precision", default="IR", choices=["DP", "IR"],
+                    help="IR: FP32 CG with FP64 reliable updates (default); DP: plain FP64")
     ap.add_argument("--operators", default=None, choices=["csr", "stencil"],
                     help="solved operators as CSR or matrix-free stencils (default: csr for DP, stencil for IR)")
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-fp64-check", action="store_true", help="skip the plain FP64 run beside the IR form")
+    ap.add_argument("--serve-requests", type=int, default=32,
+                    help="requests of the serving stream to serve after the step benchmark (0: none)")
+    ap.add_argument("--seq-steps", type=int, default=5, help="steps per request of the sequential FP64 sample")
+    ap.add_argument("--hbm-budget-gb", type=float, default=150.0)
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

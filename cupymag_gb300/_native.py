@@ -45,7 +45,18 @@ class CGOpts(C.Structure):
 
 class FieldParams(C.Structure):
     _fields_ = [("K1", dbl), ("elasC1", dbl), ("elasC2", dbl), ("elasC3", dbl), ("lambda100", dbl),
-                ("Nd", dbl * 3), ("Hext", dbl * 3), ("R", dbl * 9), ("rot111", i32), ("has_E", i32)]
+                ("Nd", dbl * 3), ("Hext", dbl * 3), ("R", dbl * 9), ("rot111", i32), ("has_E", i32),
+                ("hext_sched", vp), ("hext_step", vp)]
+
+
+class BatchSystem(C.Structure):
+    _fields_ = [("nx", i32), ("ny", i32), ("nz", i32), ("maxiter", i32), ("tol", dbl), ("flags", vp), ("b", vp),
+                ("x", vp), ("use_init_dev", vp), ("info", vp), ("work", vp)]
+
+
+class BatchPlan(C.Structure):
+    _fields_ = [("dev", vp), ("bytes", i64), ("nsys", i32), ("grid", i32), ("ncomp", i32), ("nrhs", i32),
+                ("precision", i32), ("total_chunks", i32), ("coef", dbl * 243)]
 
 
 CG_INFO_BYTES = C.sizeof(CGInfo)
@@ -62,6 +73,12 @@ _PROTOS = {
     "cpm_stencil_apply": (C.c_int, [C.POINTER(Stencil), vp, vp, dbl, C.c_int, vp]),
     "cpm_cg_solve_stencil": (C.c_int, [C.POINTER(Stencil), vp, vp, C.c_int, C.POINTER(CGOpts), vp, C.c_size_t, vp,
                                        vp]),
+    "cpm_batch_work_bytes": (i64, [i64, i32, i32, i32]),
+    "cpm_batch_plan_bytes": (C.c_int, [C.POINTER(BatchSystem), i32, i32, i32, i32, C.POINTER(i64)]),
+    "cpm_batch_plan_build": (C.c_int, [C.POINTER(BatchSystem), i32, i32, i32, i32, vp, vp, i64, C.POINTER(BatchPlan),
+                                       vp]),
+    "cpm_cg_solve_blockdiag": (C.c_int, [C.POINTER(BatchPlan), C.POINTER(CGOpts), vp]),
+    "cpm_record_step": (C.c_int, [vp, vp, vp, vp, i32, vp]),
     "cpm_llg_field": (C.c_int, [C.POINTER(FieldParams), i64, vp, vp, vp, vp, dbl, vp, vp, vp]),
     "cpm_gs_star": (C.c_int, [C.c_int, i64, vp, vp, vp, vp, vp, dbl, vp, vp, vp]),
     "cpm_renorm_sumsq": (C.c_int, [i64, vp, vp, vp, vp, vp, dbl, dbl, vp, vp, vp, vp, vp]),

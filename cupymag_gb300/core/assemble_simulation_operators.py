@@ -107,18 +107,35 @@ class SimulationOperators:
     # ------------------------------------------------------------------ reference API
     def csr_demag_and_deriv(self):
         if self.structured:
-            e = self._cell()
-            A = self._scalar(e["K"], anchors=(0,))
-            Fs = [self._scalar(f) for f in e["F"]]
+            A = self._scalar(self._cell()["K"], anchors=(0,))
+        else:
+            A = DeviceCSR.from_scipy(self._coo()["A_demag"], self.device)
+        return (A, *self.derivative_operators())
+
+    def derivative_operators(self):
+        """Fx, Fy, Fz and ComputeDerivatives over them (without the demag matrix)."""
+        if self.structured:
+            Fs = [self._scalar(f) for f in self._cell()["F"]]
         else:
             ops = self._coo()
-            A = DeviceCSR.from_scipy(ops["A_demag"], self.device)
             Fs = [DeviceCSR.from_scipy(ops[k], self.device) for k in ("Fx", "Fy", "Fz")]
         # the three derivative matrices share one pattern: keep one index copy
         for f in Fs[1:]:
             if f.same_pattern(Fs[0]):
                 f.indptr, f.indices, f._struct = Fs[0].indptr, Fs[0].indices, None
-        return A, Fs[0], Fs[1], Fs[2], ComputeDerivatives(*Fs)
+        return Fs[0], Fs[1], Fs[2], ComputeDerivatives(*Fs)
+
+    def elastic_rhs_operator(self):
+        """F_el alone (the stencil path solves A_el matrix-free); None without ME."""
+        if not self.p.ME:
+            return None
+        if self.structured:
+            g, e, n = self.fem_grid, self._cell(), self.n_dof
+            SF = SH.stencil_from_element(e["Fel"], 3, 6)
+            ip, ix, dv = SH.elastic_F_csr(g.Nx, g.Ny, g.Nz, SF, self.device)
+            ip, ix, dv = SH.anchor(ip, ix, dv, (0, n, 2 * n), cols_too=False, diag_one=False)
+            return _device_csr(ip, ix, dv, (3 * n, 6 * n))
+        return DeviceCSR.from_scipy(self._coo()["F_el"], self.device)
 
     def csr_GS(self):
         if self.structured:
@@ -141,11 +158,7 @@ class SimulationOperators:
             ip, ix, dv = SH.elastic_A_csr(g.Nx, g.Ny, g.Nz, SA, self.device)
             ip, ix, dv = SH.anchor(ip, ix, dv, (0, n, 2 * n))
             A_el = _device_csr(ip, ix, dv, (3 * n, 3 * n))
-            SF = SH.stencil_from_element(e["Fel"], 3, 6)
-            ip, ix, dv = SH.elastic_F_csr(g.Nx, g.Ny, g.Nz, SF, self.device)
-            ip, ix, dv = SH.anchor(ip, ix, dv, (0, n, 2 * n), cols_too=False, diag_one=False)
-            F_el = _device_csr(ip, ix, dv, (3 * n, 6 * n))
-            return A_el, F_el
+            return A_el, self.elastic_rhs_operator()
         ops = self._coo()
         return DeviceCSR.from_scipy(ops["A_el"], self.device), DeviceCSR.from_scipy(ops["F_el"], self.device)
 

@@ -1,0 +1,735 @@
+// Block-diagonal conjugate gradient: many stencil systems in one persistent
+// cooperative launch (sm_103a).  This is the solver of the serving loop.
+//
+// A batch holds S independent systems A_s x_s = b_s of one operator kind
+// (scalar with 1 or 3 right-hand sides, or elastic) on periodic hex grids of
+// different sizes that share one coefficient table (requests with the same
+// material and time step).  Each system's DOFs are cut into chunks whose size
+// depends only on the operator kind; a chunk's partial dot products are
+// reduced in a fixed order, and a system's totals add its own chunks'
+// partials in a fixed order.  A system's iterates are therefore bit-for-bit
+// the same whether it is solved alone or together with any other systems:
+// the batch only changes which CTA works on which chunk.
+//
+// CTAs are given to systems in proportion to their chunks (equal load per
+// CTA).  All CTAs pass the same grid barriers; a system that has converged
+// idles, and the launch ends when a device counter of systems that are still
+// iterating drops to zero.  Every wait is bounded (GridBarrier).
+//
+// Precision 0 is the three-phase FP64 CG of csrc/stencil.cu.  Precision 1 is
+// FP32 CG with FP64 reliable updates in a form that needs no extra barrier:
+// when the FP32 recursive residual has fallen by inner_tol (or below the
+// stopping threshold, or at maxiter), the next iteration's first phase also
+// computes the true residual b - A64 (x + d) in FP64 beside q = A32 p; it
+// replaces the FP32 residual and rho, decides convergence, and the second
+// phase folds d into x.  The stopping test is only ever decided on the FP64
+// true residual.
+#include <algorithm>
+#include <cmath>
+#include <vector>
+
+#include "stencil_ops.cuh"
+
+namespace cpm {
+
+constexpr int kSlot = 8;  // doubles per chunk partial (>= 2 * 3 systems)
+
+// Grid geometry of one system in registers.
+struct Geo {
+  int nx, ny, nz, n;
+  const uint8_t *flags;
+};
+
+struct BSeg {
+  int nx, ny, nz, n;
+  const uint8_t *flags;
+  const double *b;
+  double *x;
+  const int *use_init_dev;
+  cpm_cg_info *info;
+  double tol;
+  int maxiter;
+  int chunk0, nchunks, cta0, ncta, chunk_dofs;
+  double *r, *p, *q;             // precision 0
+  float *r32, *p32, *q32, *d32;  // precision 1
+};
+
+struct BatchArgs {
+  double c64[243];
+  float c32[243];
+  const BSeg *segs;
+  const int *cta_seg;
+  double *part;          // two halves of total_chunks * kSlot doubles
+  long long half;
+  GridBarrier *bar;
+  int *live;             // systems (segments) still iterating
+  unsigned long long timeout_ns;
+  double inner_tol;
+};
+
+template <int NC, int NR>
+__host__ __device__ constexpr int b_systems() { return NC == 1 ? NR : 1; }
+
+template <int NC, int NR>
+__device__ __forceinline__ int b_sys(int comp) { return NC == 1 ? comp : 0; }
+
+// Partials of this CTA's chunks: body(d0, d1, v) accumulates the calling
+// thread's DOFs of [d0, d1) (stride kCGThreads) into v.
+template <int NV, typename Body>
+__device__ __forceinline__ void chunk_partials(const BSeg &S, int l, double *half, double (*sred)[kCGWarps],
+                                               Body body) {
+  for (int c = l; c < S.nchunks; c += S.ncta) {
+    double v[NV];
+#pragma unroll
+    for (int j = 0; j < NV; ++j) v[j] = 0.0;
+    const int d0 = c * S.chunk_dofs;
+    const int d1 = min(S.n, d0 + S.chunk_dofs);
+    body(d0, d1, v);
+    block_sum<NV>(v, sred);
+    double *dst = half + (size_t)(S.chunk0 + c) * kSlot;
+#pragma unroll
+    for (int j = 0; j < NV; ++j)
+      if (threadIdx.x == j) dst[j] = v[j];
+  }
+}
+
+// One reduction: this CTA's chunk partials (when `work`), a grid barrier, the
+// segment's totals in chunk order.  Every CTA calls it equally often; the
+// partial buffer alternates halves as in grid_sum.
+template <int NV, typename Body>
+__device__ __forceinline__ bool seg_reduce(const BatchArgs &a, const BSeg &S, int l, bool work, int &par,
+                                           double (*sred)[kCGWarps], double (&v)[NV], Body body) {
+  double *half = a.part + (size_t)par * (size_t)a.half;
+  par ^= 1;
+  if (work) chunk_partials<NV>(S, l, half, sred, body);
+  if (!grid_sync(a.bar, gridDim.x, a.timeout_ns)) return false;
+  if (work) {
+#pragma unroll
+    for (int j = 0; j < NV; ++j) v[j] = 0.0;
+    for (int c = threadIdx.x; c < S.nchunks; c += kCGThreads) {
+      const double *src = half + (size_t)(S.chunk0 + c) * kSlot;
+#pragma unroll
+      for (int j = 0; j < NV; ++j) v[j] += __ldcg(src + j);
+    }
+    block_sum<NV>(v, sred);
+  }
+  return true;
+}
+
+__device__ __forceinline__ void write_info(cpm_cg_info *info, int status, const int *iters, const double *resid,
+                                           int ns, int outer, const GridBarrier *bar) {
+  int st = status;
+  if (*(volatile const int *)&bar->error && st == CPM_OK) st = CPM_BARRIER_TIMEOUT;
+  for (int j = 0; j < 3; ++j) {
+    info->iters[j] = j < ns ? iters[j] : 0;
+    info->resid[j] = j < ns ? resid[j] : 0.0;
+  }
+  info->outer = outer;
+  info->pad = 0;
+  info->status = st;
+}
+
+// ---------------------------------------------------------------- FP64
+template <int NC, int NR>
+__global__ void __launch_bounds__(kCGThreads) cg_batched_fp64_kernel(const __grid_constant__ BatchArgs a) {
+  constexpr int U = NC * NR;
+  constexpr int NS = b_systems<NC, NR>();
+  __shared__ double s_red[2 * 3][kCGWarps];
+  const BSeg &S = a.segs[a.cta_seg[blockIdx.x]];
+  const int l = blockIdx.x - S.cta0;
+  const bool lead = l == 0 && threadIdx.x == 0;
+  const Geo g{S.nx, S.ny, S.nz, S.n, S.flags};
+  const int64_t n = g.n;
+  const double *__restrict__ b = S.b;
+  double *x = S.x, *r = S.r, *p = S.p, *q = S.q;
+  const double tol = S.tol;
+  const int maxiter = S.maxiter;
+  const bool use_init = S.use_init_dev && __ldcg(S.use_init_dev) != 0;
+  const double *c = a.c64;
+  int par = 0;
+
+  double v[2 * NS];
+  bool ok = seg_reduce<2 * NS>(a, S, l, true, par, s_red, v, [&](int d0, int d1, double (&w)[2 * NS]) {
+    for (int dof = d0 + threadIdx.x; dof < d1; dof += kCGThreads) {
+      double y[U];
+      if (use_init) apply_c<double, NC, NR>(g, c, x, dof, y);
+#pragma unroll
+      for (int u = 0; u < U; ++u) {
+        const int64_t i = uidx<NC, NR>(n, dof, u);
+        const double bi = b[i];
+        const double ri = use_init ? bi - y[u] : bi;
+        r[i] = ri;
+        p[i] = ri;
+        if (!use_init) x[i] = 0.0;
+        const int s = b_sys<NC, NR>(u);
+        w[s] = fma(bi, bi, w[s]);
+        w[NS + s] = fma(ri, ri, w[NS + s]);
+      }
+    }
+  });
+  double atol[NS], rho[NS], resid[NS];
+  int active[NS], iters[NS], unconv[NS];
+  bool any = false;
+  int status = ok ? CPM_OK : CPM_BARRIER_TIMEOUT;
+#pragma unroll
+  for (int j = 0; j < NS; ++j) {
+    const double bn = ok ? sqrt(v[j]) : 0.0;
+    atol[j] = tol * bn;
+    rho[j] = ok ? v[NS + j] : 0.0;
+    resid[j] = sqrt(rho[j]);
+    active[j] = bn != 0.0;
+    iters[j] = 0;
+    unconv[j] = 0;
+    any |= active[j] != 0;
+  }
+  if (lead) {
+    for (int j = 0; j < 3; ++j) S.info->bnorm[j] = j < NS ? sqrt(ok ? v[j] : 0.0) : 0.0;
+    if (any) atomicAdd(a.live, 1);
+  }
+  if (ok && use_init) {
+    for (int cc = l; cc < S.nchunks; cc += S.ncta) {
+      const int d1 = min(g.n, (cc + 1) * S.chunk_dofs);
+      for (int dof = cc * S.chunk_dofs + threadIdx.x; dof < d1; dof += kCGThreads)
+#pragma unroll
+        for (int u = 0; u < U; ++u)
+          if (!active[b_sys<NC, NR>(u)]) x[uidx<NC, NR>(n, dof, u)] = b[uidx<NC, NR>(n, dof, u)];
+    }
+  }
+  for (int k = 0; ok; ++k) {
+    if (k > 0) {
+      if (!grid_sync(a.bar, gridDim.x, a.timeout_ns)) { status = CPM_BARRIER_TIMEOUT; break; }
+      // every change of the counter happened before this barrier and none
+      // happens before the next one: all CTAs read the same value
+      if (__ldcg(a.live) == 0) break;
+    }
+    // ---- q = A p, p.q
+    double pq[NS];
+    if (!seg_reduce<NS>(a, S, l, any, par, s_red, pq, [&](int d0, int d1, double (&w)[NS]) {
+          for (int dof = d0 + threadIdx.x; dof < d1; dof += kCGThreads) {
+            double y[U];
+            apply_c<double, NC, NR>(g, c, p, dof, y);
+#pragma unroll
+            for (int u = 0; u < U; ++u) {
+              const int64_t i = uidx<NC, NR>(n, dof, u);
+              q[i] = y[u];
+              w[b_sys<NC, NR>(u)] = fma(p[i], y[u], w[b_sys<NC, NR>(u)]);
+            }
+          }
+        })) {
+      status = CPM_BARRIER_TIMEOUT;
+      break;
+    }
+    double alpha[NS];
+    bool bad = false;
+#pragma unroll
+    for (int j = 0; j < NS; ++j) {
+      alpha[j] = (any && active[j]) ? rho[j] / pq[j] : 0.0;
+      if (any && active[j] && !isfinite(alpha[j])) bad = true;
+    }
+    if (bad) {
+      status = CPM_NONFINITE;
+#pragma unroll
+      for (int j = 0; j < NS; ++j) active[j] = 0;
+      if (lead) atomicSub(a.live, 1);
+      any = false;
+    }
+    // ---- x += alpha p, r -= alpha q, r.r
+    double rr[NS];
+    if (!seg_reduce<NS>(a, S, l, any, par, s_red, rr, [&](int d0, int d1, double (&w)[NS]) {
+          for (int dof = d0 + threadIdx.x; dof < d1; dof += kCGThreads) {
+#pragma unroll
+            for (int u = 0; u < U; ++u) {
+              const int s = b_sys<NC, NR>(u);
+              if (!active[s]) continue;
+              const int64_t i = uidx<NC, NR>(n, dof, u);
+              x[i] = __fma_rn(alpha[s], p[i], x[i]);
+              const double rn = __fma_rn(-alpha[s], q[i], r[i]);
+              r[i] = rn;
+              w[s] = fma(rn, rn, w[s]);
+            }
+          }
+        })) {
+      status = CPM_BARRIER_TIMEOUT;
+      break;
+    }
+    if (!any) continue;
+    double beta[NS];
+    bool still = false;
+#pragma unroll
+    for (int j = 0; j < NS; ++j) {
+      beta[j] = 0.0;
+      if (!active[j]) continue;
+      if (!isfinite(rr[j])) bad = true;
+      iters[j] += 1;
+      beta[j] = rr[j] / rho[j];
+      rho[j] = rr[j];
+      resid[j] = sqrt(rr[j]);
+      if (resid[j] <= atol[j]) active[j] = 0;
+      else if (iters[j] >= maxiter) { active[j] = 0; unconv[j] = 1; }
+      still |= active[j] != 0;
+    }
+    if (bad) {
+      status = CPM_NONFINITE;
+      still = false;
+    }
+    if (!still) {
+      if (lead) atomicSub(a.live, 1);
+      any = false;
+      continue;
+    }
+    // ---- p = r + beta p
+    for (int cc = l; cc < S.nchunks; cc += S.ncta) {
+      const int d1 = min(g.n, (cc + 1) * S.chunk_dofs);
+      for (int dof = cc * S.chunk_dofs + threadIdx.x; dof < d1; dof += kCGThreads)
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+          const int s = b_sys<NC, NR>(u);
+          if (!active[s]) continue;
+          const int64_t i = uidx<NC, NR>(n, dof, u);
+          p[i] = __fma_rn(beta[s], p[i], r[i]);
+        }
+    }
+  }
+  if (lead) {
+    int st = status;
+#pragma unroll
+    for (int j = 0; j < NS; ++j)
+      if (st == CPM_OK && (unconv[j] || active[j])) st = CPM_NOT_CONVERGED;
+    write_info(S.info, st, iters, resid, NS, 0, a.bar);
+  }
+}
+
+// ---------------------------------------------------------------- FP32 + FP64 reliable updates
+template <int NC, int NR>
+__global__ void __launch_bounds__(kCGThreads) cg_batched_ir_kernel(const __grid_constant__ BatchArgs a) {
+  constexpr int U = NC * NR;
+  constexpr int NS = b_systems<NC, NR>();
+  __shared__ double s_red[2 * 3][kCGWarps];
+  const BSeg &S = a.segs[a.cta_seg[blockIdx.x]];
+  const int l = blockIdx.x - S.cta0;
+  const bool lead = l == 0 && threadIdx.x == 0;
+  const Geo g{S.nx, S.ny, S.nz, S.n, S.flags};
+  const int64_t n = g.n;
+  const double *__restrict__ b = S.b;
+  double *x = S.x;
+  float *r32 = S.r32, *p32 = S.p32, *q32 = S.q32, *d32 = S.d32;
+  const double tol = S.tol;
+  const int maxiter = S.maxiter;
+  const bool use_init = S.use_init_dev && __ldcg(S.use_init_dev) != 0;
+  const double delta = a.inner_tol;
+  int par = 0;
+
+  // ---- r = b - A64 x, r32 = p32 = r, d = 0; ||b||, ||r||
+  double v[2 * NS];
+  bool ok = seg_reduce<2 * NS>(a, S, l, true, par, s_red, v, [&](int d0, int d1, double (&w)[2 * NS]) {
+    for (int dof = d0 + threadIdx.x; dof < d1; dof += kCGThreads) {
+      double y[U];
+      if (use_init) apply_c<double, NC, NR>(g, a.c64, x, dof, y);
+#pragma unroll
+      for (int u = 0; u < U; ++u) {
+        const int64_t i = uidx<NC, NR>(n, dof, u);
+        const double bi = b[i];
+        const double ri = use_init ? bi - y[u] : bi;
+        if (!use_init) x[i] = 0.0;
+        r32[i] = (float)ri;
+        p32[i] = (float)ri;
+        d32[i] = 0.0f;
+        const int s = b_sys<NC, NR>(u);
+        w[s] = fma(bi, bi, w[s]);
+        w[NS + s] = fma(ri, ri, w[NS + s]);
+      }
+    }
+  });
+  double atol[NS], rho[NS], resid[NS], r0[NS];
+  int active[NS], need[NS], iters[NS], unconv[NS];
+  bool any = false;
+  int status = ok ? CPM_OK : CPM_BARRIER_TIMEOUT;
+  int updates = 0;
+#pragma unroll
+  for (int j = 0; j < NS; ++j) {
+    const double bn = ok ? sqrt(v[j]) : 0.0;
+    atol[j] = tol * bn;
+    rho[j] = ok ? v[NS + j] : 0.0;
+    resid[j] = sqrt(rho[j]);
+    r0[j] = resid[j];
+    active[j] = bn != 0.0;
+    need[j] = 0;
+    iters[j] = 0;
+    unconv[j] = 0;
+    any |= active[j] != 0;
+  }
+  if (lead) {
+    for (int j = 0; j < 3; ++j) S.info->bnorm[j] = j < NS ? sqrt(ok ? v[j] : 0.0) : 0.0;
+    if (any) atomicAdd(a.live, 1);
+  }
+  if (ok && use_init) {
+    for (int cc = l; cc < S.nchunks; cc += S.ncta) {
+      const int d1 = min(g.n, (cc + 1) * S.chunk_dofs);
+      for (int dof = cc * S.chunk_dofs + threadIdx.x; dof < d1; dof += kCGThreads)
+#pragma unroll
+        for (int u = 0; u < U; ++u)
+          if (!active[b_sys<NC, NR>(u)]) x[uidx<NC, NR>(n, dof, u)] = b[uidx<NC, NR>(n, dof, u)];
+    }
+  }
+  for (int k = 0; ok; ++k) {
+    if (k > 0) {
+      if (!grid_sync(a.bar, gridDim.x, a.timeout_ns)) { status = CPM_BARRIER_TIMEOUT; break; }
+      if (__ldcg(a.live) == 0) break;
+    }
+    bool pending = false;
+#pragma unroll
+    for (int j = 0; j < NS; ++j) pending |= need[j] != 0;
+    // ---- q = A32 p, p.q (FP32 per thread); pending updates: t = b - A64 (x + d), r32 = t, t.t
+    double pt[2 * NS];
+    if (!seg_reduce<2 * NS>(a, S, l, any, par, s_red, pt, [&](int d0, int d1, double (&w)[2 * NS]) {
+          float pqf[NS];
+#pragma unroll
+          for (int j = 0; j < NS; ++j) pqf[j] = 0.0f;
+          for (int dof = d0 + threadIdx.x; dof < d1; dof += kCGThreads) {
+            float y[U];
+            apply_c<float, NC, NR>(g, a.c32, p32, dof, y);
+#pragma unroll
+            for (int u = 0; u < U; ++u) {
+              const int64_t i = uidx<NC, NR>(n, dof, u);
+              q32[i] = y[u];
+              pqf[b_sys<NC, NR>(u)] = fmaf(p32[i], y[u], pqf[b_sys<NC, NR>(u)]);
+            }
+            if (pending) {
+              double yx[U], yd[U];
+              apply_c<double, NC, NR>(g, a.c64, x, dof, yx);
+              apply_c<double, NC, NR>(g, a.c64, d32, dof, yd);
+#pragma unroll
+              for (int u = 0; u < U; ++u) {
+                const int s = b_sys<NC, NR>(u);
+                if (!need[s]) continue;
+                const int64_t i = uidx<NC, NR>(n, dof, u);
+                const double t = b[i] - (yx[u] + yd[u]);
+                r32[i] = (float)t;
+                w[NS + s] = fma(t, t, w[NS + s]);
+              }
+            }
+          }
+#pragma unroll
+          for (int j = 0; j < NS; ++j) w[j] += (double)pqf[j];
+        })) {
+      status = CPM_BARRIER_TIMEOUT;
+      break;
+    }
+    double alpha[NS];
+    bool bad = false, still = false;
+#pragma unroll
+    for (int j = 0; j < NS; ++j) {
+      alpha[j] = 0.0;
+      if (!any) continue;
+      if (need[j]) {
+        resid[j] = sqrt(pt[NS + j]);
+        r0[j] = resid[j];
+        rho[j] = pt[NS + j];
+        if (!isfinite(resid[j])) bad = true;
+        if (resid[j] <= atol[j]) active[j] = 0;
+        else if (iters[j] >= maxiter) { active[j] = 0; unconv[j] = 1; }
+      }
+      if (active[j]) {
+        alpha[j] = rho[j] / pt[j];
+        if (!isfinite(alpha[j])) bad = true;
+      }
+      still |= active[j] != 0;
+    }
+    if (any && pending) ++updates;
+    if (bad) {
+      status = CPM_NONFINITE;
+      still = false;
+#pragma unroll
+      for (int j = 0; j < NS; ++j) active[j] = need[j] = 0;
+    }
+    const bool fold = any && !bad;
+    if (any && !still) {
+      if (lead) atomicSub(a.live, 1);
+      any = false;
+    }
+    // ---- pending: x += d, d = 0; active: d += alpha p, r32 -= alpha q, r32.r32
+    double rr[NS];
+    float af[NS];
+#pragma unroll
+    for (int j = 0; j < NS; ++j) af[j] = (float)alpha[j];
+    if (!seg_reduce<NS>(a, S, l, fold, par, s_red, rr, [&](int d0, int d1, double (&w)[NS]) {
+          float rrf[NS];
+#pragma unroll
+          for (int j = 0; j < NS; ++j) rrf[j] = 0.0f;
+          for (int dof = d0 + threadIdx.x; dof < d1; dof += kCGThreads) {
+#pragma unroll
+            for (int u = 0; u < U; ++u) {
+              const int s = b_sys<NC, NR>(u);
+              const int64_t i = uidx<NC, NR>(n, dof, u);
+              float dd = d32[i];
+              if (need[s]) {
+                x[i] += (double)dd;
+                dd = 0.0f;
+              }
+              if (active[s]) {
+                dd = fmaf(af[s], p32[i], dd);
+                const float rn = fmaf(-af[s], q32[i], r32[i]);
+                r32[i] = rn;
+                rrf[s] = fmaf(rn, rn, rrf[s]);
+              }
+              if (need[s] || active[s]) d32[i] = dd;
+            }
+          }
+#pragma unroll
+          for (int j = 0; j < NS; ++j) w[j] = (double)rrf[j];
+        })) {
+      status = CPM_BARRIER_TIMEOUT;
+      break;
+    }
+#pragma unroll
+    for (int j = 0; j < NS; ++j) need[j] = 0;
+    if (!any) continue;
+    float beta[NS];
+#pragma unroll
+    for (int j = 0; j < NS; ++j) {
+      beta[j] = 0.0f;
+      if (!active[j]) continue;
+      if (!isfinite(rr[j])) bad = true;
+      iters[j] += 1;
+      const double rn = sqrt(rr[j]);
+      need[j] = (rn < delta * r0[j]) || (rn <= atol[j]) || (iters[j] >= maxiter);
+      beta[j] = (float)(rr[j] / rho[j]);
+      rho[j] = rr[j];
+    }
+    if (bad) {
+      status = CPM_NONFINITE;
+#pragma unroll
+      for (int j = 0; j < NS; ++j) active[j] = need[j] = 0;
+      if (lead) atomicSub(a.live, 1);
+      any = false;
+      continue;
+    }
+    // ---- p = r32 + beta p
+    for (int cc = l; cc < S.nchunks; cc += S.ncta) {
+      const int d1 = min(g.n, (cc + 1) * S.chunk_dofs);
+      for (int dof = cc * S.chunk_dofs + threadIdx.x; dof < d1; dof += kCGThreads)
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+          const int s = b_sys<NC, NR>(u);
+          if (!active[s]) continue;
+          const int64_t i = uidx<NC, NR>(n, dof, u);
+          p32[i] = fmaf(beta[s], p32[i], r32[i]);
+        }
+    }
+  }
+  if (lead) {
+    int st = status;
+#pragma unroll
+    for (int j = 0; j < NS; ++j)
+      if (st == CPM_OK && (unconv[j] || active[j])) st = CPM_NOT_CONVERGED;
+    write_info(S.info, st, iters, resid, NS, updates, a.bar);
+  }
+}
+
+// ---------------------------------------------------------------- host side
+static int chunk_dofs_for(int ncomp, int nrhs) { return ncomp == 3 ? 1024 : (nrhs == 3 ? 2048 : 4096); }
+
+static const void *batched_kernel(int ncomp, int nrhs, int precision) {
+  if (precision == 0) {
+    if (ncomp == 3) return (const void *)cg_batched_fp64_kernel<3, 1>;
+    return nrhs == 3 ? (const void *)cg_batched_fp64_kernel<1, 3> : (const void *)cg_batched_fp64_kernel<1, 1>;
+  }
+  if (ncomp == 3) return (const void *)cg_batched_ir_kernel<3, 1>;
+  return nrhs == 3 ? (const void *)cg_batched_ir_kernel<1, 3> : (const void *)cg_batched_ir_kernel<1, 1>;
+}
+
+static size_t vec_bytes(int64_t n, int ncomp, int nrhs, int precision) {
+  return align256((size_t)n * ncomp * nrhs * (precision ? 4 : 8));
+}
+
+struct PlanLayout {
+  size_t bar, part, segs, ctamap, total;
+};
+
+static PlanLayout plan_layout(int64_t total_chunks, int nsys, int grid) {
+  PlanLayout L;
+  L.bar = 0;                       // GridBarrier (16 bytes) then the live counter at +16
+  L.part = 256;
+  L.segs = L.part + align256(sizeof(double) * 2 * (size_t)total_chunks * kSlot);
+  L.ctamap = L.segs + align256(sizeof(BSeg) * (size_t)nsys);
+  L.total = L.ctamap + align256(sizeof(int) * (size_t)grid);
+  return L;
+}
+
+struct Assignment {
+  std::vector<int> nchunks, ncta;
+  int64_t total_chunks = 0;
+  int grid = 0;
+};
+
+static int assign(const cpm_batch_system *sys, int nsys, int ncomp, int nrhs, int precision, Assignment &A,
+                  const char *who) {
+  if (!sys || nsys < 1 || (ncomp != 1 && ncomp != 3) || (nrhs != 1 && nrhs != 3) || (ncomp == 3 && nrhs != 1) ||
+      precision < 0 || precision > 1) {
+    set_error("%s: bad batch (nsys >= 1, ncomp 1 or 3, nrhs 1 or 3 with ncomp 1, precision 0 or 1)", who);
+    return CPM_BAD_ARG;
+  }
+  const int cd = chunk_dofs_for(ncomp, nrhs);
+  A.nchunks.assign(nsys, 0);
+  A.total_chunks = 0;
+  for (int s = 0; s < nsys; ++s) {
+    const cpm_batch_system &y = sys[s];
+    const int64_t n = (int64_t)y.nx * y.ny * y.nz;
+    if (y.nx < 3 || y.ny < 3 || y.nz < 3 || n * ncomp * nrhs >= ((int64_t)1 << 31) || !y.b || !y.x || !y.info ||
+        !y.work || y.maxiter < 1 || !(y.tol >= 0.0)) {
+      set_error("%s: bad system %d (at least 3 cells per axis, fewer than 2^31 unknowns, b, x, info and work "
+                "set, maxiter >= 1, tol >= 0)", who, s);
+      return CPM_BAD_ARG;
+    }
+    A.nchunks[s] = (int)((n + cd - 1) / cd);
+    A.total_chunks += A.nchunks[s];
+  }
+  int occ = 0;
+  CPM_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, batched_kernel(ncomp, nrhs, precision), kCGThreads,
+                                                        0));
+  if (occ < 1) {
+    set_error("%s: kernel cannot be resident on an SM", who);
+    return CPM_CUDA_ERROR;
+  }
+  int64_t gmax = (int64_t)occ * sm_count();
+  if (gmax > kMaxGrid) gmax = kMaxGrid;
+  if (nsys > gmax) {
+    set_error("%s: %d systems exceed the %lld CTAs that can be resident; split the batch", who, nsys,
+              (long long)gmax);
+    return CPM_BAD_ARG;
+  }
+  // equal chunks per CTA: the smallest load whose CTA count fits
+  int64_t load = std::max<int64_t>(1, (A.total_chunks + gmax - 1) / gmax);
+  for (;; ++load) {
+    int64_t g = 0;
+    for (int s = 0; s < nsys; ++s) g += (A.nchunks[s] + load - 1) / load;
+    if (g <= gmax) break;
+  }
+  A.ncta.assign(nsys, 0);
+  A.grid = 0;
+  for (int s = 0; s < nsys; ++s) {
+    A.ncta[s] = (int)((A.nchunks[s] + load - 1) / load);
+    A.grid += A.ncta[s];
+  }
+  return CPM_OK;
+}
+
+}  // namespace cpm
+
+extern "C" int64_t cpm_batch_work_bytes(int64_t n, int32_t ncomp, int32_t nrhs, int32_t precision) {
+  using namespace cpm;
+  return (int64_t)((precision ? 4 : 3) * vec_bytes(n, ncomp, nrhs, precision));
+}
+
+extern "C" int cpm_batch_plan_bytes(const cpm_batch_system *sys, int32_t nsys, int32_t ncomp, int32_t nrhs,
+                                    int32_t precision, int64_t *bytes) {
+  using namespace cpm;
+  Assignment A;
+  if (int e = assign(sys, nsys, ncomp, nrhs, precision, A, "cpm_batch_plan_bytes")) return e;
+  if (!bytes) {
+    set_error("cpm_batch_plan_bytes: bytes is NULL");
+    return CPM_BAD_ARG;
+  }
+  *bytes = (int64_t)plan_layout(A.total_chunks, nsys, A.grid).total;
+  return CPM_OK;
+}
+
+extern "C" int cpm_batch_plan_build(const cpm_batch_system *sys, int32_t nsys, int32_t ncomp, int32_t nrhs,
+                                    int32_t precision, const double *coef, void *plan_dev, int64_t plan_bytes,
+                                    cpm_batch_plan *plan, void *stream) {
+  using namespace cpm;
+  Assignment A;
+  if (int e = assign(sys, nsys, ncomp, nrhs, precision, A, "cpm_batch_plan_build")) return e;
+  const PlanLayout L = plan_layout(A.total_chunks, nsys, A.grid);
+  if (!coef || !plan || !plan_dev || plan_bytes < (int64_t)L.total || ((uintptr_t)plan_dev & 255)) {
+    set_error("cpm_batch_plan_build: bad arguments (coef, plan and a 256-byte aligned device buffer of at least "
+              "%zu bytes)", L.total);
+    return CPM_BAD_ARG;
+  }
+  const int cd = chunk_dofs_for(ncomp, nrhs);
+  std::vector<BSeg> segs(nsys);
+  std::vector<int> cmap(A.grid);
+  int chunk0 = 0, cta0 = 0;
+  for (int s = 0; s < nsys; ++s) {
+    const cpm_batch_system &y = sys[s];
+    BSeg &S = segs[s];
+    S = BSeg{};
+    S.nx = y.nx;
+    S.ny = y.ny;
+    S.nz = y.nz;
+    S.n = y.nx * y.ny * y.nz;
+    S.flags = y.flags;
+    S.b = y.b;
+    S.x = y.x;
+    S.use_init_dev = y.use_init_dev;
+    S.info = y.info;
+    S.tol = y.tol;
+    S.maxiter = y.maxiter;
+    S.chunk0 = chunk0;
+    S.nchunks = A.nchunks[s];
+    S.cta0 = cta0;
+    S.ncta = A.ncta[s];
+    S.chunk_dofs = cd;
+    const size_t vb = vec_bytes(S.n, ncomp, nrhs, precision);
+    char *w = (char *)y.work;
+    if (precision == 0) {
+      S.r = (double *)w;
+      S.p = (double *)(w + vb);
+      S.q = (double *)(w + 2 * vb);
+    } else {
+      S.r32 = (float *)w;
+      S.p32 = (float *)(w + vb);
+      S.q32 = (float *)(w + 2 * vb);
+      S.d32 = (float *)(w + 3 * vb);
+    }
+    for (int t = 0; t < S.ncta; ++t) cmap[cta0 + t] = s;
+    chunk0 += S.nchunks;
+    cta0 += S.ncta;
+  }
+  cudaStream_t st = (cudaStream_t)stream;
+  char *base = (char *)plan_dev;
+  CPM_TRY(cudaMemcpyAsync(base + L.segs, segs.data(), sizeof(BSeg) * nsys, cudaMemcpyHostToDevice, st));
+  CPM_TRY(cudaMemcpyAsync(base + L.ctamap, cmap.data(), sizeof(int) * A.grid, cudaMemcpyHostToDevice, st));
+  CPM_TRY(cudaStreamSynchronize(st));  // the staging vectors go out of scope
+  plan->dev = plan_dev;
+  plan->bytes = (int64_t)L.total;
+  plan->nsys = nsys;
+  plan->grid = A.grid;
+  plan->ncomp = ncomp;
+  plan->nrhs = nrhs;
+  plan->precision = precision;
+  plan->total_chunks = (int32_t)A.total_chunks;
+  const int nc = 27 * ncomp * ncomp;
+  for (int i = 0; i < 243; ++i) plan->coef[i] = i < nc ? coef[i] : 0.0;
+  return CPM_OK;
+}
+
+extern "C" int cpm_cg_solve_blockdiag(const cpm_batch_plan *plan, const cpm_cg_opts *opts, void *stream) {
+  using namespace cpm;
+  if (!plan || !plan->dev || plan->nsys < 1 || plan->grid < 1 || !opts) {
+    set_error("cpm_cg_solve_blockdiag: bad arguments (a built plan and options)");
+    return CPM_BAD_ARG;
+  }
+  const PlanLayout L = plan_layout(plan->total_chunks, plan->nsys, plan->grid);
+  char *base = (char *)plan->dev;
+  BatchArgs a{};
+  for (int i = 0; i < 243; ++i) {
+    a.c64[i] = plan->coef[i];
+    a.c32[i] = (float)plan->coef[i];
+  }
+  a.segs = (const BSeg *)(base + L.segs);
+  a.cta_seg = (const int *)(base + L.ctamap);
+  a.part = (double *)(base + L.part);
+  a.half = (long long)plan->total_chunks * kSlot;
+  a.bar = (GridBarrier *)(base + L.bar);
+  a.live = (int *)(base + L.bar + sizeof(GridBarrier));
+  const double tmo = opts->barrier_timeout_s > 0 ? opts->barrier_timeout_s : 2.0;
+  a.timeout_ns = (unsigned long long)(tmo * 1e9);
+  a.inner_tol = opts->inner_tol > 0 ? opts->inner_tol : 0.1;
+  cudaStream_t st = (cudaStream_t)stream;
+  CPM_TRY(cudaMemsetAsync(base + L.bar, 0, 32, st));
+  void *args[] = {&a};
+  CPM_TRY(cudaLaunchCooperativeKernel(batched_kernel(plan->ncomp, plan->nrhs, plan->precision), dim3(plan->grid),
+                                      dim3(kCGThreads), args, 0, st));
+  return CPM_OK;
+}

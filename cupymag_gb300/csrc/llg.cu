@@ -124,6 +124,8 @@ struct FieldP {
   double K1, C1, C2, C3, lam;
   double Nd[3], Hext[3], R[9];
   int rot, hasE;
+  const double *hsched;  // device field schedule (steps x 3) or NULL
+  const int *hstep;      // device index into hsched
 };
 
 __global__ void __launch_bounds__(kEwThreads) field_kernel(FieldP P, int64_t n, const double *__restrict__ mm,
@@ -135,6 +137,13 @@ __global__ void __launch_bounds__(kEwThreads) field_kernel(FieldP P, int64_t n, 
   const double hb1 = 0.5 * (-P.Nd[1] * avg_m[1]);
   const double hb2 = 0.5 * (-P.Nd[2] * avg_m[2]);
   const double k2 = -2.0 * P.K1, c1 = 2.0 * P.C1, c2 = 2.0 * P.C2, c3 = P.C3;
+  double H0 = P.Hext[0], H1 = P.Hext[1], H2 = P.Hext[2];
+  if (P.hsched) {
+    const int64_t s = *P.hstep;
+    H0 = P.hsched[3 * s];
+    H1 = P.hsched[3 * s + 1];
+    H2 = P.hsched[3 * s + 2];
+  }
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
     const double x0 = mm[3 * i], x1 = mm[3 * i + 1], x2 = mm[3 * i + 2];
     double e0 = 0, e1 = 0, e2 = 0, e3 = 0, e4 = 0, e5 = 0;
@@ -151,9 +160,9 @@ __global__ void __launch_bounds__(kEwThreads) field_kernel(FieldP P, int64_t n, 
     if (!P.rot) {
       const double s0 = x0 * x0, s1 = x1 * x1, s2 = x2 * x2;
       const double o0 = s1 + s2, o1 = s2 + s0, o2 = s0 + s1;
-      f0 = (((k2 * x0) * o0 + hb0) + h0) + P.Hext[0];
-      f1 = (((k2 * x1) * o1 + hb1) + h1) + P.Hext[1];
-      f2 = (((k2 * x2) * o2 + hb2) + h2) + P.Hext[2];
+      f0 = (((k2 * x0) * o0 + hb0) + h0) + H0;
+      f1 = (((k2 * x1) * o1 + hb1) + h1) + H1;
+      f2 = (((k2 * x2) * o2 + hb2) + h2) + H2;
       if (P.hasE) {
         f0 = ((f0 - (c1 * x0) * o0) - (c2 * (e0 - P.lam)) * x0) - c3 * (e3 * x1 + e5 * x2);
         f1 = ((f1 - (c1 * x1) * o1) - (c2 * (e1 - P.lam)) * x1) - c3 * (e4 * x2 + e3 * x0);
@@ -177,9 +186,9 @@ __global__ void __launch_bounds__(kEwThreads) field_kernel(FieldP P, int64_t n, 
       const double w0 = (v0 * R[0] + v1 * R[1]) + v2 * R[2];
       const double w1 = (v0 * R[3] + v1 * R[4]) + v2 * R[5];
       const double w2 = (v0 * R[6] + v1 * R[7]) + v2 * R[8];
-      f0 = ((w0 + hb0) + h0) + P.Hext[0];
-      f1 = ((w1 + hb1) + h1) + P.Hext[1];
-      f2 = ((w2 + hb2) + h2) + P.Hext[2];
+      f0 = ((w0 + hb0) + h0) + H0;
+      f1 = ((w1 + hb1) + h1) + H1;
+      f2 = ((w2 + hb2) + h2) + H2;
     }
     if (fout) {
       fout[3 * i] = f0;
@@ -457,8 +466,36 @@ extern "C" int cpm_llg_field(const cpm_field_params *P, int64_t n, const double 
   for (int k = 0; k < 9; ++k) q.R[k] = P->R[k];
   q.rot = P->rot111;
   q.hasE = P->has_E;
+  q.hsched = P->hext_sched;
+  q.hstep = P->hext_step;
+  if (q.hsched && !q.hstep) {
+    set_error("cpm_llg_field: hext_sched without hext_step");
+    return CPM_BAD_ARG;
+  }
   field_kernel<<<ew_grid(n), kEwThreads, 0, (cudaStream_t)stream>>>(q, n, mm, E, Ht, avg_m, dt, f, t);
   return check_launch("cpm_llg_field");
+}
+
+// ------------------------------------------------------------ per-step record
+__global__ void record_step_kernel(const double *avg_m, const double *sumsq, double *hist, int *step, int cap) {
+  const int s = *step;
+  if (s < cap) {
+    hist[4 * s] = avg_m[0];
+    hist[4 * s + 1] = avg_m[1];
+    hist[4 * s + 2] = avg_m[2];
+    hist[4 * s + 3] = *sumsq;
+    *step = s + 1;
+  }
+}
+
+extern "C" int cpm_record_step(const double *avg_m, const double *sumsq, double *hist, int32_t *step_dev,
+                               int32_t capacity, void *stream) {
+  if (!avg_m || !sumsq || !hist || !step_dev || capacity < 1) {
+    set_error("cpm_record_step: bad arguments");
+    return CPM_BAD_ARG;
+  }
+  record_step_kernel<<<1, 1, 0, (cudaStream_t)stream>>>(avg_m, sumsq, hist, step_dev, capacity);
+  return check_launch("cpm_record_step");
 }
 
 extern "C" int cpm_gs_star(int stage, int64_t n, const double *m, const double *g, const double *g1s,

@@ -25,7 +25,9 @@ struct Nbr {
   int zk[3];
 };
 
-__device__ __forceinline__ Nbr neighbours(const StencilOp &S, int dof) {
+// Geo is any record with int nx, ny, nz, n and const uint8_t *flags.
+template <typename Geo>
+__device__ __forceinline__ Nbr neighbours(const Geo &S, int dof) {
   const unsigned nyz = (unsigned)S.ny * (unsigned)S.nz;
   const unsigned i = (unsigned)dof / nyz;
   const unsigned rem = (unsigned)dof - i * nyz;
@@ -53,8 +55,8 @@ __device__ __forceinline__ const float *coefs<float>(const StencilOp &S) { retur
 
 // y = A x at one DOF for a scalar operator (nc = 1), NR interleaved vectors.
 // CHECK selects the path that tests every neighbour's column flag.
-template <typename T, int NR, bool CHECK>
-__device__ __forceinline__ void scalar_rows(const StencilOp &S, const T *c, const T *__restrict__ x, int dof,
+template <typename T, int NR, bool CHECK, typename Geo, typename TX>
+__device__ __forceinline__ void scalar_rows(const Geo &S, const T *c, const TX *__restrict__ x, int dof,
                                             T (&y)[NR]) {
   const Nbr b = neighbours(S, dof);
 #pragma unroll
@@ -69,12 +71,12 @@ __device__ __forceinline__ void scalar_rows(const StencilOp &S, const T *c, cons
         if (CHECK && (S.flags[q] & kColExcluded)) continue;
         const T w = c[(ia * 3 + ib) * 3 + ic];
 #pragma unroll
-        for (int r = 0; r < NR; ++r) y[r] = fma(w, x[q * NR + r], y[r]);
+        for (int r = 0; r < NR; ++r) y[r] = fma(w, (T)x[q * NR + r], y[r]);
       }
 }
 
-template <typename T, bool CHECK>
-__device__ __forceinline__ void elastic_rows(const StencilOp &S, const T *c, const T *__restrict__ x, int dof,
+template <typename T, bool CHECK, typename Geo, typename TX>
+__device__ __forceinline__ void elastic_rows(const Geo &S, const T *c, const TX *__restrict__ x, int dof,
                                              T (&y)[3]) {
   const int n = S.n;
   const Nbr b = neighbours(S, dof);
@@ -88,7 +90,7 @@ __device__ __forceinline__ void elastic_rows(const StencilOp &S, const T *c, con
         const int q = b.xi[ia] + b.yj[ib] + b.zk[ic];
         if (CHECK && (S.flags[q] & kColExcluded)) continue;
         const int d = (ia * 3 + ib) * 3 + ic;
-        const T u0 = x[q], u1 = x[n + q], u2 = x[2 * n + q];
+        const T u0 = (T)x[q], u1 = (T)x[n + q], u2 = (T)x[2 * n + q];
 #pragma unroll
         for (int r = 0; r < 3; ++r) {
           T acc = y[r];
@@ -100,16 +102,17 @@ __device__ __forceinline__ void elastic_rows(const StencilOp &S, const T *c, con
       }
 }
 
-// y at one DOF (all NC*NR components) in T.  Rows flagged as unit / empty are
-// handled first; only rows next to an excluded column test neighbour flags.
-template <typename T, int NC, int NR>
-__device__ __forceinline__ void apply_c(const StencilOp &S, const T *c, const T *__restrict__ x, int dof,
+// y at one DOF (all NC*NR components) in T, for x stored as TX.  Rows
+// flagged as unit / empty are handled first; only rows next to an excluded
+// column test neighbour flags.
+template <typename T, int NC, int NR, typename Geo, typename TX>
+__device__ __forceinline__ void apply_c(const Geo &S, const T *c, const TX *__restrict__ x, int dof,
                                         T (&y)[NC * NR]) {
   const uint8_t f = S.flags ? S.flags[dof] : 0;
   if (f & (kRowIdentity | kRowZero)) {
 #pragma unroll
     for (int u = 0; u < NC * NR; ++u)
-      y[u] = (f & kRowIdentity) ? x[NC == 1 ? dof * NR + u : u * S.n + dof] : T(0);
+      y[u] = (f & kRowIdentity) ? (T)x[NC == 1 ? dof * NR + u : u * S.n + dof] : T(0);
     return;
   }
   if (NC == 1) {

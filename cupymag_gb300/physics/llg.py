@@ -46,27 +46,34 @@ SOLVE_NAMES = ["elasticity", "demag", "Gauss-Seidel g1n/g2n/g3n", "Gauss-Seidel 
 class LLGSolver:
     """Device-resident state and operators of one LLG run."""
 
-    def __init__(self, sim_ops, params, precision="DP", device=None, ops=None, operators="csr"):
+    def __init__(self, sim_ops, params, precision="DP", device=None, ops=None, operators="csr", info=None):
         self.p = params
         self.precision = "DP" if precision == "DP" else "IR"
         self.dev = device or sim_ops.device
         dev = self.dev
         self.n = n = sim_ops.n_dof
-        if ops is None:
+        self.operators = operators
+        if operators == "stencil":
+            # matrix-free forms of the solved operators and of F1 (structured hex
+            # grids); only the derivative matrices and F_el stay CSR
+            so = sim_ops.stencil_operators()
+            A_demag, A1, A2, F1 = so["A_demag"], so["A1"], so["A2"], so["F1"]
+            A_el = so.get("A_el")
+            if ops is None:
+                Fx, Fy, Fz, Deriv = sim_ops.derivative_operators()
+                F_el = sim_ops.elastic_rhs_operator()
+                Avg = sim_ops.volume_average()
+            else:
+                _, Fx, Fy, Fz, Deriv, _, _, _, _, F_el, Avg = ops
+            if F_el is None and params.ME:
+                raise ValueError("magnetoelastic run without F_el")
+        elif ops is None:
             A_demag, Fx, Fy, Fz, Deriv = sim_ops.csr_demag_and_deriv()
             A1, A2, F1 = sim_ops.csr_GS()
             A_el, F_el = sim_ops.csr_elasticity()
             Avg = sim_ops.volume_average()
         else:
             A_demag, Fx, Fy, Fz, Deriv, A1, A2, F1, A_el, F_el, Avg = ops
-        self.operators = operators
-        if operators == "stencil":
-            # matrix-free forms of the solved operators and of F1 (structured hex grids)
-            so = sim_ops.stencil_operators()
-            A_demag, A1, A2, F1 = so["A_demag"], so["A1"], so["A2"], so["F1"]
-            A_el = so.get("A_el")
-            if Fx is not None and F_el is None and params.ME:
-                raise ValueError("magnetoelastic run without F_el")
         self.A_demag, self.Fx, self.Fy, self.Fz, self.Deriv = A_demag, Fx, Fy, Fz, Deriv
         self.A1, self.A2, self.F1, self.A_el, self.F_el, self.Avg = A1, A2, F1, A_el, F_el, Avg
         if self.precision == "IR":
@@ -89,7 +96,12 @@ class LLGSolver:
             self.u, self.E, self.E0, self.b_el = z(3 * n), z(n, 6), z(6 * n), z(3 * n)
         else:
             self.u = self.E = self.E0 = self.b_el = None
-        self.info = new_info(len(SOLVE_NAMES), dev)
+        if info is None:
+            info = new_info(len(SOLVE_NAMES), dev)
+        elif tuple(info.shape) != (len(SOLVE_NAMES), N.CG_INFO_BYTES):
+            raise ValueError(f"info must be a ({len(SOLVE_NAMES)}, {N.CG_INFO_BYTES}) uint8 device tensor")
+        self.info = info
+        self.hsched = self.hstep = self.hist = None
         mask = np.zeros(n, dtype=np.uint8)
         mask[np.asarray(sim_ops.DefDOF, dtype=np.int64)] = 1
         self.defect = torch.as_tensor(mask, device=dev)
@@ -107,6 +119,8 @@ class LLGSolver:
     # ------------------------------------------------------------------ state
     def set_magnetization(self, m0):
         m0 = torch.as_tensor(m0, dtype=torch.float64).reshape(self.n, 3)
+        if self.hstep is not None:
+            self.hstep.zero_()
         self.m.copy_(m0, non_blocking=True)
         self.m_prev.copy_(self.m)
         self.Avg.average_into(self.m, self.avg_m)
@@ -114,16 +128,31 @@ class LLGSolver:
         self.sumsq.fill_(math.inf)
         self.nstep = 0
 
+    def set_field_schedule(self, fields):
+        """Drive the applied field from a device schedule (steps, 3), normalised by Ms.
+
+        Step s then uses fields[s] read on the device from a step counter that
+        the end of each step advances, so a step captured once in a CUDA graph
+        follows the sweep when replayed; the Hext argument of step() is then
+        ignored.  Each step also records (<m>, sumsq) into ``hist`` (steps, 4)."""
+        f = torch.as_tensor(np.asarray(fields, dtype=np.float64).reshape(-1, 3), device=self.dev)
+        self.hsched = f.contiguous()
+        self.hstep = torch.zeros(1, dtype=torch.int32, device=self.dev)
+        self.hist = torch.zeros((f.shape[0], 4), dtype=torch.float64, device=self.dev)
+
     # ------------------------------------------------------------------ building blocks
     def _field_params(self, Hext):
         P = N.FieldParams()
         C1, C2, C3 = self.p.step_elasC
         P.K1, P.elasC1, P.elasC2, P.elasC3, P.lambda100 = self.p.K1, C1, C2, C3, self.p.lambda100
         P.Nd[:] = (self.p.N_x, self.p.N_y, self.p.N_z)
-        P.Hext[:] = tuple(float(h) for h in Hext)
+        P.Hext[:] = (0.0, 0.0, 0.0) if Hext is None else tuple(float(h) for h in Hext)
         P.R[:] = tuple(self.R9)
         P.rot111 = 1 if self.rot else 0
         P.has_E = 1 if self.ME else 0
+        if self.hsched is not None:
+            P.hext_sched = self.hsched.data_ptr()
+            P.hext_step = self.hstep.data_ptr()
         return P
 
     def _cg(self, A, b, x, k):
@@ -217,6 +246,10 @@ class LLGSolver:
                                    self.m_prev.data_ptr(), w.data_ptr(), V, self.thresh, self.sumsq.data_ptr(),
                                    self.avg_m.data_ptr(), self.use_init.data_ptr(), self.scratch.data_ptr(), s),
                 "cpm_renorm_sumsq")
+        if self.hsched is not None:
+            self.launches += 1
+            N.check(L.cpm_record_step(self.avg_m.data_ptr(), self.sumsq.data_ptr(), self.hist.data_ptr(),
+                                      self.hstep.data_ptr(), self.hist.shape[0], s), "cpm_record_step")
 
     def step(self, Hext):
         """One GSPM step at applied field Hext (normalised by Ms); asynchronous."""
@@ -252,15 +285,20 @@ class LLGSolver:
         its += inf[5]["iters"][:3]
         return its
 
-    def check(self):
-        """Synchronise and raise the reference's RuntimeError if a solve failed."""
-        inf = self.solve_infos()
+    def solve_slots(self):
+        """(k, A, b, x) of every solve a step requests, in order (slot k = SOLVE_NAMES[k])."""
         pairs = [(0, self.A_el, self.b_el, self.u), (1, self.A_demag, self.bdemag, self.U),
                  (2, self.A1, self.b3, self.g), (3, self.A1, self.b1, self.g1s), (4, self.A1, self.b1, self.g2s),
                  (5, self.A2, self.b3, self.mss)]
-        for k, A, b, x in pairs:
-            if k == 0 and not self.ME:
-                continue
+        return [t for t in pairs if self.ME or t[0] != 0]
+
+    def check(self):
+        """Synchronise and raise the reference's RuntimeError if a solve failed."""
+        return self.check_infos(self.solve_infos())
+
+    def check_infos(self, inf):
+        """Raise the reference's RuntimeError for the first failed solve in decoded infos."""
+        for k, A, b, x in self.solve_slots():
             nrhs = 3 if k in (2, 5) else 1
             raise_for(inf[k], A, b, x, system=SOLVE_NAMES[k], nrhs=nrhs)
         return inf

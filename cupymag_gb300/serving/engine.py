@@ -1,0 +1,319 @@
+"""Continuous-batching serving loop for LLG runs on one GPU.
+
+Requests (independent LLG runs: a hex mesh, a field sweep, a seeded initial
+magnetisation) arrive over time.  The engine admits a waiting request as soon
+as a slot is free and its estimated device memory fits the HBM budget, keeps
+every admitted run's state (m, u, fields, warm-start flag, CG vectors)
+resident on the device, and advances all admitted runs together, one
+Gauss-Seidel-projection step (cupymag/core/Micromagnetics.py:110-307) at a
+time:
+
+* each run's element-wise kernels run on its own data; each of the step's
+  solve slots (elasticity, demag, A1 x3, g1*, g2*, A2 x3) is ONE block-diagonal
+  CG launch over all runs that have that solve (one launch per coefficient
+  table);
+* the step is captured in a CUDA graph once per batch composition: the first
+  step after a change runs eagerly, the following ones replay the graph; the
+  applied field follows each run's sweep through a device step counter;
+* after each step one device-to-host copy returns every run's solver status;
+  a run that finished its sweep is retired (slot and memory released, its
+  final m and <m> history copied out) and waiting requests are admitted.
+
+A run's result does not depend on which other runs share its batch: the
+block-diagonal solver reduces each system in a fixed order of its own, and
+every other kernel of a run reads and writes only that run's data.
+"""
+from __future__ import annotations
+
+import time
+from collections import deque
+from dataclasses import dataclass, field
+
+import numpy as np
+import torch
+
+from .. import _native as N
+from ..core.assemble_simulation_operators import SimulationOperators
+from ..physics.llg import SOLVE_NAMES, LLGSolver
+from ..solvers.linear_solvers import decode_info
+from ..workloads import seeded_m0
+from .blockdiag import BlockDiagPlan, BlockSystem, coef_key, work_bytes
+
+NSLOTS = len(SOLVE_NAMES)
+
+
+def estimate_bytes(p, precision="IR") -> int:
+    """Device bytes one run holds (stencil operators, FP64 state, CSR derivative matrices).
+
+    Per DOF: 33 FP64 vectors of the step (51 with magnetoelastic coupling),
+    the volume-average weights, five flag arrays and the defect mask, the
+    three derivative matrices (27 non-zeros per row, shared indices), the
+    elastic right-hand-side matrix (3 rows x 162 non-zeros) with coupling, and
+    the block-diagonal CG vectors of the largest solve (3n unknowns)."""
+    n = int(p.Nx) * int(p.Ny) * int(p.Nz)
+    per = (51 if p.ME else 33) * 8 + 8 + 6 + (4 + 27 * 4 + 3 * 27 * 8)
+    if p.ME:
+        per += 3 * 4 + 3 * 162 * 12
+    per += 3 * (16 if precision != "DP" else 24)
+    return int(per * n * 1.05) + (8 << 20)
+
+
+@dataclass
+class Run:
+    req: object
+    solver: LLGSolver
+    slot: int
+    work: torch.Tensor
+    est_bytes: int
+    t_admit: float
+    steps_done: int = 0
+    error: str = None
+
+
+@dataclass
+class Result:
+    rid: int
+    arrival: float
+    admitted: float
+    completed: float
+    steps: int
+    hist: np.ndarray            # (steps, 4): <m> and sumsq after each step
+    m: np.ndarray = None        # final magnetisation (n, 3)
+    error: str = None
+    setup_s: float = 0.0
+
+    @property
+    def latency(self):
+        return self.completed - self.arrival
+
+
+@dataclass
+class ServeStats:
+    makespan_s: float = 0.0
+    steps: int = 0
+    requests: int = 0
+    failed: int = 0
+    latency_p50_s: float = 0.0
+    latency_p99_s: float = 0.0
+    graph_steps: int = 0
+    eager_steps: int = 0
+    captures: int = 0
+    batch_steps: int = 0
+    mean_batch: float = 0.0
+    max_batch: int = 0
+    peak_budget_gb: float = 0.0
+    graph_error: str = None
+    blockdiag_launches: int = 0
+    extra: dict = field(default_factory=dict)
+
+    @property
+    def steps_per_s(self):
+        return self.steps / self.makespan_s if self.makespan_s > 0 else 0.0
+
+
+class ServingEngine:
+    def __init__(self, precision="IR", hbm_budget_gb=150.0, max_runs=64, use_graphs=True, device=None,
+                 keep_m=False):
+        N.require_cuda()
+        self.dev = torch.device(device) if device is not None else torch.device("cuda", torch.cuda.current_device())
+        self.precision = "DP" if precision == "DP" else "IR"
+        self.budget = float(hbm_budget_gb) * 1e9
+        self.max_runs = int(max_runs)
+        self.use_graphs = bool(use_graphs)
+        self.keep_m = keep_m
+        self.infos = torch.zeros((self.max_runs, NSLOTS, N.CG_INFO_BYTES), dtype=torch.uint8, device=self.dev)
+        self.free = list(range(self.max_runs))[::-1]
+        self.active = []
+        self.used = 0
+        self.plans = None
+        self.graph = None
+        self.eager_since_change = 0
+        self.stats = ServeStats()
+
+    # ------------------------------------------------------------------ admission
+    def fits(self, req) -> bool:
+        return bool(self.free) and self.used + estimate_bytes(req.params(), self.precision) <= self.budget
+
+    def admit(self, req, now):
+        p = req.params()
+        est = estimate_bytes(p, self.precision)
+        S = SimulationOperators(p, device=self.dev)
+        slot = self.free.pop()
+        self.infos[slot].zero_()
+        L = LLGSolver(S, p, precision=self.precision, operators="stencil", info=self.infos[slot])
+        L.set_field_schedule(req.fields(p))
+        L.set_magnetization(torch.as_tensor(seeded_m0(S.n_dof, S.DefDOF, req.seed)))
+        work = torch.empty(work_bytes(S.n_dof, 3, 1, self.precision), dtype=torch.uint8, device=self.dev)
+        run = Run(req, L, slot, work, est, now)
+        self.active.append(run)
+        self.used += est
+        self.stats.peak_budget_gb = max(self.stats.peak_budget_gb, self.used / 1e9)
+        self._changed()
+        return run
+
+    def _changed(self):
+        self.plans = None
+        self.graph = None
+        self.eager_since_change = 0
+
+    # ------------------------------------------------------------------ one batched step
+    def _build_plans(self):
+        groups = {}
+        for run in self.active:
+            L = run.solver
+            for k, A, b, x in L.solve_slots():
+                key = (k, A.ncomp, 1 if b.dim() == 1 else int(b.shape[1]), coef_key(A))
+                groups.setdefault(key, []).append(
+                    BlockSystem(A, b, x, L.info[k], run.work, L.p.tol, L.p.maxiter, L.use_init))
+        plans = {k: [] for k in range(NSLOTS)}
+        for key, systems in groups.items():
+            plans[key[0]].append(BlockDiagPlan(systems, self.precision, device=self.dev))
+        self.plans = plans
+
+    def _step_all(self):
+        """Launch one step of every active run: element-wise kernels per run, one CG launch per slot."""
+        gens = [r.solver.step_gen(None) for r in self.active]
+        cur = [next(g, None) for g in gens]
+        for k in range(NSLOTS):
+            idx = [i for i, q in enumerate(cur) if q is not None and q.k == k]
+            if not idx:
+                continue
+            for plan in self.plans[k]:
+                plan.launch()
+                self.stats.blockdiag_launches += 1
+            for i in idx:
+                cur[i] = next(gens[i], None)
+        if any(q is not None for q in cur):
+            raise RuntimeError("a run requested a solve outside the step's slot order")
+
+    def step(self):
+        """Advance every active run by one step (asynchronous)."""
+        if self.plans is None:
+            self._build_plans()
+        if self.graph is None and self.use_graphs and self.eager_since_change >= 1:
+            try:
+                g = torch.cuda.CUDAGraph()
+                with torch.cuda.graph(g):
+                    self._step_all()
+                self.graph = g
+                self.stats.captures += 1
+            except Exception as e:  # capture unsupported: keep stepping eagerly
+                self.use_graphs = False
+                self.stats.graph_error = f"{type(e).__name__}: {e}"
+                torch.cuda.synchronize(self.dev)
+        if self.graph is not None:
+            self.graph.replay()
+            self.stats.graph_steps += 1
+        else:
+            self._step_all()
+            self.stats.eager_steps += 1
+            self.eager_since_change += 1
+        b = len(self.active)
+        self.stats.batch_steps += 1
+        self.stats.mean_batch += b
+        self.stats.max_batch = max(self.stats.max_batch, b)
+        for r in self.active:
+            r.steps_done += 1
+
+    # ------------------------------------------------------------------ completion
+    def _poll(self, now, results):
+        """Read every run's solver status (one copy) and retire finished or failed runs."""
+        raw = self.infos.cpu().numpy()
+        retired = False
+        for run in list(self.active):
+            err = None
+            for k, *_ in run.solver.solve_slots():
+                d = decode_info(raw[run.slot, k])
+                if d["status"] != N.CPM_OK:
+                    err = (f"step {run.steps_done}: CG for {SOLVE_NAMES[k]} ended with "
+                           f"{N.STATUS_NAMES.get(d['status'], d['status'])} (iterations {d['iters']})")
+                    break
+            if err is None and run.steps_done < run.req.steps:
+                continue
+            L = run.solver
+            results[run.req.rid] = Result(run.req.rid, run.req.arrival, run.t_admit, now, run.steps_done,
+                                          L.hist[:run.steps_done].cpu().numpy(),
+                                          L.m.cpu().numpy() if self.keep_m else None, err)
+            self.active.remove(run)
+            self.free.append(run.slot)
+            self.used -= run.est_bytes
+            retired = True
+        if retired:
+            self._changed()
+
+    def serve(self, requests, realtime=True):
+        """Serve the requests (arrival offsets in seconds when realtime); returns ({rid: Result}, ServeStats)."""
+        pending = deque(sorted(requests, key=lambda r: r.arrival))
+        results = {}
+        for r in list(pending):
+            if estimate_bytes(r.params(), self.precision) > self.budget:
+                pending.remove(r)
+                results[r.rid] = Result(r.rid, r.arrival, 0.0, 0.0, 0, np.zeros((0, 4)),
+                                        error="request exceeds the HBM budget")
+        torch.cuda.synchronize(self.dev)
+        t0 = time.perf_counter()
+        clock = lambda: time.perf_counter() - t0  # noqa: E731
+        while pending or self.active:
+            now = clock()
+            while pending and (not realtime or pending[0].arrival <= now) and self.fits(pending[0]):
+                self.admit(pending.popleft(), now)
+            if not self.active:
+                if pending:
+                    time.sleep(max(0.0, min(pending[0].arrival - clock(), 0.05)))
+                continue
+            self.step()
+            # requests that arrived meanwhile are set up while the step runs
+            now = clock()
+            while pending and (not realtime or pending[0].arrival <= now) and self.fits(pending[0]):
+                self.admit(pending.popleft(), now)
+            torch.cuda.synchronize(self.dev)
+            self._poll(clock(), results)
+        st = self.stats
+        done = [r for r in results.values() if r.completed > 0]
+        first = min((r.arrival for r in done), default=0.0)
+        st.makespan_s = max((r.completed for r in done), default=0.0) - first
+        st.steps = sum(r.steps for r in done if r.error is None)
+        st.requests = len(results)
+        st.failed = sum(1 for r in results.values() if r.error)
+        lat = np.array([r.latency for r in done if r.error is None])
+        if lat.size:
+            st.latency_p50_s = float(np.percentile(lat, 50))
+            st.latency_p99_s = float(np.percentile(lat, 99))
+        if st.batch_steps:
+            st.mean_batch /= st.batch_steps
+        return results, st
+
+
+def run_sequential(requests, precision="DP", operators="stencil", device=None, keep_m=False, max_steps=None):
+    """Each request alone, one after another, with a host check after every step (the unbatched baseline).
+
+    Returns ({rid: Result}, total seconds); times include each run's setup
+    (Result.setup_s).  max_steps stops every run early (a timing sample)."""
+    N.require_cuda()
+    dev = torch.device(device) if device is not None else torch.device("cuda", torch.cuda.current_device())
+    results = {}
+    torch.cuda.synchronize(dev)
+    t0 = time.perf_counter()
+    for req in requests:
+        ts = time.perf_counter() - t0
+        p = req.params()
+        S = SimulationOperators(p, device=dev)
+        L = LLGSolver(S, p, precision=precision, operators=operators)
+        L.set_field_schedule(req.fields(p))
+        L.set_magnetization(torch.as_tensor(seeded_m0(S.n_dof, S.DefDOF, req.seed)))
+        torch.cuda.synchronize(dev)
+        t_setup = time.perf_counter() - t0 - ts
+        err = None
+        for _ in range(req.steps if max_steps is None else min(req.steps, max_steps)):
+            L.step(None)
+            try:
+                L.check()
+            except RuntimeError as e:
+                err = str(e)
+                break
+        torch.cuda.synchronize(dev)
+        te = time.perf_counter() - t0
+        done = int(L.hstep.item())
+        results[req.rid] = Result(req.rid, ts, ts, te, done, L.hist[:done].cpu().numpy(),
+                                  L.m.cpu().numpy() if keep_m else None, err, t_setup)
+    return results, time.perf_counter() - t0

@@ -18,6 +18,9 @@ from .. import _native as N
 from ..mesh import shapes
 
 
+_BLOCK = 1 << 18  # elements per block of the weight computation
+
+
 def dof_weights(coords, elements, gid, n, defect_flag=None):
     nen = elements.shape[1] - 1
     cdof = gid[elements[:, :nen]].astype(np.int64)
@@ -27,18 +30,25 @@ def dof_weights(coords, elements, gid, n, defect_flag=None):
     else:
         pts, w = shapes.tet_gauss_points()
         Nf, dNf = shapes.tet_N, shapes.tet_dN
-    cc = coords[cdof]
+    ng = len(pts)
+    # dN of every Gauss point side by side: J for all points is one GEMM per block
+    dN = np.concatenate([dNf(r, s, t)[:nen] for (r, s, t) in pts], axis=1)  # (nen, 3*ng), column 3g + j
+    Nt = np.stack([Nf(r, s, t) for (r, s, t) in pts])                        # (ng, nen)
     Ne = len(cdof)
-    contrib = np.zeros((Ne, nen))
-    vol_e = np.zeros(Ne)
-    for g, (r, s, t) in enumerate(pts):
-        J = np.einsum("enk,nj->ekj", cc, dNf(r, s, t)[:nen])
-        det = (J[:, 0, 0] * (J[:, 1, 1] * J[:, 2, 2] - J[:, 1, 2] * J[:, 2, 1])
-               - J[:, 0, 1] * (J[:, 1, 0] * J[:, 2, 2] - J[:, 1, 2] * J[:, 2, 0])
-               + J[:, 0, 2] * (J[:, 1, 0] * J[:, 2, 1] - J[:, 1, 1] * J[:, 2, 0]))
-        vw = np.abs(det) * w[g]
-        contrib += vw[:, None] * Nf(r, s, t)[None, :]
-        vol_e += vw
+    contrib = np.empty((Ne, nen))
+    vol_e = np.empty(Ne)
+    for e0 in range(0, Ne, _BLOCK):
+        cc = coords[cdof[e0:e0 + _BLOCK]]                                    # (B, nen, 3)
+        B = len(cc)
+        J = (cc.transpose(0, 2, 1).reshape(B * 3, nen) @ dN).reshape(B, 3, ng, 3)  # J[e, k, g, j]
+        a = lambda k, j: J[:, k, :, j]  # noqa: E731
+        # cofactor expansion along the first row, as volume_average.py:123-125
+        det = (a(0, 0) * (a(1, 1) * a(2, 2) - a(1, 2) * a(2, 1))
+               - a(0, 1) * (a(1, 0) * a(2, 2) - a(1, 2) * a(2, 0))
+               + a(0, 2) * (a(1, 0) * a(2, 1) - a(1, 1) * a(2, 0)))
+        vw = np.abs(det) * w[None, :]
+        contrib[e0:e0 + B] = vw @ Nt
+        vol_e[e0:e0 + B] = vw.sum(axis=1)
     if defect_flag is not None:
         keep = 1.0 - np.asarray(defect_flag, dtype=np.float64)
         contrib *= keep[:, None]

@@ -149,6 +149,56 @@ int cpm_stencil_apply(const cpm_stencil *S, const double *x, double *y, double a
 int cpm_cg_solve_stencil(const cpm_stencil *S, const double *b, double *x, int nrhs, const cpm_cg_opts *opts,
                          void *workspace, size_t workspace_bytes, cpm_cg_info *info_dev, void *stream);
 
+/* ---- block-diagonal CG over many stencil systems (the serving loop) ----
+ * Replaces, for a batch of independent runs, one solve_cg call per run
+ * (cupymag/solvers/linear_solvers.py:20-74, called from
+ * cupymag/core/Micromagnetics.py:123,170,223,229,235,290) with one launch.
+ * All systems of a batch have the same operator kind (ncomp, nrhs) and the
+ * same coefficient table; grids, flags, tolerances, maxiter and warm-start
+ * flags are per system.  Each system keeps cupyx cg semantics and gets its
+ * own cpm_cg_info.  A system's result does not depend on the other systems
+ * of the batch (bit-for-bit). */
+typedef struct {
+  int32_t nx, ny, nz;      /* cells per axis (>= 3) */
+  int32_t maxiter;         /* >= 1 */
+  double tol;              /* stop when ||r|| <= tol * ||b|| */
+  const uint8_t *flags;    /* per-DOF flags as in cpm_stencil, or NULL */
+  const double *b;         /* device right-hand side(s) */
+  double *x;               /* device solution (initial guess when *use_init_dev != 0) */
+  const int32_t *use_init_dev; /* device warm-start flag, or NULL (cold start) */
+  cpm_cg_info *info;       /* device result record of this system */
+  void *work;              /* device work vectors, cpm_batch_work_bytes() bytes, 256-byte aligned */
+} cpm_batch_system;
+
+/* Launch plan built by cpm_batch_plan_build (host struct; `dev` is device memory). */
+typedef struct {
+  void *dev;
+  int64_t bytes;
+  int32_t nsys, grid, ncomp, nrhs, precision, total_chunks;
+  double coef[243];
+} cpm_batch_plan;
+
+/* Work-vector bytes of one system of n DOFs. */
+int64_t cpm_batch_work_bytes(int64_t n, int32_t ncomp, int32_t nrhs, int32_t precision);
+
+/* Device bytes of the plan for these systems (CTA assignment, partial sums, tables). */
+int cpm_batch_plan_bytes(const cpm_batch_system *sys, int32_t nsys, int32_t ncomp, int32_t nrhs,
+                         int32_t precision, int64_t *bytes);
+
+/* Build the plan into plan_dev (256-byte aligned, plan_bytes from
+ * cpm_batch_plan_bytes): copies the system table to the device and waits for
+ * the copy on `stream`, so it is called outside stream capture, once per
+ * batch composition.  coef: host, 27*ncomp*ncomp FP64 coefficients. */
+int cpm_batch_plan_build(const cpm_batch_system *sys, int32_t nsys, int32_t ncomp, int32_t nrhs,
+                         int32_t precision, const double *coef, void *plan_dev, int64_t plan_bytes,
+                         cpm_batch_plan *plan, void *stream);
+
+/* Solve every system of the plan in one cooperative launch on `stream`
+ * (a memset and a kernel: the call can be captured in a CUDA graph).  opts:
+ * inner_tol and barrier_timeout_s are used; tolerances, maxiter and
+ * warm-start flags come from the systems. */
+int cpm_cg_solve_blockdiag(const cpm_batch_plan *plan, const cpm_cg_opts *opts, void *stream);
+
 /* ---- LLG step kernels (cupymag/core/Micromagnetics.py:110-307) ---- */
 typedef struct {
   double K1, elasC1, elasC2, elasC3, lambda100;
@@ -157,6 +207,8 @@ typedef struct {
   double R[9];             /* [100] -> [111] rotation, row-major; used when rot111 */
   int32_t rot111;
   int32_t has_E;           /* 0: strain is identically zero (ME off) */
+  const double *hext_sched;/* device (steps, 3) field schedule, or NULL to use Hext */
+  const int32_t *hext_step;/* device index of the current step into hext_sched */
 } cpm_field_params;
 
 /* Effective field of Micromagnetics.py:175-215 (rot111 variant :190-211) at
@@ -166,6 +218,14 @@ typedef struct {
  * f (n,3) when f != NULL and t = f * dt + mm (n,3). */
 int cpm_llg_field(const cpm_field_params *P, int64_t n, const double *mm, const double *E, const double *Ht,
                   const double *avg_m, double dt, double *f, double *t, void *stream);
+
+/* End-of-step record for runs driven by a device step counter (a captured
+ * step replayed along a field sweep): hist[4*s + 0..2] = avg_m,
+ * hist[4*s + 3] = sumsq, then *step_dev = s + 1, for s = *step_dev < capacity.
+ * The reference appends the same values to its hysteresis output
+ * (Micromagnetics.py:303-317). */
+int cpm_record_step(const double *avg_m, const double *sumsq, double *hist, int32_t *step_dev, int32_t capacity,
+                    void *stream);
 
 /* Gauss-Seidel star updates (Micromagnetics.py:225-237).  g (n,3) holds
  * (g1n, g2n, g3n), f (n,3) the field from cpm_llg_field, mstar (n,3) the star

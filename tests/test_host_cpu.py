@@ -186,3 +186,43 @@ def test_library_exports_every_header_symbol():
     assert set(names) <= set(N.EXPORTED) | {"cpm_device_sm_count"}
     assert lib.cpm_version().startswith(b"cupymag_gb300")
     assert lib.cpm_cg_workspace_bytes(1000, 3, 1) > lib.cpm_cg_workspace_bytes(10, 1, 1)
+
+
+# ------------------------------------------------------------------ serving (host side)
+def test_serving_workload_shape():
+    from cupymag_gb300.serving.workload import serving_requests
+    reqs = serving_requests()
+    assert len(reqs) == 256
+    edges = np.array([r.edge for r in reqs])
+    assert edges.min() >= 16 and edges.max() <= 96
+    assert all(0 <= r.defect <= r.edge // 4 for r in reqs)
+    assert sum(r.ME for r in reqs) == 128
+    arr = np.array([r.arrival for r in reqs])
+    assert np.all(np.diff(arr) >= 0) and arr[0] == 0.0
+    assert 15.0 < (len(arr) - 1) / arr[-1] < 25.0
+    assert all(0.05 <= r.B0 <= 0.2 and r.steps == 100 for r in reqs)
+    # log-uniform edges: about half below the geometric mean of 16 and 96
+    assert 0.35 < np.mean(edges < np.sqrt(16 * 96)) < 0.65
+    assert serving_requests()[17] == reqs[17]
+
+
+def test_serving_field_schedule():
+    from cupymag_gb300.core.constants import MU0
+    from cupymag_gb300.serving.workload import Request
+    r = Request(0, 16, 2, False, 0.1, 5, 1)
+    p = r.params()
+    f = r.fields(p)
+    assert f.shape == (5, 3)
+    np.testing.assert_allclose(f[0, 0] * p.ms * MU0, 0.1)
+    np.testing.assert_allclose(f[-1, 0] * p.ms * MU0, -0.1)
+    assert np.all(f[:, 1:] == 0)
+
+
+def test_memory_estimate_grows_with_size_and_coupling():
+    from cupymag_gb300.serving.engine import estimate_bytes
+    from cupymag_gb300.workloads import hex_params
+    a = estimate_bytes(hex_params(32, 4, False, False))
+    b = estimate_bytes(hex_params(32, 4, True, True))
+    c = estimate_bytes(hex_params(64, 4, True, True))
+    assert a < b < c
+    assert 5e9 < estimate_bytes(hex_params(96, 12, True, True)) < 8e9
