@@ -1,0 +1,115 @@
+"""Time the CG solver on one operator of a structured hex grid.
+
+    python -m cupymag_gb300.cgbench [--edge 128] [--op A_el|A_demag|A1|A2] [--nrhs 1|3]
+                                    [--precision IR|DP] [--operators stencil|csr]
+                                    [--solves 3] [--maxiter 20000] [--batch 1]
+
+Builds only the requested operator (the magnetoelastic 128^3 material), a
+seeded right-hand side with the reference's pins (b[0] = 0 for A_demag,
+b[0] = b[n] = b[2n] = 0 for A_el), and times cold-start solves with CUDA
+events on the launching stream.  Prints one JSON line: iterations, reliable
+updates, ms per solve, ms per iteration and the algorithmic GB/s of the
+launch (vector traffic only for stencil operators, matrix + vectors for CSR).
+With --batch B > 1 the solve is B copies of the system in one block-diagonal
+launch.  A capped --maxiter keeps a profiled launch short; the status is then
+reported, not raised.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+
+import numpy as np
+import torch
+
+
+def _bytes(op, nrhs, iters, outer, fp32, csr):
+    u = op.shape[0] * nrhs
+    if not csr:
+        return u * (44 * iters + 48 * max(outer, 1)) if fp32 else u * (88 * iters + 24)
+    ip = op.indptr.element_size()
+    spmv = op.nnz * ((4 if fp32 else 8) + 4) + (op.shape[0] + 1) * ip + nrhs * (op.shape[1] + op.shape[0]) * (
+        4 if fp32 else 8)
+    return 2 * u * 8 + iters * (spmv + 6 * u * (4 if fp32 else 8))
+
+
+def main(argv=None):
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--edge", type=int, default=128)
+    ap.add_argument("--op", default="A_el", choices=["A_el", "A_demag", "A1", "A2"])
+    ap.add_argument("--nrhs", type=int, default=1, choices=[1, 3])
+    ap.add_argument("--precision", default="IR", choices=["IR", "DP"])
+    ap.add_argument("--operators", default="stencil", choices=["stencil", "csr"])
+    ap.add_argument("--solves", type=int, default=3)
+    ap.add_argument("--maxiter", type=int, default=20000)
+    ap.add_argument("--batch", type=int, default=1)
+    args = ap.parse_args(argv)
+
+    from . import _native as N
+    from .core.assemble_simulation_operators import SimulationOperators
+    from .solvers.linear_solvers import CGSolver, decode_info, new_info
+    from .workloads import hex_params
+    N.require_cuda()
+    N.load()
+    p = hex_params(args.edge, args.edge // 8, args.op == "A_el", True)
+    S = SimulationOperators(p)
+    csr = args.operators == "csr"
+    if csr:
+        op = {"A_el": lambda: S.csr_elasticity()[0], "A_demag": lambda: S.csr_demag_and_deriv()[0],
+              "A1": lambda: S.csr_GS()[0], "A2": lambda: S.csr_GS()[1]}[args.op]()
+    else:
+        op = S.stencil_operators()[args.op]
+    nrhs = 1 if args.op == "A_el" else args.nrhs
+    n = op.shape[0]
+    rng = np.random.default_rng(7)
+    b = rng.normal(size=(n, nrhs)) if nrhs == 3 else rng.normal(size=n)
+    if args.op == "A_demag":
+        b[0] = 0.0
+    if args.op == "A_el":
+        b[[0, n // 3, 2 * n // 3]] = 0.0
+    bd = torch.as_tensor(b, device="cuda").contiguous()
+    stream = torch.cuda.current_stream()
+    times, infos = [], []
+    if args.batch > 1:
+        if csr:
+            raise SystemExit("--batch needs stencil operators")
+        from .serving.blockdiag import BlockDiagPlan, BlockSystem, work_bytes
+        systems = []
+        for _ in range(args.batch):
+            systems.append(BlockSystem(op, bd, torch.zeros_like(bd), new_info(1)[0],
+                                       torch.empty(work_bytes(op.n, op.ncomp, nrhs, args.precision),
+                                                   dtype=torch.uint8, device="cuda"), p.tol, args.maxiter))
+        plan = BlockDiagPlan(systems, args.precision)
+        launch = plan.launch
+        info_of = lambda: systems[0].info  # noqa: E731
+    else:
+        solver = CGSolver()
+        x = torch.zeros_like(bd)
+        info = new_info(1)
+
+        def launch():
+            solver.launch(op, bd, x, info[0], tol=p.tol, maxiter=args.maxiter, precision=args.precision)
+        info_of = lambda: info[0]  # noqa: E731
+    for _ in range(args.solves):
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record(stream)
+        launch()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        times.append(e0.elapsed_time(e1))
+        infos.append(decode_info(info_of().cpu().numpy()))
+    d = infos[-1]
+    its = max(d["iters"][:nrhs])
+    ms = float(np.median(times))
+    nb = _bytes(op, nrhs, its, d["outer"], args.precision == "IR", csr) * args.batch
+    print(json.dumps({"op": args.op, "edge": args.edge, "n": n, "nrhs": nrhs, "precision": args.precision,
+                      "operators": args.operators, "batch": args.batch, "status": N.STATUS_NAMES[d["status"]],
+                      "iters": its, "outer": d["outer"], "ms_per_solve": round(ms, 3),
+                      "us_per_iter": round(1e3 * ms / max(its, 1), 2), "GB/s": round(nb / (ms / 1e3) / 1e9, 1),
+                      "solve_ms": [round(t, 3) for t in times]}))
+
+
+if __name__ == "__main__":
+    main()

@@ -20,10 +20,12 @@
 // FP32 CG with FP64 reliable updates in a form that needs no extra barrier:
 // when the FP32 recursive residual has fallen by inner_tol (or below the
 // stopping threshold, or at maxiter), the next iteration's first phase also
-// computes the true residual b - A64 (x + d) in FP64 beside q = A32 p; it
-// replaces the FP32 residual and rho, decides convergence, and the second
-// phase folds d into x.  The stopping test is only ever decided on the FP64
-// true residual.
+// computes the true residual t = b - A64 (x + d) in FP64 beside q = A32 p;
+// t replaces the FP32 residual and rho, decides convergence, and the second
+// phase folds d into x.  The direction p of that iteration was formed from
+// the recursive residual, so its step length is the exact line search
+// alpha = (t.p) / (p.A p) rather than (t.t) / (p.A p).  The stopping test is
+// only ever decided on the FP64 true residual.
 #include <algorithm>
 #include <cmath>
 #include <vector>
@@ -32,7 +34,7 @@
 
 namespace cpm {
 
-constexpr int kSlot = 8;  // doubles per chunk partial (>= 2 * 3 systems)
+constexpr int kSlot = 12;  // doubles per chunk partial (>= 3 values x 3 systems)
 
 // Grid geometry of one system in registers.
 struct Geo {
@@ -50,6 +52,7 @@ struct BSeg {
   double tol;
   int maxiter;
   int chunk0, nchunks, cta0, ncta, chunk_dofs;
+  int quads;                     // FP32 product on quads of 4 DOFs along z
   double *r, *p, *q;             // precision 0
   float *r32, *p32, *q32, *d32;  // precision 1
 };
@@ -131,10 +134,10 @@ __device__ __forceinline__ void write_info(cpm_cg_info *info, int status, const 
 
 // ---------------------------------------------------------------- FP64
 template <int NC, int NR>
-__global__ void __launch_bounds__(kCGThreads) cg_batched_fp64_kernel(const __grid_constant__ BatchArgs a) {
+__global__ void __launch_bounds__(kCGThreads, 2) cg_batched_fp64_kernel(const __grid_constant__ BatchArgs a) {
   constexpr int U = NC * NR;
   constexpr int NS = b_systems<NC, NR>();
-  __shared__ double s_red[2 * 3][kCGWarps];
+  __shared__ double s_red[9][kCGWarps];
   const BSeg &S = a.segs[a.cta_seg[blockIdx.x]];
   const int l = blockIdx.x - S.cta0;
   const bool lead = l == 0 && threadIdx.x == 0;
@@ -300,23 +303,31 @@ __global__ void __launch_bounds__(kCGThreads) cg_batched_fp64_kernel(const __gri
 }
 
 // ---------------------------------------------------------------- FP32 + FP64 reliable updates
+// The single-system FP32 solver of csrc/stencil.cu per segment (three grid
+// barriers per iteration, lagged reliable updates with the exact line search,
+// quads when nz % 4 == 0).  The CG state of the CTA's system lives in shared
+// memory (IRState, updated by thread 0 after each reduction with the
+// transitions of stencil_ops.cuh), so the DOF loops keep only alpha/beta and
+// two bitmasks in registers.
 template <int NC, int NR>
-__global__ void __launch_bounds__(kCGThreads) cg_batched_ir_kernel(const __grid_constant__ BatchArgs a) {
+__global__ void __launch_bounds__(kCGThreads, (NC == 1 && NR == 3) ? 3 : 4) cg_batched_ir_kernel(
+    const __grid_constant__ BatchArgs a) {
   constexpr int U = NC * NR;
   constexpr int NS = b_systems<NC, NR>();
-  __shared__ double s_red[2 * 3][kCGWarps];
+  __shared__ double s_red[9][kCGWarps];
+  __shared__ IRState st[NS];
+  __shared__ float s_ab[NS];
+  __shared__ int s_mask[3];  // active, need, status
   const BSeg &S = a.segs[a.cta_seg[blockIdx.x]];
   const int l = blockIdx.x - S.cta0;
-  const bool lead = l == 0 && threadIdx.x == 0;
+  const bool lead = l == 0;
   const Geo g{S.nx, S.ny, S.nz, S.n, S.flags};
   const int64_t n = g.n;
   const double *__restrict__ b = S.b;
   double *x = S.x;
   float *r32 = S.r32, *p32 = S.p32, *q32 = S.q32, *d32 = S.d32;
-  const double tol = S.tol;
-  const int maxiter = S.maxiter;
   const bool use_init = S.use_init_dev && __ldcg(S.use_init_dev) != 0;
-  const double delta = a.inner_tol;
+  const bool quads = S.quads != 0;  // chunks are multiples of 4 DOFs
   int par = 0;
 
   // ---- r = b - A64 x, r32 = p32 = r, d = 0; ||b||, ||r||
@@ -340,118 +351,123 @@ __global__ void __launch_bounds__(kCGThreads) cg_batched_ir_kernel(const __grid_
       }
     }
   });
-  double atol[NS], rho[NS], resid[NS], r0[NS];
-  int active[NS], need[NS], iters[NS], unconv[NS];
-  bool any = false;
+  if (threadIdx.x == 0) {
+    int am = 0;
+    for (int j = 0; j < NS; ++j) {
+      const double bn = ok ? sqrt(v[j]) : 0.0;
+      ir_init(st[j], bn, ok ? v[NS + j] : 0.0, S.tol);
+      am |= st[j].active << j;
+      if (lead) S.info->bnorm[j] = bn;
+    }
+    if (lead) {
+      for (int j = NS; j < 3; ++j) S.info->bnorm[j] = 0.0;
+      if (am) atomicAdd(a.live, 1);
+    }
+    s_mask[0] = am;
+    s_mask[1] = 0;
+    s_mask[2] = CPM_OK;
+  }
+  __syncthreads();
+  int activem = s_mask[0], needm = 0;
   int status = ok ? CPM_OK : CPM_BARRIER_TIMEOUT;
-  int updates = 0;
-#pragma unroll
-  for (int j = 0; j < NS; ++j) {
-    const double bn = ok ? sqrt(v[j]) : 0.0;
-    atol[j] = tol * bn;
-    rho[j] = ok ? v[NS + j] : 0.0;
-    resid[j] = sqrt(rho[j]);
-    r0[j] = resid[j];
-    active[j] = bn != 0.0;
-    need[j] = 0;
-    iters[j] = 0;
-    unconv[j] = 0;
-    any |= active[j] != 0;
-  }
-  if (lead) {
-    for (int j = 0; j < 3; ++j) S.info->bnorm[j] = j < NS ? sqrt(ok ? v[j] : 0.0) : 0.0;
-    if (any) atomicAdd(a.live, 1);
-  }
   if (ok && use_init) {
     for (int cc = l; cc < S.nchunks; cc += S.ncta) {
       const int d1 = min(g.n, (cc + 1) * S.chunk_dofs);
       for (int dof = cc * S.chunk_dofs + threadIdx.x; dof < d1; dof += kCGThreads)
 #pragma unroll
         for (int u = 0; u < U; ++u)
-          if (!active[b_sys<NC, NR>(u)]) x[uidx<NC, NR>(n, dof, u)] = b[uidx<NC, NR>(n, dof, u)];
+          if (!((activem >> b_sys<NC, NR>(u)) & 1)) x[uidx<NC, NR>(n, dof, u)] = b[uidx<NC, NR>(n, dof, u)];
     }
   }
   for (int k = 0; ok; ++k) {
     if (k > 0) {
       if (!grid_sync(a.bar, gridDim.x, a.timeout_ns)) { status = CPM_BARRIER_TIMEOUT; break; }
+      // every change of the counter happened before this barrier and none
+      // happens before the next one: all CTAs read the same value
       if (__ldcg(a.live) == 0) break;
     }
-    bool pending = false;
-#pragma unroll
-    for (int j = 0; j < NS; ++j) pending |= need[j] != 0;
-    // ---- q = A32 p, p.q (FP32 per thread); pending updates: t = b - A64 (x + d), r32 = t, t.t
-    double pt[2 * NS];
-    if (!seg_reduce<2 * NS>(a, S, l, any, par, s_red, pt, [&](int d0, int d1, double (&w)[2 * NS]) {
+    const bool busy = activem != 0;  // pending updates belong to active systems
+    // ---- q = A32 p, p.q (FP32 per thread); pending updates: t = b - A64 (x + d), r32 = t, t.t, t.p
+    double pt[3 * NS];
+    if (!seg_reduce<3 * NS>(a, S, l, busy, par, s_red, pt, [&](int d0, int d1, double (&w)[3 * NS]) {
           float pqf[NS];
 #pragma unroll
           for (int j = 0; j < NS; ++j) pqf[j] = 0.0f;
-          for (int dof = d0 + threadIdx.x; dof < d1; dof += kCGThreads) {
-            float y[U];
-            apply_c<float, NC, NR>(g, a.c32, p32, dof, y);
-#pragma unroll
-            for (int u = 0; u < U; ++u) {
-              const int64_t i = uidx<NC, NR>(n, dof, u);
-              q32[i] = y[u];
-              pqf[b_sys<NC, NR>(u)] = fmaf(p32[i], y[u], pqf[b_sys<NC, NR>(u)]);
+          if (quads) {
+            for (int qd = d0 + 4 * threadIdx.x; qd < d1; qd += 4 * kCGThreads) {
+              float y[4][U];
+              apply4_c<float, NC, NR>(g, a.c32, p32, qd, y);
+              quad_store<float, NC, NR>(q32, n, qd, y);
+              quad_dot<NC, NR>(p32, n, qd, y, pqf);
             }
-            if (pending) {
+          } else {
+            for (int dof = d0 + threadIdx.x; dof < d1; dof += kCGThreads) {
+              float y[U];
+              apply_c<float, NC, NR>(g, a.c32, p32, dof, y);
+#pragma unroll
+              for (int u = 0; u < U; ++u) {
+                const int64_t i = uidx<NC, NR>(n, dof, u);
+                q32[i] = y[u];
+                pqf[b_sys<NC, NR>(u)] = fmaf(p32[i], y[u], pqf[b_sys<NC, NR>(u)]);
+              }
+            }
+          }
+#pragma unroll
+          for (int j = 0; j < NS; ++j) w[j] += (double)pqf[j];
+          if (needm) {
+            for (int dof = d0 + threadIdx.x; dof < d1; dof += kCGThreads) {
               double yx[U], yd[U];
               apply_c<double, NC, NR>(g, a.c64, x, dof, yx);
               apply_c<double, NC, NR>(g, a.c64, d32, dof, yd);
 #pragma unroll
               for (int u = 0; u < U; ++u) {
                 const int s = b_sys<NC, NR>(u);
-                if (!need[s]) continue;
+                if (!((needm >> s) & 1)) continue;
                 const int64_t i = uidx<NC, NR>(n, dof, u);
                 const double t = b[i] - (yx[u] + yd[u]);
                 r32[i] = (float)t;
                 w[NS + s] = fma(t, t, w[NS + s]);
+                w[2 * NS + s] = fma(t, (double)p32[i], w[2 * NS + s]);
               }
             }
           }
-#pragma unroll
-          for (int j = 0; j < NS; ++j) w[j] += (double)pqf[j];
         })) {
       status = CPM_BARRIER_TIMEOUT;
       break;
     }
-    double alpha[NS];
-    bool bad = false, still = false;
-#pragma unroll
-    for (int j = 0; j < NS; ++j) {
-      alpha[j] = 0.0;
-      if (!any) continue;
-      if (need[j]) {
-        resid[j] = sqrt(pt[NS + j]);
-        r0[j] = resid[j];
-        rho[j] = pt[NS + j];
-        if (!isfinite(resid[j])) bad = true;
-        if (resid[j] <= atol[j]) active[j] = 0;
-        else if (iters[j] >= maxiter) { active[j] = 0; unconv[j] = 1; }
-      }
-      if (active[j]) {
-        alpha[j] = rho[j] / pt[j];
-        if (!isfinite(alpha[j])) bad = true;
-      }
-      still |= active[j] != 0;
-    }
-    if (any && pending) ++updates;
-    if (bad) {
-      status = CPM_NONFINITE;
-      still = false;
-#pragma unroll
-      for (int j = 0; j < NS; ++j) active[j] = need[j] = 0;
-    }
-    const bool fold = any && !bad;
-    if (any && !still) {
-      if (lead) atomicSub(a.live, 1);
-      any = false;
-    }
-    // ---- pending: x += d, d = 0; active: d += alpha p, r32 -= alpha q, r32.r32
-    double rr[NS];
     float af[NS];
 #pragma unroll
-    for (int j = 0; j < NS; ++j) af[j] = (float)alpha[j];
+    for (int j = 0; j < NS; ++j) af[j] = 0.0f;
+    if (busy) {
+      if (threadIdx.x == 0) {
+        int am = 0, bad = 0;
+        for (int j = 0; j < NS; ++j) {
+          double al;
+          bad |= ir_after_pq(st[j], pt[j], pt[NS + j], pt[2 * NS + j], S.maxiter, al) ? 1 : 0;
+          s_ab[j] = (float)al;
+          am |= st[j].active << j;
+        }
+        if (needm) st[0].updates += 1;
+        if (bad) {
+          for (int j = 0; j < NS; ++j) st[j].active = 0;
+          am = 0;
+        }
+        if (lead && am == 0) atomicSub(a.live, 1);
+        s_mask[0] = am;
+        s_mask[2] = bad ? CPM_NONFINITE : CPM_OK;
+      }
+      __syncthreads();
+      activem = s_mask[0];
+      if (s_mask[2] != CPM_OK) {
+        status = s_mask[2];
+        needm = 0;
+      }
+#pragma unroll
+      for (int j = 0; j < NS; ++j) af[j] = s_ab[j];
+    }
+    // ---- pending: x += d, d = 0; active: d += alpha p, r32 -= alpha q, r32.r32
+    const bool fold = (needm | activem) != 0;
+    double rr[NS];
     if (!seg_reduce<NS>(a, S, l, fold, par, s_red, rr, [&](int d0, int d1, double (&w)[NS]) {
           float rrf[NS];
 #pragma unroll
@@ -460,19 +476,21 @@ __global__ void __launch_bounds__(kCGThreads) cg_batched_ir_kernel(const __grid_
 #pragma unroll
             for (int u = 0; u < U; ++u) {
               const int s = b_sys<NC, NR>(u);
+              const bool nd = (needm >> s) & 1, ac = (activem >> s) & 1;
+              if (!nd && !ac) continue;
               const int64_t i = uidx<NC, NR>(n, dof, u);
               float dd = d32[i];
-              if (need[s]) {
+              if (nd) {
                 x[i] += (double)dd;
                 dd = 0.0f;
               }
-              if (active[s]) {
+              if (ac) {
                 dd = fmaf(af[s], p32[i], dd);
                 const float rn = fmaf(-af[s], q32[i], r32[i]);
                 r32[i] = rn;
                 rrf[s] = fmaf(rn, rn, rrf[s]);
               }
-              if (need[s] || active[s]) d32[i] = dd;
+              d32[i] = dd;
             }
           }
 #pragma unroll
@@ -481,29 +499,35 @@ __global__ void __launch_bounds__(kCGThreads) cg_batched_ir_kernel(const __grid_
       status = CPM_BARRIER_TIMEOUT;
       break;
     }
-#pragma unroll
-    for (int j = 0; j < NS; ++j) need[j] = 0;
-    if (!any) continue;
-    float beta[NS];
-#pragma unroll
-    for (int j = 0; j < NS; ++j) {
-      beta[j] = 0.0f;
-      if (!active[j]) continue;
-      if (!isfinite(rr[j])) bad = true;
-      iters[j] += 1;
-      const double rn = sqrt(rr[j]);
-      need[j] = (rn < delta * r0[j]) || (rn <= atol[j]) || (iters[j] >= maxiter);
-      beta[j] = (float)(rr[j] / rho[j]);
-      rho[j] = rr[j];
+    needm = 0;
+    if (!activem) continue;
+    if (threadIdx.x == 0) {
+      int nm = 0, bad = 0;
+      for (int j = 0; j < NS; ++j) {
+        float be;
+        bad |= ir_after_rr(st[j], rr[j], a.inner_tol, S.maxiter, be) ? 1 : 0;
+        s_ab[j] = be;
+        nm |= st[j].need << j;
+      }
+      if (bad) {
+        for (int j = 0; j < NS; ++j) st[j].active = st[j].need = 0;
+        nm = 0;
+        if (lead) atomicSub(a.live, 1);
+      }
+      s_mask[0] = bad ? 0 : activem;
+      s_mask[1] = nm;
+      s_mask[2] = bad ? CPM_NONFINITE : CPM_OK;
     }
-    if (bad) {
-      status = CPM_NONFINITE;
-#pragma unroll
-      for (int j = 0; j < NS; ++j) active[j] = need[j] = 0;
-      if (lead) atomicSub(a.live, 1);
-      any = false;
+    __syncthreads();
+    if (s_mask[2] != CPM_OK) {
+      status = s_mask[2];
+      activem = 0;
       continue;
     }
+    needm = s_mask[1];
+    float beta[NS];
+#pragma unroll
+    for (int j = 0; j < NS; ++j) beta[j] = s_ab[j];
     // ---- p = r32 + beta p
     for (int cc = l; cc < S.nchunks; cc += S.ncta) {
       const int d1 = min(g.n, (cc + 1) * S.chunk_dofs);
@@ -511,18 +535,23 @@ __global__ void __launch_bounds__(kCGThreads) cg_batched_ir_kernel(const __grid_
 #pragma unroll
         for (int u = 0; u < U; ++u) {
           const int s = b_sys<NC, NR>(u);
-          if (!active[s]) continue;
+          if (!((activem >> s) & 1)) continue;
           const int64_t i = uidx<NC, NR>(n, dof, u);
           p32[i] = fmaf(beta[s], p32[i], r32[i]);
         }
     }
   }
-  if (lead) {
-    int st = status;
-#pragma unroll
-    for (int j = 0; j < NS; ++j)
-      if (st == CPM_OK && (unconv[j] || active[j])) st = CPM_NOT_CONVERGED;
-    write_info(S.info, st, iters, resid, NS, updates, a.bar);
+  if (lead && threadIdx.x == 0) {
+    int sta = status;
+    if (*(volatile const int *)&a.bar->error && sta == CPM_OK) sta = CPM_BARRIER_TIMEOUT;
+    for (int j = 0; j < 3; ++j) {
+      if (j < NS && sta == CPM_OK && (st[j].unconv || st[j].active)) sta = CPM_NOT_CONVERGED;
+      S.info->iters[j] = j < NS ? st[j].iters : 0;
+      S.info->resid[j] = j < NS ? st[j].resid : 0.0;
+    }
+    S.info->outer = st[0].updates;
+    S.info->pad = 0;
+    S.info->status = sta;
   }
 }
 
@@ -576,9 +605,9 @@ static int assign(const cpm_batch_system *sys, int nsys, int ncomp, int nrhs, in
     const cpm_batch_system &y = sys[s];
     const int64_t n = (int64_t)y.nx * y.ny * y.nz;
     if (y.nx < 3 || y.ny < 3 || y.nz < 3 || n * ncomp * nrhs >= ((int64_t)1 << 31) || !y.b || !y.x || !y.info ||
-        !y.work || y.maxiter < 1 || !(y.tol >= 0.0)) {
-      set_error("%s: bad system %d (at least 3 cells per axis, fewer than 2^31 unknowns, b, x, info and work "
-                "set, maxiter >= 1, tol >= 0)", who, s);
+        !y.work || ((uintptr_t)y.work & 255) || y.maxiter < 1 || !(y.tol >= 0.0)) {
+      set_error("%s: bad system %d (at least 3 cells per axis, fewer than 2^31 unknowns, b, x, info and a "
+                "256-byte aligned work buffer set, maxiter >= 1, tol >= 0)", who, s);
       return CPM_BAD_ARG;
     }
     A.nchunks[s] = (int)((n + cd - 1) / cd);
@@ -670,6 +699,7 @@ extern "C" int cpm_batch_plan_build(const cpm_batch_system *sys, int32_t nsys, i
     S.cta0 = cta0;
     S.ncta = A.ncta[s];
     S.chunk_dofs = cd;
+    S.quads = (y.nz & 3) == 0 && ((uintptr_t)y.flags & 3) == 0;
     const size_t vb = vec_bytes(S.n, ncomp, nrhs, precision);
     char *w = (char *)y.work;
     if (precision == 0) {

@@ -8,7 +8,7 @@ namespace cpm {
 constexpr int kCGThreads = 256;
 constexpr int kCGWarps = kCGThreads / kWarp;
 constexpr int kMaxGrid = 4096;                 // CTAs of one cooperative launch (upper bound)
-constexpr size_t kPartHalf = (size_t)6 * kMaxGrid;  // doubles per half of the partials buffer
+constexpr size_t kPartHalf = (size_t)9 * kMaxGrid;  // doubles per half of the partials buffer (<= 9 sums per CTA)
 
 // Block-wide sum of NV values per thread, deterministic; result broadcast.
 template <int NV>
@@ -41,7 +41,9 @@ __device__ __forceinline__ bool grid_sum(double (&v)[NV], double *part, int &par
   const int G = gridDim.x;
   part += (size_t)parity * kPartHalf;
   parity ^= 1;
-  if (threadIdx.x < NV) part[(size_t)blockIdx.x * NV + threadIdx.x] = v[threadIdx.x];
+#pragma unroll
+  for (int j = 0; j < NV; ++j)
+    if (threadIdx.x == j) part[(size_t)blockIdx.x * NV + j] = v[j];
   if (!grid_sync(bar, G, tns)) return false;
   double acc[NV];
 #pragma unroll

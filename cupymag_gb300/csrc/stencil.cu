@@ -24,6 +24,7 @@
 // is the FP64 one, while the iterations run on FP32 vectors with FP32
 // coefficients and FP64 dot accumulation.  GB300 issues FP32 FMAs at many
 // times its FP64 rate, so the FP32 iterations are bound by vector traffic.
+#include <algorithm>
 #include <cmath>
 
 #include "stencil_ops.cuh"
@@ -47,6 +48,7 @@ struct StencilCG {
   cpm_cg_info *info;
   unsigned long long timeout_ns;
   int64_t dofs_per_cta;
+  int quads;  // nz % 4 == 0 and 4-byte aligned flags: the FP32 product runs on quads (apply4_c)
 };
 
 // Number of independent systems (each with its own CG scalars).
@@ -196,44 +198,56 @@ __global__ void __launch_bounds__(kCGThreads) cg_stencil_fp64_kernel(const __gri
 // ---------------------------------------------------------------- FP32 CG with FP64 reliable updates
 // Mixed-precision CG with reliable updates (Sleijpen & van der Vorst, 1996):
 // the iteration runs on FP32 vectors (p, q, the correction d and the
-// recursive residual r) with FP64 dot accumulation.  Whenever the recursive
-// residual has dropped by a factor delta (inner_tol) below the last true
-// residual -- or below the stopping threshold -- x += d in FP64 and the
-// residual is replaced by the true FP64 residual b - A x (FP64 coefficients,
-// FP64 x).  The search direction is kept across updates, so the Krylov
-// convergence of plain CG is retained (unlike restarted refinement), and the
-// stopping test ||b - A x|| <= tol ||b|| is only ever decided on the FP64
-// residual.  info->outer counts the reliable updates.
+// recursive residual r) with FP32 stencil coefficients and FP64 dot
+// accumulation across threads.  When the recursive residual has fallen by a
+// factor delta (inner_tol) below the last true residual -- or below the
+// stopping threshold, or at maxiter -- the next iteration's first phase also
+// computes the true residual t = b - A64 (x + d) with the FP64 coefficients
+// and the FP64 x: t replaces r and rho, decides convergence (the stopping
+// test ||b - A x|| <= tol ||b|| is only ever decided on t), and the second
+// phase folds d into x (FP64).  That iteration's direction p was formed from
+// the recursive residual, so its step length is the exact line search
+// alpha = (t.p) / (p.A p).  The update costs no extra grid barrier.
+// info->outer counts the reliable updates.  With nz % 4 == 0 the FP32
+// product runs on quads of 4 DOFs along z (apply4_c).  The CG state lives in
+// shared memory (IRState), updated by thread 0 after each reduction, so the
+// DOF loops keep only alpha/beta and bitmasks in registers.
 template <int NC, int NR>
-__global__ void __launch_bounds__(kCGThreads) cg_stencil_ir_kernel(const __grid_constant__ StencilCG a) {
+__global__ void __launch_bounds__(kCGThreads, 4) cg_stencil_ir_kernel(const __grid_constant__ StencilCG a) {
   constexpr int U = NC * NR;
   constexpr int NS = n_systems<NC, NR>();
-  __shared__ double s_red[2 * 3][kCGWarps];
+  __shared__ double s_red[9][kCGWarps];
+  __shared__ IRState st[NS];
+  __shared__ float s_ab[NS];
+  __shared__ int s_mask[3];  // active, need, error status
   const int64_t n = a.S.n;
   const int64_t d0 = min(n, (int64_t)blockIdx.x * a.dofs_per_cta);
   const int64_t d1 = min(n, d0 + a.dofs_per_cta);
+  const bool quads = a.quads != 0;
   const bool use_init = a.use_init_dev ? (__ldcg(a.use_init_dev) != 0) : (a.use_init_host != 0);
   const unsigned long long tns = a.timeout_ns;
-  const double delta = a.inner_tol;
+  const double *__restrict__ b = a.b;
+  double *x = a.x;
+  float *r32 = a.r32, *p32 = a.p32, *q32 = a.q32, *d32 = a.d32;
   int par = 0;
 
-  // ---- prologue: r = b - A x (FP64), r32 = p32 = r, d = 0; ||b||, ||r||
+  // ---- prologue: r = b - A64 x (FP64), r32 = p32 = r, d = 0; ||b||, ||r||
   double v[2 * NS];
 #pragma unroll
   for (int j = 0; j < 2 * NS; ++j) v[j] = 0.0;
   for (int64_t dof = d0 + threadIdx.x; dof < d1; dof += kCGThreads) {
     double y[U];
-    if (use_init) apply<double, NC, NR>(a.S, a.x, (int)dof, y);
+    if (use_init) apply<double, NC, NR>(a.S, x, (int)dof, y);
 #pragma unroll
     for (int u = 0; u < U; ++u) {
       const int64_t i = uidx<NC, NR>(n, dof, u);
-      const double bi = a.b[i];
+      const double bi = b[i];
       const double ri = use_init ? bi - y[u] : bi;
-      if (!use_init) a.x[i] = 0.0;
+      if (!use_init) x[i] = 0.0;
       const float rf = (float)ri;
-      a.r32[i] = rf;
-      a.p32[i] = rf;
-      a.d32[i] = 0.0f;
+      r32[i] = rf;
+      p32[i] = rf;
+      d32[i] = 0.0f;
       const int s = sys_of<NC, NR>(u);
       v[s] = fma(bi, bi, v[s]);
       v[NS + s] = fma(ri, ri, v[NS + s]);
@@ -243,175 +257,183 @@ __global__ void __launch_bounds__(kCGThreads) cg_stencil_ir_kernel(const __grid_
     set_status(a.info, CPM_BARRIER_TIMEOUT);
     return;
   }
-  double atol[NS], resid[NS], rho[NS], r0[NS];
-  int active[NS], iters[NS];
-  bool any = false;
-#pragma unroll
-  for (int j = 0; j < NS; ++j) {
-    const double bn = sqrt(v[j]);
-    atol[j] = a.tol * bn;
-    rho[j] = v[NS + j];
-    resid[j] = sqrt(v[NS + j]);
-    r0[j] = resid[j];
-    active[j] = bn != 0.0;
-    iters[j] = 0;
-    any |= active[j] != 0;
-    if (blockIdx.x == 0 && threadIdx.x == 0) a.info->bnorm[j] = bn;
+  if (threadIdx.x == 0) {
+    int am = 0;
+    for (int j = 0; j < NS; ++j) {
+      ir_init(st[j], sqrt(v[j]), v[NS + j], a.tol);
+      am |= st[j].active << j;
+      if (blockIdx.x == 0) a.info->bnorm[j] = sqrt(v[j]);
+    }
+    s_mask[0] = am;
+    s_mask[1] = 0;
+    s_mask[2] = CPM_OK;
   }
+  __syncthreads();
+  int activem = s_mask[0], needm = 0;
   if (use_init) {
     for (int64_t dof = d0 + threadIdx.x; dof < d1; dof += kCGThreads)
 #pragma unroll
       for (int u = 0; u < U; ++u)
-        if (!active[sys_of<NC, NR>(u)]) a.x[uidx<NC, NR>(n, dof, u)] = a.b[uidx<NC, NR>(n, dof, u)];
+        if (!((activem >> sys_of<NC, NR>(u)) & 1)) x[uidx<NC, NR>(n, dof, u)] = b[uidx<NC, NR>(n, dof, u)];
   }
   int status = CPM_OK;
-  int updates = 0;
-  for (int k = 0; any && k < a.maxiter; ++k) {
+  for (int k = 0; activem && k <= a.maxiter; ++k) {
     if (k > 0 && !grid_sync(a.bar, gridDim.x, tns)) { status = CPM_BARRIER_TIMEOUT; break; }
-    // ---- phase 1: q = A32 p, partial p.q
-    // per-thread partials in FP32 (a thread owns a few dozen DOFs), summed in FP64 across threads
+    // ---- phase 1: q = A32 p, p.q (FP32 per thread); pending: t = b - A64 (x + d), r32 = t, t.t, t.p
     float pqf[NS];
 #pragma unroll
     for (int j = 0; j < NS; ++j) pqf[j] = 0.0f;
-    for (int64_t dof = d0 + threadIdx.x; dof < d1; dof += kCGThreads) {
-      float y[U];
-      apply<float, NC, NR>(a.S, a.p32, (int)dof, y);
+    if (quads) {
+      for (int64_t qd = d0 + 4 * threadIdx.x; qd < d1; qd += 4 * kCGThreads) {
+        float y[4][U];
+        apply4_c<float, NC, NR>(a.S, a.S.c32, p32, (int)qd, y);
+        quad_store<float, NC, NR>(q32, n, qd, y);
+        quad_dot<NC, NR>(p32, n, qd, y, pqf);
+      }
+    } else {
+      for (int64_t dof = d0 + threadIdx.x; dof < d1; dof += kCGThreads) {
+        float y[U];
+        apply<float, NC, NR>(a.S, p32, (int)dof, y);
 #pragma unroll
-      for (int u = 0; u < U; ++u) {
-        const int64_t i = uidx<NC, NR>(n, dof, u);
-        a.q32[i] = y[u];
-        const int s = sys_of<NC, NR>(u);
-        pqf[s] = fmaf(a.p32[i], y[u], pqf[s]);
+        for (int u = 0; u < U; ++u) {
+          const int64_t i = uidx<NC, NR>(n, dof, u);
+          q32[i] = y[u];
+          pqf[sys_of<NC, NR>(u)] = fmaf(p32[i], y[u], pqf[sys_of<NC, NR>(u)]);
+        }
       }
     }
-    double pq[NS];
-#pragma unroll
-    for (int j = 0; j < NS; ++j) pq[j] = (double)pqf[j];
-    if (!grid_sum<NS>(pq, a.part, par, a.bar, tns, s_red)) { status = CPM_BARRIER_TIMEOUT; break; }
-    double alpha[NS];
-    bool bad = false;
+    double pt[3 * NS];
 #pragma unroll
     for (int j = 0; j < NS; ++j) {
-      alpha[j] = active[j] ? rho[j] / pq[j] : 0.0;
-      if (active[j] && !isfinite(alpha[j])) bad = true;
+      pt[j] = (double)pqf[j];
+      pt[NS + j] = 0.0;
+      pt[2 * NS + j] = 0.0;
     }
-    if (bad) { status = CPM_NONFINITE; break; }
-    // ---- phase 2: d += alpha p, r32 -= alpha q, partial r32.r32
-    float rrf[NS], af[NS];
+    if (needm) {
+      for (int64_t dof = d0 + threadIdx.x; dof < d1; dof += kCGThreads) {
+        double yx[U], yd[U];
+        apply<double, NC, NR>(a.S, x, (int)dof, yx);
+        apply_c<double, NC, NR>(a.S, a.S.c64, d32, (int)dof, yd);
 #pragma unroll
-    for (int j = 0; j < NS; ++j) {
-      rrf[j] = 0.0f;
-      af[j] = (float)alpha[j];
+        for (int u = 0; u < U; ++u) {
+          const int s = sys_of<NC, NR>(u);
+          if (!((needm >> s) & 1)) continue;
+          const int64_t i = uidx<NC, NR>(n, dof, u);
+          const double t = b[i] - (yx[u] + yd[u]);
+          r32[i] = (float)t;
+          pt[NS + s] = fma(t, t, pt[NS + s]);
+          pt[2 * NS + s] = fma(t, (double)p32[i], pt[2 * NS + s]);
+        }
+      }
     }
+    if (!grid_sum<3 * NS>(pt, a.part, par, a.bar, tns, s_red)) { status = CPM_BARRIER_TIMEOUT; break; }
+    if (threadIdx.x == 0) {
+      int am = 0, bad = 0;
+      for (int j = 0; j < NS; ++j) {
+        double al;
+        bad |= ir_after_pq(st[j], pt[j], pt[NS + j], pt[2 * NS + j], a.maxiter, al);
+        s_ab[j] = (float)al;
+        am |= st[j].active << j;
+      }
+      if (needm) st[0].updates += 1;
+      s_mask[0] = am;
+      s_mask[2] = bad ? CPM_NONFINITE : CPM_OK;
+    }
+    __syncthreads();
+    if (s_mask[2] != CPM_OK) { status = s_mask[2]; break; }
+    float af[NS];
+#pragma unroll
+    for (int j = 0; j < NS; ++j) af[j] = s_ab[j];
+    activem = s_mask[0];
+    // ---- phase 2: pending: x += d, d = 0; active: d += alpha p, r32 -= alpha q, r32.r32
+    float rrf[NS];
+#pragma unroll
+    for (int j = 0; j < NS; ++j) rrf[j] = 0.0f;
     for (int64_t dof = d0 + threadIdx.x; dof < d1; dof += kCGThreads) {
 #pragma unroll
       for (int u = 0; u < U; ++u) {
         const int s = sys_of<NC, NR>(u);
-        if (!active[s]) continue;
+        const bool nd = (needm >> s) & 1, ac = (activem >> s) & 1;
+        if (!nd && !ac) continue;
         const int64_t i = uidx<NC, NR>(n, dof, u);
-        a.d32[i] = fmaf(af[s], a.p32[i], a.d32[i]);
-        const float rn = fmaf(-af[s], a.q32[i], a.r32[i]);
-        a.r32[i] = rn;
-        rrf[s] = fmaf(rn, rn, rrf[s]);
+        float dd = d32[i];
+        if (nd) {
+          x[i] += (double)dd;
+          dd = 0.0f;
+        }
+        if (ac) {
+          dd = fmaf(af[s], p32[i], dd);
+          const float rn = fmaf(-af[s], q32[i], r32[i]);
+          r32[i] = rn;
+          rrf[s] = fmaf(rn, rn, rrf[s]);
+        }
+        d32[i] = dd;
       }
     }
     double rr[NS];
 #pragma unroll
     for (int j = 0; j < NS; ++j) rr[j] = (double)rrf[j];
     if (!grid_sum<NS>(rr, a.part, par, a.bar, tns, s_red)) { status = CPM_BARRIER_TIMEOUT; break; }
-    bool upd = false;
-    int need[NS];
-#pragma unroll
-    for (int j = 0; j < NS; ++j) {
-      need[j] = 0;
-      if (!active[j]) continue;
-      if (!isfinite(rr[j])) bad = true;
-      iters[j] += 1;
-      const double rn = sqrt(rr[j]);
-      need[j] = (rn < delta * r0[j]) || (rn <= atol[j]) || (k + 1 >= a.maxiter);
-      upd |= need[j] != 0;
-    }
-    if (bad) { status = CPM_NONFINITE; break; }
-    double rnew[NS];
-#pragma unroll
-    for (int j = 0; j < NS; ++j) rnew[j] = rr[j];
-    if (upd) {
-      // ---- reliable update: x += d (FP64), d = 0 (own DOFs), then r = b - A64 x
-      ++updates;
-      for (int64_t dof = d0 + threadIdx.x; dof < d1; dof += kCGThreads)
-#pragma unroll
-        for (int u = 0; u < U; ++u) {
-          const int s = sys_of<NC, NR>(u);
-          if (!need[s]) continue;
-          const int64_t i = uidx<NC, NR>(n, dof, u);
-          a.x[i] += (double)a.d32[i];
-          a.d32[i] = 0.0f;
-        }
-      if (!grid_sync(a.bar, gridDim.x, tns)) { status = CPM_BARRIER_TIMEOUT; break; }
-      double tr[NS];
-#pragma unroll
-      for (int j = 0; j < NS; ++j) tr[j] = 0.0;
-      for (int64_t dof = d0 + threadIdx.x; dof < d1; dof += kCGThreads) {
-        double y[U];
-        apply<double, NC, NR>(a.S, a.x, (int)dof, y);
-#pragma unroll
-        for (int u = 0; u < U; ++u) {
-          const int s = sys_of<NC, NR>(u);
-          if (!need[s]) continue;
-          const int64_t i = uidx<NC, NR>(n, dof, u);
-          const double ri = a.b[i] - y[u];
-          a.r32[i] = (float)ri;
-          tr[s] = fma(ri, ri, tr[s]);
-        }
-      }
-      if (!grid_sum<NS>(tr, a.part, par, a.bar, tns, s_red)) { status = CPM_BARRIER_TIMEOUT; break; }
-#pragma unroll
+    if (threadIdx.x == 0) {
+      int nm = 0, bad = 0;
       for (int j = 0; j < NS; ++j) {
-        if (!need[j]) continue;
-        resid[j] = sqrt(tr[j]);
-        r0[j] = resid[j];
-        rnew[j] = tr[j];
-        if (resid[j] <= atol[j]) active[j] = 0;
+        float be;
+        bad |= ir_after_rr(st[j], rr[j], a.inner_tol, a.maxiter, be);
+        s_ab[j] = be;
+        nm |= st[j].need << j;
       }
+      s_mask[1] = nm;
+      s_mask[2] = bad ? CPM_NONFINITE : CPM_OK;
     }
-    any = false;
+    __syncthreads();
+    if (s_mask[2] != CPM_OK) { status = s_mask[2]; break; }
+    needm = s_mask[1];
+    if (!activem) break;
     float beta[NS];
 #pragma unroll
-    for (int j = 0; j < NS; ++j) {
-      beta[j] = 0.0f;
-      if (!active[j]) continue;
-      beta[j] = (float)(rnew[j] / rho[j]);
-      rho[j] = rnew[j];
-      any = true;
-    }
-    if (!any || k + 1 >= a.maxiter) break;
+    for (int j = 0; j < NS; ++j) beta[j] = s_ab[j];
     // ---- phase 3: p = r32 + beta p
     for (int64_t dof = d0 + threadIdx.x; dof < d1; dof += kCGThreads) {
 #pragma unroll
       for (int u = 0; u < U; ++u) {
         const int s = sys_of<NC, NR>(u);
-        if (!active[s]) continue;
+        if (!((activem >> s) & 1)) continue;
         const int64_t i = uidx<NC, NR>(n, dof, u);
-        a.p32[i] = fmaf(beta[s], a.p32[i], a.r32[i]);
+        p32[i] = fmaf(beta[s], p32[i], r32[i]);
       }
     }
   }
   if (blockIdx.x == 0 && threadIdx.x == 0) {
-    int st = status;
-#pragma unroll
+    int stt = status;
     for (int j = 0; j < NS; ++j) {
-      if (st == CPM_OK && active[j]) st = CPM_NOT_CONVERGED;
-      a.info->iters[j] = iters[j];
-      a.info->resid[j] = resid[j];
+      if (stt == CPM_OK && (st[j].unconv || st[j].active)) stt = CPM_NOT_CONVERGED;
+      a.info->iters[j] = st[j].iters;
+      a.info->resid[j] = st[j].resid;
     }
-    a.info->outer = updates;
-    set_status(a.info, st);
+    a.info->outer = st[0].updates;
+    set_status(a.info, stt);
   } else if (status != CPM_OK && threadIdx.x == 0) {
     set_status(a.info, status);
   }
 }
 
 // ---------------------------------------------------------------- y = alpha A x (FP64)
+// Same product on quads of 4 DOFs along z (nz % 4 == 0, 16-byte aligned x and y).
+template <int NC, int NR>
+__global__ void __launch_bounds__(256) stencil_apply4_kernel(const __grid_constant__ StencilOp S, const double *x,
+                                                             double *y, double alpha) {
+  const int64_t nq = S.n / 4;
+  for (int64_t qd = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; qd < nq; qd += (int64_t)gridDim.x * blockDim.x) {
+    double t[4][NC * NR];
+    apply4_c<double, NC, NR>(S, S.c64, x, (int)(4 * qd), t);
+#pragma unroll
+    for (int kk = 0; kk < 4; ++kk)
+#pragma unroll
+      for (int u = 0; u < NC * NR; ++u) t[kk][u] = alpha * t[kk][u];
+    quad_store<double, NC, NR>(y, S.n, 4 * qd, t);
+  }
+}
+
 template <int NC, int NR>
 __global__ void __launch_bounds__(256) stencil_apply_kernel(const __grid_constant__ StencilOp S, const double *x, double *y, double alpha) {
   for (int64_t dof = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; dof < S.n;
@@ -436,6 +458,12 @@ static StencilOp to_op(const cpm_stencil *s) {
     S.c32[i] = (float)S.c64[i];
   }
   return S;
+}
+
+// The quad form needs whole quads in every z-line and 4-byte aligned flags
+// (the solver's own vectors are 256-byte aligned).
+static bool quads_ok(const cpm_stencil *s) {
+  return (s->nz & 3) == 0 && ((uintptr_t)s->flags & 3) == 0;
 }
 
 static int check_stencil(const cpm_stencil *s, const char *who) {
@@ -490,6 +518,7 @@ static int launch_stencil_cg(const cpm_stencil *s, const double *b, double *x, c
   per = (per + 31) / 32 * 32;
   G = (n + per - 1) / per;
   a.dofs_per_cta = per;
+  a.quads = quads_ok(s) ? 1 : 0;
   CPM_TRY(cudaMemsetAsync(w.bar, 0, sizeof(GridBarrier), st));
   CPM_TRY(cudaMemsetAsync(info, 0, sizeof(cpm_cg_info), st));
   void *args[] = {&a};
@@ -537,6 +566,16 @@ extern "C" int cpm_stencil_apply(const cpm_stencil *S, const double *x, double *
   const int64_t cap = (int64_t)sm_count() * 8;
   if (g > cap) g = cap;
   cudaStream_t st = (cudaStream_t)stream;
+  if (quads_ok(S) && (((uintptr_t)x | (uintptr_t)y) & 15) == 0) {
+    const int64_t gq = std::max<int64_t>(1, std::min<int64_t>(g, (op.n / 4 + 255) / 256));
+    if (S->ncomp == 3)
+      stencil_apply4_kernel<3, 1><<<(int)gq, 256, 0, st>>>(op, x, y, alpha);
+    else if (nvec == 1)
+      stencil_apply4_kernel<1, 1><<<(int)gq, 256, 0, st>>>(op, x, y, alpha);
+    else
+      stencil_apply4_kernel<1, 3><<<(int)gq, 256, 0, st>>>(op, x, y, alpha);
+    return check_launch("cpm_stencil_apply");
+  }
   if (S->ncomp == 3)
     stencil_apply_kernel<3, 1><<<(int)g, 256, 0, st>>>(op, x, y, alpha);
   else if (nvec == 1)

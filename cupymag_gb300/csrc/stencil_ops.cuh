@@ -53,10 +53,56 @@ __device__ __forceinline__ const double *coefs<double>(const StencilOp &S) { ret
 template <>
 __device__ __forceinline__ const float *coefs<float>(const StencilOp &S) { return S.c32; }
 
+template <typename T>
+struct Vec4;
+template <>
+struct Vec4<float> {
+  static __device__ __forceinline__ void load(const float *p, float *v) {
+    const float4 t = *reinterpret_cast<const float4 *>(p);
+    v[0] = t.x;
+    v[1] = t.y;
+    v[2] = t.z;
+    v[3] = t.w;
+  }
+  static __device__ __forceinline__ void store(float *p, const float *v) {
+    *reinterpret_cast<float4 *>(p) = make_float4(v[0], v[1], v[2], v[3]);
+  }
+};
+template <>
+struct Vec4<double> {
+  static __device__ __forceinline__ void load(const double *p, double *v) {
+    const double2 a = *reinterpret_cast<const double2 *>(p);
+    const double2 b = *reinterpret_cast<const double2 *>(p + 2);
+    v[0] = a.x;
+    v[1] = a.y;
+    v[2] = b.x;
+    v[3] = b.y;
+  }
+  static __device__ __forceinline__ void store(double *p, const double *v) {
+    *reinterpret_cast<double2 *>(p) = make_double2(v[0], v[1]);
+    *reinterpret_cast<double2 *>(p + 2) = make_double2(v[2], v[3]);
+  }
+};
+
+// ---------------------------------------------------------------- operand loaders
+// The products read their operand through ld / ld4: element i (component c:
+// the right-hand side of an interleaved scalar vector, or the displacement
+// component) of a vector of any storage type, converted to T.
+template <typename T, typename TX>
+__device__ __forceinline__ T ld(const TX *x, int64_t i, int) { return (T)x[i]; }
+
+template <typename T, typename TX>
+__device__ __forceinline__ void ld4(const TX *x, int64_t i, int, T *v) {
+  TX t[4];
+  Vec4<TX>::load(x + i, t);
+#pragma unroll
+  for (int e = 0; e < 4; ++e) v[e] = (T)t[e];
+}
+
 // y = A x at one DOF for a scalar operator (nc = 1), NR interleaved vectors.
 // CHECK selects the path that tests every neighbour's column flag.
-template <typename T, int NR, bool CHECK, typename Geo, typename TX>
-__device__ __forceinline__ void scalar_rows(const Geo &S, const T *c, const TX *__restrict__ x, int dof,
+template <typename T, int NR, bool CHECK, typename Geo, typename XS>
+__device__ __forceinline__ void scalar_rows(const Geo &S, const T *c, const XS &x, int dof,
                                             T (&y)[NR]) {
   const Nbr b = neighbours(S, dof);
 #pragma unroll
@@ -71,12 +117,12 @@ __device__ __forceinline__ void scalar_rows(const Geo &S, const T *c, const TX *
         if (CHECK && (S.flags[q] & kColExcluded)) continue;
         const T w = c[(ia * 3 + ib) * 3 + ic];
 #pragma unroll
-        for (int r = 0; r < NR; ++r) y[r] = fma(w, (T)x[q * NR + r], y[r]);
+        for (int r = 0; r < NR; ++r) y[r] = fma(w, ld<T>(x, (int64_t)q * NR + r, r), y[r]);
       }
 }
 
-template <typename T, bool CHECK, typename Geo, typename TX>
-__device__ __forceinline__ void elastic_rows(const Geo &S, const T *c, const TX *__restrict__ x, int dof,
+template <typename T, bool CHECK, typename Geo, typename XS>
+__device__ __forceinline__ void elastic_rows(const Geo &S, const T *c, const XS &x, int dof,
                                              T (&y)[3]) {
   const int n = S.n;
   const Nbr b = neighbours(S, dof);
@@ -90,7 +136,7 @@ __device__ __forceinline__ void elastic_rows(const Geo &S, const T *c, const TX 
         const int q = b.xi[ia] + b.yj[ib] + b.zk[ic];
         if (CHECK && (S.flags[q] & kColExcluded)) continue;
         const int d = (ia * 3 + ib) * 3 + ic;
-        const T u0 = (T)x[q], u1 = (T)x[n + q], u2 = (T)x[2 * n + q];
+        const T u0 = ld<T>(x, q, 0), u1 = ld<T>(x, (int64_t)n + q, 1), u2 = ld<T>(x, 2 * (int64_t)n + q, 2);
 #pragma unroll
         for (int r = 0; r < 3; ++r) {
           T acc = y[r];
@@ -105,14 +151,14 @@ __device__ __forceinline__ void elastic_rows(const Geo &S, const T *c, const TX 
 // y at one DOF (all NC*NR components) in T, for x stored as TX.  Rows
 // flagged as unit / empty are handled first; only rows next to an excluded
 // column test neighbour flags.
-template <typename T, int NC, int NR, typename Geo, typename TX>
-__device__ __forceinline__ void apply_c(const Geo &S, const T *c, const TX *__restrict__ x, int dof,
+template <typename T, int NC, int NR, typename Geo, typename XS>
+__device__ __forceinline__ void apply_c(const Geo &S, const T *c, const XS &x, int dof,
                                         T (&y)[NC * NR]) {
   const uint8_t f = S.flags ? S.flags[dof] : 0;
   if (f & (kRowIdentity | kRowZero)) {
 #pragma unroll
     for (int u = 0; u < NC * NR; ++u)
-      y[u] = (f & kRowIdentity) ? (T)x[NC == 1 ? dof * NR + u : u * S.n + dof] : T(0);
+      y[u] = (f & kRowIdentity) ? ld<T>(x, NC == 1 ? (int64_t)dof * NR + u : (int64_t)u * S.n + dof, u) : T(0);
     return;
   }
   if (NC == 1) {
@@ -128,6 +174,236 @@ __device__ __forceinline__ void apply_c(const Geo &S, const T *c, const TX *__re
 #pragma unroll
     for (int r = 0; r < 3; ++r) y[r] = t[r];
   }
+}
+
+// ---------------------------------------------------------------- four DOFs along z
+// Register-blocked application to the quad of DOFs d0..d0+3 (d0 % 4 == 0,
+// nz % 4 == 0, so the quad lies in one z-line at k0..k0+3).  Each of the 9
+// (x, y) neighbour columns is read once per component as an aligned vector
+// of 4 plus the two wrapped edge values k0-1 and k0+4, and serves all three
+// z offsets of all four DOFs: 6 loads where the per-DOF form makes 12.  The
+// FMAs run in the per-DOF order (neighbour d = (dx, dy, dz) lexicographic,
+// then components), so every y is bit-identical to apply_c's.  A quad with a
+// flagged DOF (unit / empty row or a neighbour of an excluded column) takes
+// apply_c per DOF.
+template <typename T, int NC, int NR, typename Geo, typename XS>
+__device__ __forceinline__ void apply4_c(const Geo &S, const T *c, const XS &x, int d0,
+                                         T (&y)[4][NC * NR]) {
+  if (S.flags && *reinterpret_cast<const uint32_t *>(S.flags + d0) != 0u) {
+#pragma unroll
+    for (int kk = 0; kk < 4; ++kk) {
+      T t[NC * NR];
+      apply_c<T, NC, NR>(S, c, x, d0 + kk, t);
+#pragma unroll
+      for (int u = 0; u < NC * NR; ++u) y[kk][u] = t[u];
+    }
+    return;
+  }
+  const Nbr b = neighbours(S, d0);
+  const int k0 = b.zk[1];
+  const int km = b.zk[0];                                  // k0 - 1 (wrapped)
+  const int kp = (k0 + 4 == S.nz) ? 0 : k0 + 4;            // k0 + 4 (wrapped)
+#pragma unroll
+  for (int kk = 0; kk < 4; ++kk)
+#pragma unroll
+    for (int u = 0; u < NC * NR; ++u) y[kk][u] = T(0);
+#pragma unroll
+  for (int ia = 0; ia < 3; ++ia)
+#pragma unroll
+    for (int ib = 0; ib < 3; ++ib) {
+      const int col = b.xi[ia] + b.yj[ib];
+      if (NC == 1) {
+        // w[z][r]: z = 0 is k0 - 1, 1..4 the quad, 5 is k0 + 4
+        T w[6][NR];
+        if (NR == 1) {
+          T v[4];
+          ld4<T>(x, (int64_t)col + k0, 0, v);
+          w[0][0] = ld<T>(x, (int64_t)col + km, 0);
+#pragma unroll
+          for (int e = 0; e < 4; ++e) w[1 + e][0] = v[e];
+          w[5][0] = ld<T>(x, (int64_t)col + kp, 0);
+        } else {
+#pragma unroll
+          for (int h = 0; h < NR; ++h) {
+            T v[4];
+            ld4<T>(x, (int64_t)(col + k0) * NR + 4 * h, (4 * h) % NR, v);
+#pragma unroll
+            for (int e = 0; e < 4; ++e) w[1 + (4 * h + e) / NR][(4 * h + e) % NR] = v[e];
+          }
+#pragma unroll
+          for (int r = 0; r < NR; ++r) {
+            w[0][r] = ld<T>(x, (int64_t)(col + km) * NR + r, r);
+            w[5][r] = ld<T>(x, (int64_t)(col + kp) * NR + r, r);
+          }
+        }
+#pragma unroll
+        for (int ic = 0; ic < 3; ++ic) {
+          const T cw = c[(ia * 3 + ib) * 3 + ic];
+#pragma unroll
+          for (int kk = 0; kk < 4; ++kk)
+#pragma unroll
+            for (int r = 0; r < NR; ++r) y[kk][r] = fma(cw, w[kk + ic][r], y[kk][r]);
+        }
+      } else {
+        const int n = S.n;
+        T w[3][6];
+#pragma unroll
+        for (int cm = 0; cm < 3; ++cm) {
+          const int64_t xc = (int64_t)cm * n + col;
+          T v[4];
+          ld4<T>(x, xc + k0, cm, v);
+          w[cm][0] = ld<T>(x, xc + km, cm);
+#pragma unroll
+          for (int e = 0; e < 4; ++e) w[cm][1 + e] = v[e];
+          w[cm][5] = ld<T>(x, xc + kp, cm);
+        }
+#pragma unroll
+        for (int ic = 0; ic < 3; ++ic) {
+          const int d = (ia * 3 + ib) * 3 + ic;
+#pragma unroll
+          for (int kk = 0; kk < 4; ++kk)
+#pragma unroll
+            for (int r = 0; r < 3; ++r) {
+              T acc = y[kk][r];
+              acc = fma(c[(r * 3 + 0) * 27 + d], w[0][kk + ic], acc);
+              acc = fma(c[(r * 3 + 1) * 27 + d], w[1][kk + ic], acc);
+              acc = fma(c[(r * 3 + 2) * 27 + d], w[2][kk + ic], acc);
+              y[kk][r] = acc;
+            }
+        }
+      }
+    }
+}
+
+// The NC*NR unknowns of the quad d0..d0+3 of a vector, as o[kk][u] (aligned vector accesses).
+template <typename T, int NC, int NR>
+__device__ __forceinline__ void quad_load(const T *v, int64_t n, int64_t d0, T (&o)[4][NC * NR]) {
+  if (NC == 3) {
+#pragma unroll
+    for (int cm = 0; cm < 3; ++cm) {
+      T t[4];
+      Vec4<T>::load(v + cm * n + d0, t);
+#pragma unroll
+      for (int kk = 0; kk < 4; ++kk) o[kk][cm] = t[kk];
+    }
+  } else {
+#pragma unroll
+    for (int h = 0; h < NR; ++h) {
+      T t[4];
+      Vec4<T>::load(v + d0 * NR + 4 * h, t);
+#pragma unroll
+      for (int e = 0; e < 4; ++e) o[(4 * h + e) / NR][(4 * h + e) % NR] = t[e];
+    }
+  }
+}
+
+template <typename T, int NC, int NR>
+__device__ __forceinline__ void quad_store(T *v, int64_t n, int64_t d0, const T (&o)[4][NC * NR]) {
+  if (NC == 3) {
+#pragma unroll
+    for (int cm = 0; cm < 3; ++cm) {
+      T t[4];
+#pragma unroll
+      for (int kk = 0; kk < 4; ++kk) t[kk] = o[kk][cm];
+      Vec4<T>::store(v + cm * n + d0, t);
+    }
+  } else {
+#pragma unroll
+    for (int h = 0; h < NR; ++h) {
+      T t[4];
+#pragma unroll
+      for (int e = 0; e < 4; ++e) t[e] = o[(4 * h + e) / NR][(4 * h + e) % NR];
+      Vec4<T>::store(v + d0 * NR + 4 * h, t);
+    }
+  }
+}
+
+// acc[sys(u)] += v[quad, u] * y[kk][u] over the quad, reading v in aligned groups of 4.
+template <int NC, int NR>
+__device__ __forceinline__ void quad_dot(const float *v, int64_t n, int64_t d0, const float (&y)[4][NC * NR],
+                                         float (&acc)[NC == 1 ? NR : 1]) {
+  if (NC == 3) {
+#pragma unroll
+    for (int cm = 0; cm < 3; ++cm) {
+      float t[4];
+      Vec4<float>::load(v + cm * n + d0, t);
+#pragma unroll
+      for (int kk = 0; kk < 4; ++kk) acc[0] = fmaf(t[kk], y[kk][cm], acc[0]);
+    }
+  } else {
+#pragma unroll
+    for (int h = 0; h < NR; ++h) {
+      float t[4];
+      Vec4<float>::load(v + d0 * NR + 4 * h, t);
+#pragma unroll
+      for (int e = 0; e < 4; ++e) {
+        const int kk = (4 * h + e) / NR, r = (4 * h + e) % NR;
+        acc[r] = fmaf(t[e], y[kk][r], acc[r]);
+      }
+    }
+  }
+}
+
+// ---------------------------------------------------------------- reliable-update CG state
+// State of one system of the FP32 CG with lagged FP64 reliable updates
+// (csrc/stencil.cu, csrc/batched.cu).  The transitions below are the whole
+// scalar logic of that solver; the kernels call them once per reduction.
+struct IRState {
+  double atol, resid, rho, r0;
+  int active, need, iters, unconv, updates, pad;
+};
+
+__device__ __forceinline__ void ir_init(IRState &s, double bnorm, double rr0, double tol) {
+  s.atol = tol * bnorm;
+  s.rho = rr0;
+  s.resid = sqrt(rr0);
+  s.r0 = s.resid;
+  s.active = bnorm != 0.0;
+  s.need = 0;
+  s.iters = 0;
+  s.unconv = 0;
+  s.updates = 0;
+}
+
+// After the p.q reduction (pq) with, for a pending update, the true residual
+// norm tt = t.t and tp = t.p: decide convergence on t and return alpha
+// (exact line search along p when t replaced the residual).  Returns true on
+// a non-finite value.
+__device__ __forceinline__ bool ir_after_pq(IRState &s, double pq, double tt, double tp, int maxiter, double &alpha) {
+  bool bad = false;
+  alpha = 0.0;
+  if (s.need) {
+    s.resid = sqrt(tt);
+    s.r0 = s.resid;
+    s.rho = tt;
+    if (!isfinite(s.resid)) bad = true;
+    if (s.resid <= s.atol) s.active = 0;
+    else if (s.iters >= maxiter) {
+      s.active = 0;
+      s.unconv = 1;
+    }
+  }
+  if (s.active) {
+    alpha = (s.need ? tp : s.rho) / pq;
+    if (!isfinite(alpha)) bad = true;
+  }
+  return bad;
+}
+
+// After the r.r reduction: count the iteration, schedule a reliable update
+// (residual fell by delta since the last true residual, reached the
+// threshold, or maxiter) and return beta.  Returns true on a non-finite value.
+__device__ __forceinline__ bool ir_after_rr(IRState &s, double rr, double delta, int maxiter, float &beta) {
+  s.need = 0;
+  beta = 0.0f;
+  if (!s.active) return false;
+  const bool bad = !isfinite(rr);
+  s.iters += 1;
+  const double rn = sqrt(rr);
+  s.need = (rn < delta * s.r0) || (rn <= s.atol) || (s.iters >= maxiter);
+  beta = (float)(rr / s.rho);
+  s.rho = rr;
+  return bad;
 }
 
 // y at one DOF with the operator's own (launch-parameter) coefficients.

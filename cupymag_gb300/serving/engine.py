@@ -9,9 +9,10 @@ Gauss-Seidel-projection step (cupymag/core/Micromagnetics.py:110-307) at a
 time:
 
 * each run's element-wise kernels run on its own data; each of the step's
-  solve slots (elasticity, demag, A1 x3, g1*, g2*, A2 x3) is ONE block-diagonal
-  CG launch over all runs that have that solve (one launch per coefficient
-  table);
+  solve slots (elasticity, demag, A1 x3, g1*, g2*, A2 x3) is one block-diagonal
+  CG launch over all runs that have that solve, per coefficient table and size
+  class (runs within a factor ``size_ratio`` of each other in DOFs share a
+  launch, since a launch lasts as long as its slowest system);
 * the step is captured in a CUDA graph once per batch composition: the first
   step after a change runs eagerly, the following ones replay the graph; the
   applied field follows each run's sweep through a device step counter;
@@ -25,6 +26,7 @@ every other kernel of a run reads and writes only that run's data.
 """
 from __future__ import annotations
 
+import math
 import time
 from collections import deque
 from dataclasses import dataclass, field
@@ -113,7 +115,7 @@ class ServeStats:
 
 class ServingEngine:
     def __init__(self, precision="IR", hbm_budget_gb=150.0, max_runs=64, use_graphs=True, device=None,
-                 keep_m=False):
+                 keep_m=False, size_ratio=4.0):
         N.require_cuda()
         self.dev = torch.device(device) if device is not None else torch.device("cuda", torch.cuda.current_device())
         self.precision = "DP" if precision == "DP" else "IR"
@@ -121,6 +123,9 @@ class ServingEngine:
         self.max_runs = int(max_runs)
         self.use_graphs = bool(use_graphs)
         self.keep_m = keep_m
+        # systems whose DOF counts differ by more than this ratio go to separate launches
+        # (a launch lasts as long as its slowest system; None: one launch per slot)
+        self.size_ratio = size_ratio
         self.infos = torch.zeros((self.max_runs, NSLOTS, N.CG_INFO_BYTES), dtype=torch.uint8, device=self.dev)
         self.free = list(range(self.max_runs))[::-1]
         self.active = []
@@ -161,8 +166,9 @@ class ServingEngine:
         groups = {}
         for run in self.active:
             L = run.solver
+            cls = 0 if not self.size_ratio else int(math.floor(math.log(L.n) / math.log(self.size_ratio)))
             for k, A, b, x in L.solve_slots():
-                key = (k, A.ncomp, 1 if b.dim() == 1 else int(b.shape[1]), coef_key(A))
+                key = (k, A.ncomp, 1 if b.dim() == 1 else int(b.shape[1]), coef_key(A), cls)
                 groups.setdefault(key, []).append(
                     BlockSystem(A, b, x, L.info[k], run.work, L.p.tol, L.p.maxiter, L.use_init))
         plans = {k: [] for k in range(NSLOTS)}
