@@ -131,6 +131,13 @@ def stencil_launch_bytes(A, nvec, iters, outer, fp32):
     return u * (88 * iters + 24)
 
 
+# DRAM bytes (read + write) per unknown and iteration of the FP32 stencil CG, measured with ncu on a GB300
+# (dram__bytes_read.sum + dram__bytes_write.sum of a 300-iteration elastic 128^3 launch / (300 x unknowns));
+# the vectors fit the L2 about half way, so this is below the 44 algorithmic bytes.  Traffic of a launch
+# is this figure times its unknowns and iterations (it grows in proportion at a fixed grid size).
+IR_STENCIL_DRAM_BYTES_PER_UNKNOWN_ITER = 21.4
+
+
 def cg_launch_bytes(A, nvec, iters, warm):
     n = A.shape[0]
     per_it = spmv_bytes(A, nvec) + 6 * n * 8 * nvec
@@ -183,11 +190,12 @@ def cpu_sample(p, S, iters_per_solve, cap=3):
 
 # ------------------------------------------------------------------ plain FP64 beside the precision form
 def fp64_check(args, S, p, L, m0, fields):
-    """The same steps from the same m0 with every solve in FP64 (stencil operators); returns (solver, ms)."""
+    """The same steps from the same m0 with every solve in FP64 (stencil operators on structured grids,
+    the same CSR matrices otherwise); returns (solver, ms)."""
     import torch
     from cupymag_gb300.physics.llg import LLGSolver
-    ops = (None, L.Fx, L.Fy, L.Fz, L.Deriv, None, None, None, None, L.F_el, L.Avg)
-    R = LLGSolver(S, p, precision="DP", operators="stencil", ops=ops)
+    ops = (L.A_demag, L.Fx, L.Fy, L.Fz, L.Deriv, L.A1, L.A2, L.F1, L.A_el, L.F_el, L.Avg)
+    R = LLGSolver(S, p, precision="DP", operators="stencil" if S.structured else "csr", ops=ops)
     R.set_magnetization(torch.as_tensor(m0))
     for s in range(args.warmup):
         R.step(fields[s])
@@ -261,8 +269,8 @@ def run_ours(args):
 
     p, w = workload(args.workload)
     t_setup = time.perf_counter()
-    S = SimulationOperators(p)
-    ops_kind = args.operators or ("csr" if args.precision == "DP" else "stencil")
+    S = SimulationOperators(p, mesh=w.get("mesh"))
+    ops_kind = args.operators or ("csr" if args.precision == "DP" or not S.structured else "stencil")
     L = LLGSolver(S, p, precision=args.precision, operators=ops_kind)
     torch.cuda.synchronize()
     t_setup = time.perf_counter() - t_setup
@@ -350,9 +358,15 @@ def run_ours(args):
     achieved = tot_bytes / (tot_ms / 1e3) / 1e9
     kname = {("csr", "DP"): "cg_fp64_kernel", ("csr", "IR"): "cg_ir_kernel",
              ("stencil", "DP"): "cg_stencil_fp64_kernel", ("stencil", "IR"): "cg_stencil_ir_kernel"}[(ops_kind, args.precision)]
+    traffic = None
+    if kname == "cg_stencil_ir_kernel" and "elasticity" in dom and args.workload == "hex128_me":
+        # per elasticity launch, scaled from the ncu capture of the same kernel on this grid
+        traffic = {"bytes_per_launch": round(IR_STENCIL_DRAM_BYTES_PER_UNKNOWN_ITER * 3 * S.n_dof *
+                                             dom["elasticity"][2] / args.steps / 1e9, 2), "unit": "GB",
+                   "source": "ncu dram bytes per unknown-iteration x this run's elasticity iterations"}
     roof = {"kernel": kname, "bound": "hbm",
             "achieved": round(achieved, 1), "peak": peak, "peak_kind": peak_kind, "unit": "GB/s",
-            "frac": round(achieved / peak, 4), "traffic": None,
+            "frac": round(achieved / peak, 4), "traffic": traffic,
             "share_of_step": round(tot_ms / ms, 4),
             "per_solve": {k: {"GB/s": round(v[0] / (v[1] / 1e3) / 1e9, 1), "ms": round(v[1] / args.steps, 3),
                               "iters": round(v[2] / args.steps, 1)} for k, v in dom.items()}}
@@ -382,7 +396,7 @@ def run_ours(args):
         v64 = args.steps / (ms64 / 1e3)
         err_m = float((m_timed - R.m).abs().max())
         err_avg = float((avg_timed - R.avg_m).abs().max() / R.avg_m.abs().max())
-        fp64 = {"steps_per_s": round(v64, 4), "ms_per_step": round(ms64 / args.steps, 3), "operators": "stencil",
+        fp64 = {"steps_per_s": round(v64, 4), "ms_per_step": round(ms64 / args.steps, 3), "operators": R.operators,
                 "speedup": round(value / world / v64, 3), "max_abs_m_err": err_m, "avg_m_rel_err": err_avg,
                 "after_steps": args.warmup + args.steps, "bound": 1e-6}
         del R
@@ -414,7 +428,10 @@ def run_ours(args):
             "warmup": args.warmup, "ms_per_step": round(ms_max / args.steps, 3), "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64" if args.precision == "DP" else "f32+f64",
             "data": "synthetic (seeded m0 = normalise((1,0,0)+N(0,1e-3)), fixed field sweep)",
-            "config": {"workload": args.workload, "mesh": f"hex {w['n']}^3 periodic, defect {w['defect']}^3",
+            "config": {"workload": args.workload,
+                       "mesh": (f"hex {w['n']}^3 periodic, defect {w['defect']}^3" if S.structured else
+                                f"{w['n']}^3 cube of Kuhn tets ({S.n_elements} tets, interior nodes jittered "
+                                f"+-{w['jitter']} h), {w['defect']} defect, seeded rotation"),
                        "n_dof": S.n_dof, "magnetoelastic": w["ME"], "rot111": w["rot111"],
                        "precision": args.precision, "operators": ops_kind, "tol": p.tol, "sweep": f"+{w['B0']} T -> -{w['B0']} T over "
                        f"{w['steps']} steps", "timed_steps": f"{args.warmup}..{args.warmup + args.steps - 1}",
@@ -450,7 +467,7 @@ def run_reference(args):
     p, w = workload(args.workload)
     dev = "cuda" if torch.cuda.is_available() else "cpu"
     # setup only (not timed): the structured assembly builds the same CSR matrices
-    S = SimulationOperators(p, device=dev)
+    S = SimulationOperators(p, device=dev, mesh=w.get("mesh"))
     its = REFERENCE_ITERS.get(args.workload)
     times = []
     for s in range(args.warmup + args.steps):

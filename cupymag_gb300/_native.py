@@ -79,6 +79,7 @@ _PROTOS = {
                                        vp]),
     "cpm_cg_solve_blockdiag": (C.c_int, [C.POINTER(BatchPlan), C.POINTER(CGOpts), vp]),
     "cpm_record_step": (C.c_int, [vp, vp, vp, vp, i32, vp]),
+    "cpm_coo_segment_sum": (C.c_int, [vp, vp, i64, vp, vp]),
     "cpm_llg_field": (C.c_int, [C.POINTER(FieldParams), i64, vp, vp, vp, vp, dbl, vp, vp, vp]),
     "cpm_gs_star": (C.c_int, [C.c_int, i64, vp, vp, vp, vp, vp, dbl, vp, vp, vp]),
     "cpm_renorm_sumsq": (C.c_int, [i64, vp, vp, vp, vp, vp, dbl, dbl, vp, vp, vp, vp, vp]),

@@ -43,6 +43,8 @@ def main(argv=None):
     ap.add_argument("--solves", type=int, default=3)
     ap.add_argument("--maxiter", type=int, default=20000)
     ap.add_argument("--batch", type=int, default=1)
+    ap.add_argument("--inner-tol", type=float, default=0.1,
+                    help="reliable-update factor of the FP32 solver (residual drop between FP64 updates)")
     args = ap.parse_args(argv)
 
     from . import _native as N
@@ -79,11 +81,12 @@ def main(argv=None):
             systems.append(BlockSystem(op, bd, torch.zeros_like(bd), new_info(1)[0],
                                        torch.empty(work_bytes(op.n, op.ncomp, nrhs, args.precision),
                                                    dtype=torch.uint8, device="cuda"), p.tol, args.maxiter))
-        plan = BlockDiagPlan(systems, args.precision)
+        plan = BlockDiagPlan(systems, args.precision, inner_tol=args.inner_tol)
         launch = plan.launch
         info_of = lambda: systems[0].info  # noqa: E731
     else:
         solver = CGSolver()
+        solver.inner_tol = args.inner_tol
         x = torch.zeros_like(bd)
         info = new_info(1)
 
@@ -105,6 +108,7 @@ def main(argv=None):
     ms = float(np.median(times))
     nb = _bytes(op, nrhs, its, d["outer"], args.precision == "IR", csr) * args.batch
     print(json.dumps({"op": args.op, "edge": args.edge, "n": n, "nrhs": nrhs, "precision": args.precision,
+                      "inner_tol": args.inner_tol,
                       "operators": args.operators, "batch": args.batch, "status": N.STATUS_NAMES[d["status"]],
                       "iters": its, "outer": d["outer"], "ms_per_solve": round(ms, 3),
                       "us_per_iter": round(1e3 * ms / max(its, 1), 2), "GB/s": round(nb / (ms / 1e3) / 1e9, 1),

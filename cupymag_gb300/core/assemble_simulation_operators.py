@@ -35,6 +35,9 @@ def _device_csr(indptr, indices, data, shape):
     return DeviceCSR(ip.contiguous(), indices.contiguous(), data.contiguous(), shape)
 
 
+DEVICE_COO_ELEMENTS = 200_000  # unstructured meshes at least this large assemble on the device
+
+
 class SimulationOperators:
     def __init__(self, params, device=None, assembly="auto", mesh=None):
         self.p = params
@@ -62,11 +65,14 @@ class SimulationOperators:
         self.alpha2 = params.alpha2
         g = self.fem_grid
         structured = isinstance(g, HexGrid) and min(g.Nx, g.Ny, g.Nz) >= 3
-        if assembly == "coo":
+        if assembly in ("coo", "device"):
             structured = False
         elif assembly == "structured" and not structured:
             raise ValueError("structured assembly needs a hex grid with at least 3 cells per axis")
         self.structured = structured
+        # unstructured meshes: host COO (SciPy) for small meshes, device COO for large ones
+        self.device_coo = assembly == "device" or (assembly == "auto" and not structured
+                                                    and self.n_elements >= DEVICE_COO_ELEMENTS)
         self._coo_ops = None
         self._elem = None
 
@@ -76,11 +82,24 @@ class SimulationOperators:
         return AS.stiffness_voigt(p.c11, p.c12, p.c44, get_M_matrix() if p.rot111 else None)
 
     def _coo(self):
+        """Operators of the general COO path: SciPy CSR (host) or DeviceCSR (device assembly)."""
         if self._coo_ops is None:
-            self._coo_ops = AS.assemble_coo(self.node_coords_np, self.elements_np, self.global_id_np, self.n_dof,
-                                            self.DefDOF, self.alpha1, self.alpha2, ME=self.p.ME,
-                                            C=self._C() if self.p.ME else None)
+            args = (self.node_coords_np, self.elements_np, self.global_id_np, self.n_dof, self.DefDOF, self.alpha1,
+                    self.alpha2)
+            kw = dict(ME=self.p.ME, C=self._C() if self.p.ME else None)
+            if self.device_coo:
+                from ..physics.device_assembly import assemble_device
+                n = self.n_dof
+                shapes = {"A_el": (3 * n, 3 * n), "F_el": (3 * n, 6 * n)}
+                dev_ops = assemble_device(*args, device=self.device, **kw)
+                self._coo_ops = {k: _device_csr(*v, shapes.get(k, (n, n))) for k, v in dev_ops.items()}
+            else:
+                self._coo_ops = AS.assemble_coo(*args, **kw)
         return self._coo_ops
+
+    def _coo_op(self, name):
+        A = self._coo()[name]
+        return A if isinstance(A, DeviceCSR) else DeviceCSR.from_scipy(A, self.device)
 
     def _cell(self):
         """Element matrices of the unit cell at the origin (all cells are identical)."""
@@ -109,7 +128,7 @@ class SimulationOperators:
         if self.structured:
             A = self._scalar(self._cell()["K"], anchors=(0,))
         else:
-            A = DeviceCSR.from_scipy(self._coo()["A_demag"], self.device)
+            A = self._coo_op("A_demag")
         return (A, *self.derivative_operators())
 
     def derivative_operators(self):
@@ -117,8 +136,7 @@ class SimulationOperators:
         if self.structured:
             Fs = [self._scalar(f) for f in self._cell()["F"]]
         else:
-            ops = self._coo()
-            Fs = [DeviceCSR.from_scipy(ops[k], self.device) for k in ("Fx", "Fy", "Fz")]
+            Fs = [self._coo_op(k) for k in ("Fx", "Fy", "Fz")]
         # the three derivative matrices share one pattern: keep one index copy
         for f in Fs[1:]:
             if f.same_pattern(Fs[0]):
@@ -135,7 +153,7 @@ class SimulationOperators:
             ip, ix, dv = SH.elastic_F_csr(g.Nx, g.Ny, g.Nz, SF, self.device)
             ip, ix, dv = SH.anchor(ip, ix, dv, (0, n, 2 * n), cols_too=False, diag_one=False)
             return _device_csr(ip, ix, dv, (3 * n, 6 * n))
-        return DeviceCSR.from_scipy(self._coo()["F_el"], self.device)
+        return self._coo_op("F_el")
 
     def csr_GS(self):
         if self.structured:
@@ -144,8 +162,7 @@ class SimulationOperators:
             A2 = self._scalar(e["K"] * self.alpha2 + e["M"], defect=self.DefDOF)
             F1 = self._scalar(e["M"], defect=self.DefDOF, rows_only=True)
             return A1, A2, F1
-        ops = self._coo()
-        return tuple(DeviceCSR.from_scipy(ops[k], self.device) for k in ("A1", "A2", "F1"))
+        return tuple(self._coo_op(k) for k in ("A1", "A2", "F1"))
 
     def csr_elasticity(self):
         if not self.p.ME:
@@ -159,8 +176,7 @@ class SimulationOperators:
             ip, ix, dv = SH.anchor(ip, ix, dv, (0, n, 2 * n))
             A_el = _device_csr(ip, ix, dv, (3 * n, 3 * n))
             return A_el, self.elastic_rhs_operator()
-        ops = self._coo()
-        return DeviceCSR.from_scipy(ops["A_el"], self.device), DeviceCSR.from_scipy(ops["F_el"], self.device)
+        return self._coo_op("A_el"), self._coo_op("F_el")
 
     def stencil_operators(self):
         """Matrix-free forms of A_demag, A1, A2, F1 (and A_el with ME) for structured hex grids."""

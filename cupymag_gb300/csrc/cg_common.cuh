@@ -10,9 +10,9 @@ constexpr int kCGWarps = kCGThreads / kWarp;
 constexpr int kMaxGrid = 4096;                 // CTAs of one cooperative launch (upper bound)
 constexpr size_t kPartHalf = (size_t)9 * kMaxGrid;  // doubles per half of the partials buffer (<= 9 sums per CTA)
 
-// Block-wide sum of NV values per thread, deterministic; result broadcast.
-template <int NV>
-__device__ __forceinline__ void block_sum(double (&v)[NV], double (*s)[kCGWarps]) {
+// Block-wide sum of NV values per thread over NW warps, deterministic; result broadcast.
+template <int NV, int NW>
+__device__ __forceinline__ void block_sum(double (&v)[NV], double (*s)[NW]) {
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
 #pragma unroll
   for (int j = 0; j < NV; ++j) {
@@ -24,7 +24,7 @@ __device__ __forceinline__ void block_sum(double (&v)[NV], double (*s)[kCGWarps]
   for (int j = 0; j < NV; ++j) {
     double t = 0.0;
 #pragma unroll
-    for (int k = 0; k < kCGWarps; ++k) t += s[j][k];
+    for (int k = 0; k < NW; ++k) t += s[j][k];
     v[j] = t;
   }
   __syncthreads();
@@ -34,9 +34,9 @@ __device__ __forceinline__ void block_sum(double (&v)[NV], double (*s)[kCGWarps]
 // The partials buffer alternates between two halves: a CTA may start writing
 // the next reduction's partials while slower CTAs still read this one's, and
 // the barrier of the next reduction orders the reuse of a half.
-template <int NV>
+template <int NV, int NW>
 __device__ __forceinline__ bool grid_sum(double (&v)[NV], double *part, int &parity, GridBarrier *bar,
-                                         unsigned long long tns, double (*s)[kCGWarps]) {
+                                         unsigned long long tns, double (*s)[NW]) {
   block_sum<NV>(v, s);
   const int G = gridDim.x;
   part += (size_t)parity * kPartHalf;

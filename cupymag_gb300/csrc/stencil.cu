@@ -212,11 +212,17 @@ __global__ void __launch_bounds__(kCGThreads) cg_stencil_fp64_kernel(const __gri
 // product runs on quads of 4 DOFs along z (apply4_c).  The CG state lives in
 // shared memory (IRState), updated by thread 0 after each reduction, so the
 // DOF loops keep only alpha/beta and bitmasks in registers.
+// 256-thread CTAs, four per SM (measured faster than one 1024-thread CTA per
+// SM: the CTA-wide reductions and barriers of 32 warps cost more than the
+// extra grid-barrier arrivals of 4x as many CTAs).
+constexpr int kIRThreads = 256;
+
 template <int NC, int NR>
-__global__ void __launch_bounds__(kCGThreads, 4) cg_stencil_ir_kernel(const __grid_constant__ StencilCG a) {
+__global__ void __launch_bounds__(kIRThreads, 4) cg_stencil_ir_kernel(const __grid_constant__ StencilCG a) {
   constexpr int U = NC * NR;
   constexpr int NS = n_systems<NC, NR>();
-  __shared__ double s_red[9][kCGWarps];
+  constexpr int TH = kIRThreads;
+  __shared__ double s_red[9][TH / kWarp];
   __shared__ IRState st[NS];
   __shared__ float s_ab[NS];
   __shared__ int s_mask[3];  // active, need, error status
@@ -235,7 +241,7 @@ __global__ void __launch_bounds__(kCGThreads, 4) cg_stencil_ir_kernel(const __gr
   double v[2 * NS];
 #pragma unroll
   for (int j = 0; j < 2 * NS; ++j) v[j] = 0.0;
-  for (int64_t dof = d0 + threadIdx.x; dof < d1; dof += kCGThreads) {
+  for (int64_t dof = d0 + threadIdx.x; dof < d1; dof += TH) {
     double y[U];
     if (use_init) apply<double, NC, NR>(a.S, x, (int)dof, y);
 #pragma unroll
@@ -271,7 +277,7 @@ __global__ void __launch_bounds__(kCGThreads, 4) cg_stencil_ir_kernel(const __gr
   __syncthreads();
   int activem = s_mask[0], needm = 0;
   if (use_init) {
-    for (int64_t dof = d0 + threadIdx.x; dof < d1; dof += kCGThreads)
+    for (int64_t dof = d0 + threadIdx.x; dof < d1; dof += TH)
 #pragma unroll
       for (int u = 0; u < U; ++u)
         if (!((activem >> sys_of<NC, NR>(u)) & 1)) x[uidx<NC, NR>(n, dof, u)] = b[uidx<NC, NR>(n, dof, u)];
@@ -284,14 +290,14 @@ __global__ void __launch_bounds__(kCGThreads, 4) cg_stencil_ir_kernel(const __gr
 #pragma unroll
     for (int j = 0; j < NS; ++j) pqf[j] = 0.0f;
     if (quads) {
-      for (int64_t qd = d0 + 4 * threadIdx.x; qd < d1; qd += 4 * kCGThreads) {
+      for (int64_t qd = d0 + 4 * threadIdx.x; qd < d1; qd += 4 * TH) {
         float y[4][U];
         apply4_c<float, NC, NR>(a.S, a.S.c32, p32, (int)qd, y);
         quad_store<float, NC, NR>(q32, n, qd, y);
         quad_dot<NC, NR>(p32, n, qd, y, pqf);
       }
     } else {
-      for (int64_t dof = d0 + threadIdx.x; dof < d1; dof += kCGThreads) {
+      for (int64_t dof = d0 + threadIdx.x; dof < d1; dof += TH) {
         float y[U];
         apply<float, NC, NR>(a.S, p32, (int)dof, y);
 #pragma unroll
@@ -310,7 +316,7 @@ __global__ void __launch_bounds__(kCGThreads, 4) cg_stencil_ir_kernel(const __gr
       pt[2 * NS + j] = 0.0;
     }
     if (needm) {
-      for (int64_t dof = d0 + threadIdx.x; dof < d1; dof += kCGThreads) {
+      for (int64_t dof = d0 + threadIdx.x; dof < d1; dof += TH) {
         double yx[U], yd[U];
         apply<double, NC, NR>(a.S, x, (int)dof, yx);
         apply_c<double, NC, NR>(a.S, a.S.c64, d32, (int)dof, yd);
@@ -349,7 +355,7 @@ __global__ void __launch_bounds__(kCGThreads, 4) cg_stencil_ir_kernel(const __gr
     float rrf[NS];
 #pragma unroll
     for (int j = 0; j < NS; ++j) rrf[j] = 0.0f;
-    for (int64_t dof = d0 + threadIdx.x; dof < d1; dof += kCGThreads) {
+    for (int64_t dof = d0 + threadIdx.x; dof < d1; dof += TH) {
 #pragma unroll
       for (int u = 0; u < U; ++u) {
         const int s = sys_of<NC, NR>(u);
@@ -393,7 +399,7 @@ __global__ void __launch_bounds__(kCGThreads, 4) cg_stencil_ir_kernel(const __gr
 #pragma unroll
     for (int j = 0; j < NS; ++j) beta[j] = s_ab[j];
     // ---- phase 3: p = r32 + beta p
-    for (int64_t dof = d0 + threadIdx.x; dof < d1; dof += kCGThreads) {
+    for (int64_t dof = d0 + threadIdx.x; dof < d1; dof += TH) {
 #pragma unroll
       for (int u = 0; u < U; ++u) {
         const int s = sys_of<NC, NR>(u);
@@ -502,8 +508,9 @@ static int launch_stencil_cg(const cpm_stencil *s, const double *b, double *x, c
   a.timeout_ns = (unsigned long long)(tmo * 1e9);
   const bool fp64 = o->precision == 0;
   const void *fn = fp64 ? (const void *)cg_stencil_fp64_kernel<NC, NR> : (const void *)cg_stencil_ir_kernel<NC, NR>;
+  const int threads = fp64 ? kCGThreads : kIRThreads;
   int occ = 0;
-  CPM_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fn, kCGThreads, 0));
+  CPM_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fn, threads, 0));
   if (occ < 1) {
     set_error("stencil cg: kernel cannot be resident on an SM");
     return CPM_CUDA_ERROR;
@@ -511,7 +518,7 @@ static int launch_stencil_cg(const cpm_stencil *s, const double *b, double *x, c
   const int64_t n = a.S.n;
   int64_t gmax = (int64_t)occ * sm_count();
   if (gmax > kMaxGrid) gmax = kMaxGrid;
-  int64_t G = (n + 255) / 256;
+  int64_t G = (n + threads - 1) / threads;
   if (G > gmax) G = gmax;
   if (G < 1) G = 1;
   int64_t per = (n + G - 1) / G;
@@ -522,7 +529,7 @@ static int launch_stencil_cg(const cpm_stencil *s, const double *b, double *x, c
   CPM_TRY(cudaMemsetAsync(w.bar, 0, sizeof(GridBarrier), st));
   CPM_TRY(cudaMemsetAsync(info, 0, sizeof(cpm_cg_info), st));
   void *args[] = {&a};
-  CPM_TRY(cudaLaunchCooperativeKernel(fn, dim3((unsigned)G), dim3(kCGThreads), args, 0, st));
+  CPM_TRY(cudaLaunchCooperativeKernel(fn, dim3((unsigned)G), dim3(threads), args, 0, st));
   return CPM_OK;
 }
 

@@ -13,9 +13,12 @@ time:
   CG launch over all runs that have that solve, per coefficient table and size
   class (runs within a factor ``size_ratio`` of each other in DOFs share a
   launch, since a launch lasts as long as its slowest system);
-* the step is captured in a CUDA graph once per batch composition: the first
-  step after a change runs eagerly, the following ones replay the graph; the
-  applied field follows each run's sweep through a device step counter;
+* runs are grouped by size class; a group's step is captured in a CUDA graph
+  once per group composition (the first step after a change runs eagerly,
+  the following ones replay the graph); the applied field follows each run's
+  sweep through a device step counter; the loop steps the group that has
+  used the least GPU time so far, so small runs are not held to the pace of
+  large ones;
 * after each step one device-to-host copy returns every run's solver status;
   a run that finished its sweep is retired (slot and memory released, its
   final m and <m> history copied out) and waiting requests are admitted.
@@ -113,9 +116,26 @@ class ServeStats:
         return self.steps / self.makespan_s if self.makespan_s > 0 else 0.0
 
 
+class _Group:
+    """Runs of one size class: stepped together, with their own plans and CUDA graph."""
+
+    def __init__(self, cls):
+        self.cls = cls
+        self.runs = []
+        self.plans = None
+        self.graph = None
+        self.eager_since_change = 0
+        self.gpu_s = 0.0          # measured step time spent on this group (scheduling key)
+
+    def changed(self):
+        self.plans = None
+        self.graph = None
+        self.eager_since_change = 0
+
+
 class ServingEngine:
     def __init__(self, precision="IR", hbm_budget_gb=150.0, max_runs=64, use_graphs=True, device=None,
-                 keep_m=False, size_ratio=4.0):
+                 keep_m=False, size_ratio=4.0, time_launches=False):
         N.require_cuda()
         self.dev = torch.device(device) if device is not None else torch.device("cuda", torch.cuda.current_device())
         self.precision = "DP" if precision == "DP" else "IR"
@@ -123,17 +143,28 @@ class ServingEngine:
         self.max_runs = int(max_runs)
         self.use_graphs = bool(use_graphs)
         self.keep_m = keep_m
-        # systems whose DOF counts differ by more than this ratio go to separate launches
-        # (a launch lasts as long as its slowest system; None: one launch per slot)
+        # runs whose DOF counts lie in the same power of size_ratio form one group (None: a
+        # single group); a launch lasts as long as its slowest system, and groups are stepped
+        # independently, the one with the least step time spent so far first
         self.size_ratio = size_ratio
+        # diagnostic: CUDA events around every block-diagonal launch (steps run eagerly);
+        # per (slot, group) milliseconds accumulate in stats.extra["launch_ms"]
+        self.time_launches = bool(time_launches)
+        if self.time_launches:
+            self.use_graphs = False
+        self._events = []
         self.infos = torch.zeros((self.max_runs, NSLOTS, N.CG_INFO_BYTES), dtype=torch.uint8, device=self.dev)
         self.free = list(range(self.max_runs))[::-1]
-        self.active = []
+        self.groups = {}
         self.used = 0
-        self.plans = None
-        self.graph = None
-        self.eager_since_change = 0
         self.stats = ServeStats()
+
+    @property
+    def active(self):
+        return [r for g in self.groups.values() for r in g.runs]
+
+    def _cls(self, n):
+        return 0 if not self.size_ratio else int(math.floor(math.log(n) / math.log(self.size_ratio)))
 
     # ------------------------------------------------------------------ admission
     def fits(self, req) -> bool:
@@ -150,102 +181,121 @@ class ServingEngine:
         L.set_magnetization(torch.as_tensor(seeded_m0(S.n_dof, S.DefDOF, req.seed)))
         work = torch.empty(work_bytes(S.n_dof, 3, 1, self.precision), dtype=torch.uint8, device=self.dev)
         run = Run(req, L, slot, work, est, now)
-        self.active.append(run)
+        cls = self._cls(L.n)
+        g = self.groups.get(cls)
+        if g is None:
+            g = self.groups[cls] = _Group(cls)
+            # a new group starts level with the least-served group, so it does not monopolise the GPU
+            busy = [h.gpu_s for h in self.groups.values() if h.runs and h is not g]
+            g.gpu_s = min(busy) if busy else 0.0
+        g.runs.append(run)
+        g.changed()
         self.used += est
         self.stats.peak_budget_gb = max(self.stats.peak_budget_gb, self.used / 1e9)
-        self._changed()
         return run
 
-    def _changed(self):
-        self.plans = None
-        self.graph = None
-        self.eager_since_change = 0
-
-    # ------------------------------------------------------------------ one batched step
-    def _build_plans(self):
-        groups = {}
-        for run in self.active:
+    # ------------------------------------------------------------------ one batched step of a group
+    def _build_plans(self, g):
+        sys_by_key = {}
+        for run in g.runs:
             L = run.solver
-            cls = 0 if not self.size_ratio else int(math.floor(math.log(L.n) / math.log(self.size_ratio)))
             for k, A, b, x in L.solve_slots():
-                key = (k, A.ncomp, 1 if b.dim() == 1 else int(b.shape[1]), coef_key(A), cls)
-                groups.setdefault(key, []).append(
+                key = (k, A.ncomp, 1 if b.dim() == 1 else int(b.shape[1]), coef_key(A))
+                sys_by_key.setdefault(key, []).append(
                     BlockSystem(A, b, x, L.info[k], run.work, L.p.tol, L.p.maxiter, L.use_init))
         plans = {k: [] for k in range(NSLOTS)}
-        for key, systems in groups.items():
+        for key, systems in sys_by_key.items():
             plans[key[0]].append(BlockDiagPlan(systems, self.precision, device=self.dev))
-        self.plans = plans
+        g.plans = plans
 
-    def _step_all(self):
-        """Launch one step of every active run: element-wise kernels per run, one CG launch per slot."""
-        gens = [r.solver.step_gen(None) for r in self.active]
-        cur = [next(g, None) for g in gens]
+    def _step_runs(self, g):
+        """Launch one step of every run of the group: element-wise kernels per run, one CG launch per slot."""
+        gens = [r.solver.step_gen(None) for r in g.runs]
+        cur = [next(x, None) for x in gens]
         for k in range(NSLOTS):
             idx = [i for i, q in enumerate(cur) if q is not None and q.k == k]
             if not idx:
                 continue
-            for plan in self.plans[k]:
-                plan.launch()
+            for plan in g.plans[k]:
+                if self.time_launches:
+                    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                    e0.record()
+                    plan.launch()
+                    e1.record()
+                    self._events.append((f"slot{k}/group{g.cls}", e0, e1))
+                else:
+                    plan.launch()
                 self.stats.blockdiag_launches += 1
             for i in idx:
                 cur[i] = next(gens[i], None)
         if any(q is not None for q in cur):
             raise RuntimeError("a run requested a solve outside the step's slot order")
 
-    def step(self):
-        """Advance every active run by one step (asynchronous)."""
-        if self.plans is None:
-            self._build_plans()
-        if self.graph is None and self.use_graphs and self.eager_since_change >= 1:
+    def step(self, g=None):
+        """Advance every run of group g (all groups when None) by one step (asynchronous)."""
+        if g is None:
+            for h in list(self.groups.values()):
+                if h.runs:
+                    self.step(h)
+            return
+        if g.plans is None:
+            self._build_plans(g)
+        if g.graph is None and self.use_graphs and g.eager_since_change >= 1:
             try:
-                g = torch.cuda.CUDAGraph()
-                with torch.cuda.graph(g):
-                    self._step_all()
-                self.graph = g
+                gr = torch.cuda.CUDAGraph()
+                with torch.cuda.graph(gr):
+                    self._step_runs(g)
+                g.graph = gr
                 self.stats.captures += 1
             except Exception as e:  # capture unsupported: keep stepping eagerly
                 self.use_graphs = False
                 self.stats.graph_error = f"{type(e).__name__}: {e}"
                 torch.cuda.synchronize(self.dev)
-        if self.graph is not None:
-            self.graph.replay()
+        if g.graph is not None:
+            g.graph.replay()
             self.stats.graph_steps += 1
         else:
-            self._step_all()
+            self._step_runs(g)
             self.stats.eager_steps += 1
-            self.eager_since_change += 1
-        b = len(self.active)
+            g.eager_since_change += 1
+        b = len(g.runs)
         self.stats.batch_steps += 1
         self.stats.mean_batch += b
-        self.stats.max_batch = max(self.stats.max_batch, b)
-        for r in self.active:
+        self.stats.max_batch = max(self.stats.max_batch, len(self.active))
+        for r in g.runs:
             r.steps_done += 1
 
     # ------------------------------------------------------------------ completion
-    def _poll(self, now, results):
+    def _poll(self, now, results, groups=None):
         """Read every run's solver status (one copy) and retire finished or failed runs."""
         raw = self.infos.cpu().numpy()
-        retired = False
-        for run in list(self.active):
-            err = None
-            for k, *_ in run.solver.solve_slots():
-                d = decode_info(raw[run.slot, k])
-                if d["status"] != N.CPM_OK:
-                    err = (f"step {run.steps_done}: CG for {SOLVE_NAMES[k]} ended with "
-                           f"{N.STATUS_NAMES.get(d['status'], d['status'])} (iterations {d['iters']})")
-                    break
-            if err is None and run.steps_done < run.req.steps:
-                continue
-            L = run.solver
-            results[run.req.rid] = Result(run.req.rid, run.req.arrival, run.t_admit, now, run.steps_done,
-                                          L.hist[:run.steps_done].cpu().numpy(),
-                                          L.m.cpu().numpy() if self.keep_m else None, err)
-            self.active.remove(run)
-            self.free.append(run.slot)
-            self.used -= run.est_bytes
-            retired = True
-        if retired:
-            self._changed()
+        if self._events:
+            lm = self.stats.extra.setdefault("launch_ms", {})
+            for name, e0, e1 in self._events:
+                lm[name] = lm.get(name, 0.0) + e0.elapsed_time(e1)
+            self._events = []
+        for g in (groups if groups is not None else list(self.groups.values())):
+            retired = False
+            for run in list(g.runs):
+                err = None
+                for k, *_ in run.solver.solve_slots():
+                    d = decode_info(raw[run.slot, k])
+                    if d["status"] != N.CPM_OK:
+                        err = (f"step {run.steps_done}: CG for {SOLVE_NAMES[k]} ended with "
+                               f"{N.STATUS_NAMES.get(d['status'], d['status'])} (iterations {d['iters']})")
+                        break
+                if err is None and run.steps_done < run.req.steps:
+                    continue
+                L = run.solver
+                results[run.req.rid] = Result(run.req.rid, run.req.arrival, run.t_admit, now, run.steps_done,
+                                              L.hist[:run.steps_done].cpu().numpy(),
+                                              L.m.cpu().numpy() if self.keep_m else None, err)
+                g.runs.remove(run)
+                self.free.append(run.slot)
+                self.used -= run.est_bytes
+                retired = True
+            if retired:
+                g.changed()
 
     def serve(self, requests, realtime=True):
         """Serve the requests (arrival offsets in seconds when realtime); returns ({rid: Result}, ServeStats)."""
@@ -259,21 +309,27 @@ class ServingEngine:
         torch.cuda.synchronize(self.dev)
         t0 = time.perf_counter()
         clock = lambda: time.perf_counter() - t0  # noqa: E731
-        while pending or self.active:
+
+        def admit_arrived():
             now = clock()
             while pending and (not realtime or pending[0].arrival <= now) and self.fits(pending[0]):
                 self.admit(pending.popleft(), now)
-            if not self.active:
+
+        while pending or any(g.runs for g in self.groups.values()):
+            admit_arrived()
+            live = [g for g in self.groups.values() if g.runs]
+            if not live:
                 if pending:
                     time.sleep(max(0.0, min(pending[0].arrival - clock(), 0.05)))
                 continue
-            self.step()
+            g = min(live, key=lambda h: (h.gpu_s, h.cls))
+            ts = time.perf_counter()
+            self.step(g)
             # requests that arrived meanwhile are set up while the step runs
-            now = clock()
-            while pending and (not realtime or pending[0].arrival <= now) and self.fits(pending[0]):
-                self.admit(pending.popleft(), now)
+            admit_arrived()
             torch.cuda.synchronize(self.dev)
-            self._poll(clock(), results)
+            g.gpu_s += time.perf_counter() - ts
+            self._poll(clock(), results, [g])
         st = self.stats
         done = [r for r in results.values() if r.completed > 0]
         first = min((r.arrival for r in done), default=0.0)

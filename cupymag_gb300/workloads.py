@@ -52,7 +52,56 @@ WORKLOADS = {
 }
 
 
+TET_WORKLOADS = {
+    # 96^3 cube of Kuhn tets (5.3 M tets), interior nodes jittered +-0.2 h, rotated ellipsoidal defect
+    "tet96_me": dict(n=96, jitter=0.2, axes=(0.15, 0.10, 0.08), ME=True, rot111=True, steps=300, B0=0.1, seed=96),
+    "tet32_me": dict(n=32, jitter=0.2, axes=(0.15, 0.10, 0.08), ME=True, rot111=True, steps=300, B0=0.1, seed=32),
+}
+
+
+def seeded_rotation(seed):
+    """A proper rotation matrix from the QR factors of a seeded normal matrix."""
+    rng = np.random.default_rng(seed)
+    q, r = np.linalg.qr(rng.normal(size=(3, 3)))
+    q = q @ np.diag(np.sign(np.diag(r)))
+    if np.linalg.det(q) < 0:
+        q[:, 0] = -q[:, 0]
+    return q
+
+
+def tet_workload(w):
+    """(params, mesh) of a Kuhn-tet cube: edge n (h = 1, the reference's length unit), the defect's
+    semi-axes a fraction of the edge, centred at the box centre, with a seeded rotation."""
+    from .mesh.grids import TetraGrid, kuhn_tet_cube
+    from .utils.defect_shapes import get_defect_shape_function
+    n = w["n"]
+    coords, tets = kuhn_tet_cube(n, jitter=w["jitter"], seed=w["seed"])
+    axes = tuple(float(f) * n for f in w["axes"])
+    R = seeded_rotation(w["seed"] + 1)
+    p = SimParams(**MAGNETIC)
+    if w["ME"]:
+        for k, v in ELASTIC.items():
+            setattr(p, k, v)
+    p.grid_type = "Tet"
+    p.ME = w["ME"]
+    p.rot111 = w["rot111"]
+    p.defect_shape = "RotatedEllipsoid"
+    p.defect_parameters = axes
+    p.defect_rotation = R.tolist()
+    p = p.finalize()
+    mesh = TetraGrid(coords=coords, tets=tets,
+                     defect_shape=get_defect_shape_function("RotatedEllipsoid", (axes, R)))
+    return p, mesh
+
+
 def workload(name, **overrides):
+    """(params, workload dict); tet workloads carry their in-memory mesh as w["mesh"]."""
+    if name in TET_WORKLOADS:
+        w = dict(TET_WORKLOADS[name])
+        w.update(overrides)
+        p, w["mesh"] = tet_workload(w)
+        w["defect"] = "ellipsoid %s" % (tuple(round(a * w["n"], 2) for a in w["axes"]),)
+        return p, w
     w = dict(WORKLOADS[name])
     w.update(overrides)
     p = hex_params(w["n"], w["defect"], w["ME"], w["rot111"])

@@ -199,6 +199,15 @@ int cpm_batch_plan_build(const cpm_batch_system *sys, int32_t nsys, int32_t ncom
  * warm-start flags come from the systems. */
 int cpm_cg_solve_blockdiag(const cpm_batch_plan *plan, const cpm_cg_opts *opts, void *stream);
 
+/* ---- device assembly (unstructured meshes) ----
+ * Duplicate summation of the COO -> CSR conversion that the reference leaves
+ * to cupyx (cupymag/utils/final_assembly.py:160-205, assemble_stiffness_matrix
+ * and assemble_mass_matrix): vals_sorted holds the element entries ordered by
+ * a stable sort on (row, col); seg_start[0..nseg] delimits the runs of equal
+ * (row, col); out[s] is the in-order sum of run s (deterministic). */
+int cpm_coo_segment_sum(const double *vals_sorted, const int64_t *seg_start, int64_t nseg, double *out,
+                        void *stream);
+
 /* ---- LLG step kernels (cupymag/core/Micromagnetics.py:110-307) ---- */
 typedef struct {
   double K1, elasC1, elasC2, elasC3, lambda100;
