@@ -415,16 +415,16 @@ __global__ void __launch_bounds__(kCGThreads, (NC == 1 && NR == 3) ? 3 : 4) cg_b
 #pragma unroll
           for (int j = 0; j < NS; ++j) w[j] += (double)pqf[j];
           if (needm) {
+            const XPlusD xd{x, d32};
             for (int dof = d0 + threadIdx.x; dof < d1; dof += kCGThreads) {
-              double yx[U], yd[U];
-              apply_c<double, NC, NR>(g, a.c64, x, dof, yx);
-              apply_c<double, NC, NR>(g, a.c64, d32, dof, yd);
+              double yt[U];
+              apply_c<double, NC, NR>(g, a.c64, xd, dof, yt);
 #pragma unroll
               for (int u = 0; u < U; ++u) {
                 const int s = b_sys<NC, NR>(u);
                 if (!((needm >> s) & 1)) continue;
                 const int64_t i = uidx<NC, NR>(n, dof, u);
-                const double t = b[i] - (yx[u] + yd[u]);
+                const double t = b[i] - yt[u];
                 r32[i] = (float)t;
                 w[NS + s] = fma(t, t, w[NS + s]);
                 w[2 * NS + s] = fma(t, (double)p32[i], w[2 * NS + s]);
@@ -472,25 +472,30 @@ __global__ void __launch_bounds__(kCGThreads, (NC == 1 && NR == 3) ? 3 : 4) cg_b
           float rrf[NS];
 #pragma unroll
           for (int j = 0; j < NS; ++j) rrf[j] = 0.0f;
-          for (int dof = d0 + threadIdx.x; dof < d1; dof += kCGThreads) {
+          if (quads) {
+            for (int qd = d0 + 4 * threadIdx.x; qd < d1; qd += 4 * kCGThreads)
+              quad_update<NC, NR, NS>(n, qd, needm, activem, af, x, d32, p32, q32, r32, rrf);
+          } else {
+            for (int dof = d0 + threadIdx.x; dof < d1; dof += kCGThreads) {
 #pragma unroll
-            for (int u = 0; u < U; ++u) {
-              const int s = b_sys<NC, NR>(u);
-              const bool nd = (needm >> s) & 1, ac = (activem >> s) & 1;
-              if (!nd && !ac) continue;
-              const int64_t i = uidx<NC, NR>(n, dof, u);
-              float dd = d32[i];
-              if (nd) {
-                x[i] += (double)dd;
-                dd = 0.0f;
+              for (int u = 0; u < U; ++u) {
+                const int s = b_sys<NC, NR>(u);
+                const bool nd = (needm >> s) & 1, ac = (activem >> s) & 1;
+                if (!nd && !ac) continue;
+                const int64_t i = uidx<NC, NR>(n, dof, u);
+                float dd = d32[i];
+                if (nd) {
+                  x[i] += (double)dd;
+                  dd = 0.0f;
+                }
+                if (ac) {
+                  dd = fmaf(af[s], p32[i], dd);
+                  const float rn = fmaf(-af[s], q32[i], r32[i]);
+                  r32[i] = rn;
+                  rrf[s] = fmaf(rn, rn, rrf[s]);
+                }
+                d32[i] = dd;
               }
-              if (ac) {
-                dd = fmaf(af[s], p32[i], dd);
-                const float rn = fmaf(-af[s], q32[i], r32[i]);
-                r32[i] = rn;
-                rrf[s] = fmaf(rn, rn, rrf[s]);
-              }
-              d32[i] = dd;
             }
           }
 #pragma unroll
@@ -531,14 +536,19 @@ __global__ void __launch_bounds__(kCGThreads, (NC == 1 && NR == 3) ? 3 : 4) cg_b
     // ---- p = r32 + beta p
     for (int cc = l; cc < S.nchunks; cc += S.ncta) {
       const int d1 = min(g.n, (cc + 1) * S.chunk_dofs);
-      for (int dof = cc * S.chunk_dofs + threadIdx.x; dof < d1; dof += kCGThreads)
+      if (quads) {
+        for (int qd = cc * S.chunk_dofs + 4 * threadIdx.x; qd < d1; qd += 4 * kCGThreads)
+          quad_direction<NC, NR, NS>(n, qd, activem, beta, p32, r32);
+      } else {
+        for (int dof = cc * S.chunk_dofs + threadIdx.x; dof < d1; dof += kCGThreads)
 #pragma unroll
-        for (int u = 0; u < U; ++u) {
-          const int s = b_sys<NC, NR>(u);
-          if (!((activem >> s) & 1)) continue;
-          const int64_t i = uidx<NC, NR>(n, dof, u);
-          p32[i] = fmaf(beta[s], p32[i], r32[i]);
-        }
+          for (int u = 0; u < U; ++u) {
+            const int s = b_sys<NC, NR>(u);
+            if (!((activem >> s) & 1)) continue;
+            const int64_t i = uidx<NC, NR>(n, dof, u);
+            p32[i] = fmaf(beta[s], p32[i], r32[i]);
+          }
+      }
     }
   }
   if (lead && threadIdx.x == 0) {
@@ -699,7 +709,7 @@ extern "C" int cpm_batch_plan_build(const cpm_batch_system *sys, int32_t nsys, i
     S.cta0 = cta0;
     S.ncta = A.ncta[s];
     S.chunk_dofs = cd;
-    S.quads = (y.nz & 3) == 0 && ((uintptr_t)y.flags & 3) == 0;
+    S.quads = (y.nz & 3) == 0 && ((uintptr_t)y.flags & 3) == 0 && ((uintptr_t)y.x & 15) == 0;
     const size_t vb = vec_bytes(S.n, ncomp, nrhs, precision);
     char *w = (char *)y.work;
     if (precision == 0) {

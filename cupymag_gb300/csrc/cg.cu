@@ -231,29 +231,36 @@ __global__ void __launch_bounds__(kCGThreads) cg_fp64_kernel(CGArgs<NR, IT> a) {
   }
 }
 
-// ------------------------------------------ FP32 CG with FP64 reliable updates
-// Mixed-precision CG with reliable updates (Sleijpen & van der Vorst, 1996),
-// as in csrc/stencil.cu: FP32 values and vectors (p, q, correction d,
-// recursive residual r32) with FP64 dot accumulation; when the recursive
-// residual has dropped by inner_tol below the last true residual (or below the
-// stopping threshold), x += d in FP64 and r is replaced by b - A64 x computed
-// with the FP64 values (staged tiles).  The search direction survives the
-// update, so the iteration count stays close to plain FP64 CG; convergence is
-// only ever decided on the FP64 residual.
+// ---------------------------------------------------------------------------
+// FP32 CG with FP64 reliable updates on CSR matrices: the algorithm of the
+// stencil solver (csrc/stencil.cu): FP32 values (A->vals32) and FP32 vectors
+// (p, q, the correction d, the recursive residual r) with FP32 per-thread dot
+// partials summed in FP64 across threads; when the recursive residual has
+// fallen by inner_tol (or below the threshold, or at maxiter) the next
+// iteration's first phase also computes the true residual t = b - A64 (x + d)
+// with the FP64 values (staged tiles), t replaces r and rho and decides
+// convergence, the second phase folds d into x, and that iteration's step is
+// the exact line search (t.p) / (p.A p).  Three grid barriers per iteration;
+// the FP32 product uses the same staged tiles and thread groups per row as
+// the FP64 solver.  The CG state lives in shared memory (IRState).
 template <int NR, typename IT>
 __global__ void __launch_bounds__(kCGThreads) cg_ir_kernel(CGArgs<NR, IT> a) {
-  __shared__ double s_red[2 * NR][kCGWarps];
+  __shared__ double s_red[9][kCGWarps];
+  __shared__ IRState st[NR];
+  __shared__ float s_ab[NR];
+  __shared__ int s_mask[3];  // active, need, status
   extern __shared__ __align__(16) unsigned char s_tile[];
   const TileSmem tile = tile_smem(s_tile);
+  const TileSmem32 tile32 = tile_smem32(s_tile);
   const int G = a.group;
   const int R = kCGThreads / G;
   const bool lead = (threadIdx.x % G) == 0;
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int64_t r0 = min(a.n, (int64_t)blockIdx.x * a.rows_per_cta);
   const int64_t r1 = min(a.n, r0 + a.rows_per_cta);
   const bool use_init = a.use_init_dev ? (__ldcg(a.use_init_dev) != 0) : (a.use_init_host != 0);
   const unsigned long long tns = a.timeout_ns;
-  const double delta = a.inner_tol;
+  double *x = a.x;
+  float *r32 = a.r32, *p32 = a.pa32, *q32 = a.q32, *d32 = a.d32;
   int par = 0;
 
   // ---- prologue: r = b - A64 x (or b), r32 = p32 = r, d = 0
@@ -263,16 +270,16 @@ __global__ void __launch_bounds__(kCGThreads) cg_ir_kernel(CGArgs<NR, IT> a) {
   if (use_init) {
     for (int64_t t0 = r0; t0 < r1; t0 += R) {
       double acc[NR];
-      const int64_t row = tile_rows<NR, IT>(a.rp, a.ci, a.av, a.x, t0, min(r1, t0 + R), G, tile, acc);
+      const int64_t row = tile_rows<NR, IT>(a.rp, a.ci, a.av, x, t0, min(r1, t0 + R), G, tile, acc);
       if (row >= 0 && lead) {
 #pragma unroll
         for (int j = 0; j < NR; ++j) {
           const double bj = a.b[row * NR + j];
           const double rj = bj - acc[j];
           const float rf = (float)rj;
-          a.r32[row * NR + j] = rf;
-          a.pa32[row * NR + j] = rf;
-          a.d32[row * NR + j] = 0.0f;
+          r32[row * NR + j] = rf;
+          p32[row * NR + j] = rf;
+          d32[row * NR + j] = 0.0f;
           v[j] = fma(bj, bj, v[j]);
           v[NR + j] = fma(rj, rj, v[NR + j]);
         }
@@ -284,10 +291,10 @@ __global__ void __launch_bounds__(kCGThreads) cg_ir_kernel(CGArgs<NR, IT> a) {
       for (int j = 0; j < NR; ++j) {
         const double bj = a.b[row * NR + j];
         const float rf = (float)bj;
-        a.x[row * NR + j] = 0.0;
-        a.r32[row * NR + j] = rf;
-        a.pa32[row * NR + j] = rf;
-        a.d32[row * NR + j] = 0.0f;
+        x[row * NR + j] = 0.0;
+        r32[row * NR + j] = rf;
+        p32[row * NR + j] = rf;
+        d32[row * NR + j] = 0.0f;
         v[j] = fma(bj, bj, v[j]);
         v[NR + j] = fma(bj, bj, v[NR + j]);
       }
@@ -297,165 +304,149 @@ __global__ void __launch_bounds__(kCGThreads) cg_ir_kernel(CGArgs<NR, IT> a) {
     set_status(a.info, CPM_BARRIER_TIMEOUT);
     return;
   }
-  double atol[NR], resid[NR], rho[NR], rlast[NR];
-  int active[NR], iters[NR];
-  bool any = false;
-#pragma unroll
-  for (int j = 0; j < NR; ++j) {
-    const double bn = sqrt(v[j]);
-    atol[j] = a.tol * bn;
-    rho[j] = v[NR + j];
-    resid[j] = sqrt(v[NR + j]);
-    rlast[j] = resid[j];
-    active[j] = bn != 0.0;
-    iters[j] = 0;
-    any |= active[j] != 0;
-    if (bn == 0.0 && use_init)
-      for (int64_t row = r0 + threadIdx.x; row < r1; row += kCGThreads) a.x[row * NR + j] = a.b[row * NR + j];
-    if (blockIdx.x == 0 && threadIdx.x == 0) a.info->bnorm[j] = bn;
+  if (threadIdx.x == 0) {
+    int am = 0;
+    for (int j = 0; j < NR; ++j) {
+      ir_init(st[j], sqrt(v[j]), v[NR + j], a.tol);
+      am |= st[j].active << j;
+      if (blockIdx.x == 0) a.info->bnorm[j] = sqrt(v[j]);
+    }
+    s_mask[0] = am;
+    s_mask[1] = 0;
+    s_mask[2] = CPM_OK;
+  }
+  __syncthreads();
+  int activem = s_mask[0], needm = 0;
+  if (use_init) {
+    for (int j = 0; j < NR; ++j)
+      if (!((activem >> j) & 1))
+        for (int64_t row = r0 + threadIdx.x; row < r1; row += kCGThreads) x[row * NR + j] = a.b[row * NR + j];
   }
   int status = CPM_OK;
-  int updates = 0;
-  float *p32 = a.pa32;
-  for (int k = 0; any && k < a.maxiter; ++k) {
+  for (int k = 0; activem && k <= a.maxiter; ++k) {
     if (k > 0 && !grid_sync(a.bar, gridDim.x, tns)) { status = CPM_BARRIER_TIMEOUT; break; }
-    // ---- phase 1: q32 = A32 p32 (warp per row, FP32 products, FP64 row sum), partial p.q
-    double pq[NR];
+    // ---- phase 1: q = A32 p (staged FP32 tiles), p.q; pending: t = b - A64 (x + d), r32 = t, t.t, t.p
+    float pqf[NR];
 #pragma unroll
-    for (int j = 0; j < NR; ++j) pq[j] = 0.0;
-    for (int64_t row = r0 + warp; row < r1; row += kCGWarps) {
-      int64_t s, e;
-      row_range(a.rp, row, s, e);
+    for (int j = 0; j < NR; ++j) pqf[j] = 0.0f;
+    for (int64_t t0 = r0; t0 < r1; t0 += R) {
       float acc[NR];
-#pragma unroll
-      for (int j = 0; j < NR; ++j) acc[j] = 0.0f;
-      for (int64_t kk = s + lane; kk < e; kk += kWarp) {
-        const float av = ld_stream(a.av32 + kk);
-        const int64_t cc = ld_stream(a.ci + kk);
-#pragma unroll
-        for (int j = 0; j < NR; ++j) acc[j] = fmaf(av, p32[cc * NR + j], acc[j]);
-      }
-      double accd[NR];
-#pragma unroll
-      for (int j = 0; j < NR; ++j) accd[j] = warp_sum((double)acc[j]);
-      if (lane == 0) {
+      const int64_t row = tile_rows32<NR, IT>(a.rp, a.ci, a.av32, p32, t0, min(r1, t0 + R), G, tile32, acc);
+      if (row >= 0 && lead) {
 #pragma unroll
         for (int j = 0; j < NR; ++j) {
-          const float qf = (float)accd[j];
-          a.q32[row * NR + j] = qf;
-          pq[j] = fma((double)p32[row * NR + j], (double)qf, pq[j]);
+          q32[row * NR + j] = acc[j];
+          pqf[j] = fmaf(p32[row * NR + j], acc[j], pqf[j]);
         }
       }
     }
-    if (!grid_sum<NR>(pq, a.part, par, a.bar, tns, s_red)) { status = CPM_BARRIER_TIMEOUT; break; }
-    double alpha[NR];
-    bool bad = false;
+    double pt[3 * NR];
 #pragma unroll
     for (int j = 0; j < NR; ++j) {
-      alpha[j] = active[j] ? rho[j] / pq[j] : 0.0;
-      if (active[j] && !isfinite(alpha[j])) bad = true;
+      pt[j] = (double)pqf[j];
+      pt[NR + j] = 0.0;
+      pt[2 * NR + j] = 0.0;
     }
-    if (bad) { status = CPM_NONFINITE; break; }
-    // ---- phase 2: d += alpha p, r32 -= alpha q
-    double rr[NR];
-#pragma unroll
-    for (int j = 0; j < NR; ++j) rr[j] = 0.0;
-    for (int64_t row = r0 + threadIdx.x; row < r1; row += kCGThreads) {
-#pragma unroll
-      for (int j = 0; j < NR; ++j) {
-        if (!active[j]) continue;
-        const int64_t i = row * NR + j;
-        const float af = (float)alpha[j];
-        a.d32[i] = fmaf(af, p32[i], a.d32[i]);
-        const float rn = fmaf(-af, a.q32[i], a.r32[i]);
-        a.r32[i] = rn;
-        rr[j] = fma((double)rn, (double)rn, rr[j]);
-      }
-    }
-    if (!grid_sum<NR>(rr, a.part, par, a.bar, tns, s_red)) { status = CPM_BARRIER_TIMEOUT; break; }
-    bool upd = false;
-    int need[NR];
-#pragma unroll
-    for (int j = 0; j < NR; ++j) {
-      need[j] = 0;
-      if (!active[j]) continue;
-      if (!isfinite(rr[j])) bad = true;
-      iters[j] += 1;
-      const double rn = sqrt(rr[j]);
-      need[j] = (rn < delta * rlast[j]) || (rn <= atol[j]) || (k + 1 >= a.maxiter);
-      upd |= need[j] != 0;
-    }
-    if (bad) { status = CPM_NONFINITE; break; }
-    double rnew[NR];
-#pragma unroll
-    for (int j = 0; j < NR; ++j) rnew[j] = rr[j];
-    if (upd) {
-      ++updates;
-      for (int64_t row = r0 + threadIdx.x; row < r1; row += kCGThreads)
-#pragma unroll
-        for (int j = 0; j < NR; ++j) {
-          if (!need[j]) continue;
-          const int64_t i = row * NR + j;
-          a.x[i] += (double)a.d32[i];
-          a.d32[i] = 0.0f;
-        }
-      if (!grid_sync(a.bar, gridDim.x, tns)) { status = CPM_BARRIER_TIMEOUT; break; }
-      double tr[NR];
-#pragma unroll
-      for (int j = 0; j < NR; ++j) tr[j] = 0.0;
+    if (needm) {
+      const XPlusD xd{x, d32};
       for (int64_t t0 = r0; t0 < r1; t0 += R) {
         double acc[NR];
-        const int64_t row = tile_rows<NR, IT>(a.rp, a.ci, a.av, a.x, t0, min(r1, t0 + R), G, tile, acc);
+        const int64_t row = tile_rows<NR, IT>(a.rp, a.ci, a.av, xd, t0, min(r1, t0 + R), G, tile, acc);
         if (row >= 0 && lead) {
 #pragma unroll
           for (int j = 0; j < NR; ++j) {
-            if (!need[j]) continue;
-            const double rj = a.b[row * NR + j] - acc[j];
-            a.r32[row * NR + j] = (float)rj;
-            tr[j] = fma(rj, rj, tr[j]);
+            if (!((needm >> j) & 1)) continue;
+            const double t = a.b[row * NR + j] - acc[j];
+            r32[row * NR + j] = (float)t;
+            pt[NR + j] = fma(t, t, pt[NR + j]);
+            pt[2 * NR + j] = fma(t, (double)p32[row * NR + j], pt[2 * NR + j]);
           }
         }
       }
-      if (!grid_sum<NR>(tr, a.part, par, a.bar, tns, s_red)) { status = CPM_BARRIER_TIMEOUT; break; }
+    }
+    if (!grid_sum<3 * NR>(pt, a.part, par, a.bar, tns, s_red)) { status = CPM_BARRIER_TIMEOUT; break; }
+    if (threadIdx.x == 0) {
+      int am = 0, bad = 0;
+      for (int j = 0; j < NR; ++j) {
+        double al;
+        bad |= ir_after_pq(st[j], pt[j], pt[NR + j], pt[2 * NR + j], a.maxiter, al);
+        s_ab[j] = (float)al;
+        am |= st[j].active << j;
+      }
+      if (needm) st[0].updates += 1;
+      s_mask[0] = am;
+      s_mask[2] = bad ? CPM_NONFINITE : CPM_OK;
+    }
+    __syncthreads();
+    if (s_mask[2] != CPM_OK) { status = s_mask[2]; break; }
+    float af[NR];
+#pragma unroll
+    for (int j = 0; j < NR; ++j) af[j] = s_ab[j];
+    activem = s_mask[0];
+    // ---- phase 2: pending: x += d, d = 0; active: d += alpha p, r32 -= alpha q, r32.r32
+    float rrf[NR];
+#pragma unroll
+    for (int j = 0; j < NR; ++j) rrf[j] = 0.0f;
+    for (int64_t row = r0 + threadIdx.x; row < r1; row += kCGThreads) {
 #pragma unroll
       for (int j = 0; j < NR; ++j) {
-        if (!need[j]) continue;
-        resid[j] = sqrt(tr[j]);
-        rlast[j] = resid[j];
-        rnew[j] = tr[j];
-        if (resid[j] <= atol[j]) active[j] = 0;
+        const bool nd = (needm >> j) & 1, ac = (activem >> j) & 1;
+        if (!nd && !ac) continue;
+        const int64_t i = row * NR + j;
+        float dd = d32[i];
+        if (nd) {
+          x[i] += (double)dd;
+          dd = 0.0f;
+        }
+        if (ac) {
+          dd = fmaf(af[j], p32[i], dd);
+          const float rn = fmaf(-af[j], q32[i], r32[i]);
+          r32[i] = rn;
+          rrf[j] = fmaf(rn, rn, rrf[j]);
+        }
+        d32[i] = dd;
       }
     }
-    any = false;
+    double rr[NR];
+#pragma unroll
+    for (int j = 0; j < NR; ++j) rr[j] = (double)rrf[j];
+    if (!grid_sum<NR>(rr, a.part, par, a.bar, tns, s_red)) { status = CPM_BARRIER_TIMEOUT; break; }
+    if (threadIdx.x == 0) {
+      int nm = 0, bad = 0;
+      for (int j = 0; j < NR; ++j) {
+        float be;
+        bad |= ir_after_rr(st[j], rr[j], a.inner_tol, a.maxiter, be);
+        s_ab[j] = be;
+        nm |= st[j].need << j;
+      }
+      s_mask[1] = nm;
+      s_mask[2] = bad ? CPM_NONFINITE : CPM_OK;
+    }
+    __syncthreads();
+    if (s_mask[2] != CPM_OK) { status = s_mask[2]; break; }
+    needm = s_mask[1];
+    if (!activem) break;
     float beta[NR];
 #pragma unroll
-    for (int j = 0; j < NR; ++j) {
-      beta[j] = 0.0f;
-      if (!active[j]) continue;
-      beta[j] = (float)(rnew[j] / rho[j]);
-      rho[j] = rnew[j];
-      any = true;
-    }
-    if (!any || k + 1 >= a.maxiter) break;
+    for (int j = 0; j < NR; ++j) beta[j] = s_ab[j];
     // ---- phase 3: p = r32 + beta p
     for (int64_t row = r0 + threadIdx.x; row < r1; row += kCGThreads)
 #pragma unroll
       for (int j = 0; j < NR; ++j) {
-        if (!active[j]) continue;
+        if (!((activem >> j) & 1)) continue;
         const int64_t i = row * NR + j;
-        p32[i] = fmaf(beta[j], p32[i], a.r32[i]);
+        p32[i] = fmaf(beta[j], p32[i], r32[i]);
       }
   }
   if (blockIdx.x == 0 && threadIdx.x == 0) {
-    int st = status;
-#pragma unroll
+    int stt = status;
     for (int j = 0; j < NR; ++j) {
-      if (st == CPM_OK && active[j]) st = CPM_NOT_CONVERGED;
-      a.info->iters[j] = iters[j];
-      a.info->resid[j] = resid[j];
+      if (stt == CPM_OK && (st[j].unconv || st[j].active)) stt = CPM_NOT_CONVERGED;
+      a.info->iters[j] = st[j].iters;
+      a.info->resid[j] = st[j].resid;
     }
-    a.info->outer = updates;
-    set_status(a.info, st);
+    a.info->outer = st[0].updates;
+    set_status(a.info, stt);
   } else if (status != CPM_OK && threadIdx.x == 0) {
     set_status(a.info, status);
   }

@@ -58,6 +58,68 @@ __device__ __forceinline__ bool grid_sum(double (&v)[NV], double *part, int &par
   return true;
 }
 
+// ---------------------------------------------------------------- reliable-update CG state
+// State of one system of the FP32 CG with lagged FP64 reliable updates
+// (csrc/cg.cu, csrc/stencil.cu, csrc/batched.cu).  The transitions below are the whole
+// scalar logic of that solver; the kernels call them once per reduction.
+struct IRState {
+  double atol, resid, rho, r0;
+  int active, need, iters, unconv, updates, pad;
+};
+
+__device__ __forceinline__ void ir_init(IRState &s, double bnorm, double rr0, double tol) {
+  s.atol = tol * bnorm;
+  s.rho = rr0;
+  s.resid = sqrt(rr0);
+  s.r0 = s.resid;
+  s.active = bnorm != 0.0;
+  s.need = 0;
+  s.iters = 0;
+  s.unconv = 0;
+  s.updates = 0;
+}
+
+// After the p.q reduction (pq) with, for a pending update, the true residual
+// norm tt = t.t and tp = t.p: decide convergence on t and return alpha
+// (exact line search along p when t replaced the residual).  Returns true on
+// a non-finite value.
+__device__ __forceinline__ bool ir_after_pq(IRState &s, double pq, double tt, double tp, int maxiter, double &alpha) {
+  bool bad = false;
+  alpha = 0.0;
+  if (s.need) {
+    s.resid = sqrt(tt);
+    s.r0 = s.resid;
+    s.rho = tt;
+    if (!isfinite(s.resid)) bad = true;
+    if (s.resid <= s.atol) s.active = 0;
+    else if (s.iters >= maxiter) {
+      s.active = 0;
+      s.unconv = 1;
+    }
+  }
+  if (s.active) {
+    alpha = (s.need ? tp : s.rho) / pq;
+    if (!isfinite(alpha)) bad = true;
+  }
+  return bad;
+}
+
+// After the r.r reduction: count the iteration, schedule a reliable update
+// (residual fell by delta since the last true residual, reached the
+// threshold, or maxiter) and return beta.  Returns true on a non-finite value.
+__device__ __forceinline__ bool ir_after_rr(IRState &s, double rr, double delta, int maxiter, float &beta) {
+  s.need = 0;
+  beta = 0.0f;
+  if (!s.active) return false;
+  const bool bad = !isfinite(rr);
+  s.iters += 1;
+  const double rn = sqrt(rr);
+  s.need = (rn < delta * s.r0) || (rn <= s.atol) || (s.iters >= maxiter);
+  beta = (float)(rr / s.rho);
+  s.rho = rr;
+  return bad;
+}
+
 __device__ __forceinline__ void set_status(cpm_cg_info *info, int st) {
   atomicMax(&info->status, st);
 }

@@ -45,6 +45,62 @@ __device__ __forceinline__ double ld_stream(const double *p) { return __ldcs(p);
 __device__ __forceinline__ float ld_stream(const float *p) { return __ldcs(p); }
 __device__ __forceinline__ int ld_stream(const int *p) { return __ldcs(p); }
 
+// ---------------------------------------------------------------- vector access
+template <typename T>
+struct Vec4;
+template <>
+struct Vec4<float> {
+  static __device__ __forceinline__ void load(const float *p, float *v) {
+    const float4 t = *reinterpret_cast<const float4 *>(p);
+    v[0] = t.x;
+    v[1] = t.y;
+    v[2] = t.z;
+    v[3] = t.w;
+  }
+  static __device__ __forceinline__ void store(float *p, const float *v) {
+    *reinterpret_cast<float4 *>(p) = make_float4(v[0], v[1], v[2], v[3]);
+  }
+};
+template <>
+struct Vec4<double> {
+  static __device__ __forceinline__ void load(const double *p, double *v) {
+    const double2 a = *reinterpret_cast<const double2 *>(p);
+    const double2 b = *reinterpret_cast<const double2 *>(p + 2);
+    v[0] = a.x;
+    v[1] = a.y;
+    v[2] = b.x;
+    v[3] = b.y;
+  }
+  static __device__ __forceinline__ void store(double *p, const double *v) {
+    *reinterpret_cast<double2 *>(p) = make_double2(v[0], v[1]);
+    *reinterpret_cast<double2 *>(p + 2) = make_double2(v[2], v[3]);
+  }
+};
+
+// ---------------------------------------------------------------- operand loaders
+// The products read their operand through ld / ld4: element i (component c:
+// the right-hand side of an interleaved scalar vector, or the displacement
+// component) of a vector of any storage type, converted to T.
+template <typename T, typename TX>
+__device__ __forceinline__ T ld(const TX *x, int64_t i, int) { return (T)x[i]; }
+
+template <typename T, typename TX>
+__device__ __forceinline__ void ld4(const TX *x, int64_t i, int, T *v) {
+  TX t[4];
+  Vec4<TX>::load(x + i, t);
+#pragma unroll
+  for (int e = 0; e < 4; ++e) v[e] = (T)t[e];
+}
+
+// x + d on the fly (FP64 x, FP32 correction d): the operand of the reliable
+// update's true residual b - A64 (x + d), one FP64 product instead of two.
+struct XPlusD {
+  const double *x;
+  const float *d;
+};
+template <typename T>
+__device__ __forceinline__ double ld(const XPlusD &v, int64_t i, int) { return v.x[i] + (double)v.d[i]; }
+
 // ---------------------------------------------------------------- reductions
 // Fixed shuffle pattern: the result is a deterministic function of the inputs.
 __device__ __forceinline__ double warp_sum(double v) {

@@ -72,9 +72,9 @@ __device__ __forceinline__ void stage(const TileSmem &t, const double *av, const
 // row (threadIdx.x / G = local row).  Returns, in every thread, its row (or -1)
 // and the group's complete sum in acc (valid in the group's first lane).
 // NR right-hand sides are interleaved in x ((cols, NR) layout).
-template <int NR, typename IT>
+template <int NR, typename IT, typename XS = const double *>
 __device__ __forceinline__ int64_t tile_rows(const IT *__restrict__ rp, const int *__restrict__ ci,
-                                             const double *__restrict__ av, const double *x, int64_t t0, int64_t t1,
+                                             const double *__restrict__ av, const XS &x, int64_t t0, int64_t t1,
                                              int G, const TileSmem &t, double (&acc)[NR]) {
   const int64_t s = (int64_t)__ldg(rp + t0), e = (int64_t)__ldg(rp + t1);
   const bool staged = (e - s) <= kTileCap;
@@ -94,14 +94,92 @@ __device__ __forceinline__ int64_t tile_rows(const IT *__restrict__ rp, const in
         const double a = vv[k];
         const int64_t c = cc[k];
 #pragma unroll
-        for (int j = 0; j < NR; ++j) acc[j] = fma(a, x[c * NR + j], acc[j]);
+        for (int j = 0; j < NR; ++j) acc[j] = fma(a, ld<double>(x, c * NR + j, j), acc[j]);
       }
     } else {
       for (int64_t k = rs + sub; k < re; k += G) {
         const double a = __ldcs(av + k);
         const int64_t c = __ldcs(ci + k);
 #pragma unroll
-        for (int j = 0; j < NR; ++j) acc[j] = fma(a, x[c * NR + j], acc[j]);
+        for (int j = 0; j < NR; ++j) acc[j] = fma(a, ld<double>(x, c * NR + j, j), acc[j]);
+      }
+    }
+  }
+  for (int o = 1; o < G; o <<= 1) {
+#pragma unroll
+    for (int j = 0; j < NR; ++j) acc[j] += __shfl_xor_sync(0xffffffffu, acc[j], o);
+  }
+  __syncthreads();  // shared tile may be overwritten by the next call
+  return (row < t1) ? row : -1;
+}
+
+// FP32 form for the mixed-precision solver: FP32 values and indices staged in
+// the same 16-byte quads (element s + i lands at v[i + (s & 3)], c[i + (s & 3)]),
+// FP32 products and FP32 group sums.
+struct TileSmem32 {
+  float *v;  // kTileCap + 4 values
+  int *c;    // kTileCap + 4 indices
+};
+
+__device__ __forceinline__ TileSmem32 tile_smem32(unsigned char *base) {
+  TileSmem32 t;
+  t.v = reinterpret_cast<float *>(base);
+  t.c = reinterpret_cast<int *>(base + (size_t)(kTileCap + 4) * 4);
+  return t;
+}
+
+__device__ __forceinline__ void stage32(const TileSmem32 &t, const float *av, const int *ci, int64_t s, int64_t e) {
+  const int oc = (int)(s & 3);
+  const int tid = threadIdx.x;
+  const int64_t qa = (s + 3) & ~int64_t(3), qb = e & ~int64_t(3);
+  for (int64_t g = qa + 4 * (int64_t)tid; g < qb; g += 4 * (int64_t)blockDim.x) {
+    cp16(t.v + (g - s) + oc, av + g);
+    cp16(t.c + (g - s) + oc, ci + g);
+  }
+  const int64_t hend = qa < e ? qa : e;
+  const int64_t tbeg = qb > qa ? qb : qa;
+  if (tid >= 32 && tid < 35 && s + (tid - 32) < hend) {
+    t.v[(tid - 32) + oc] = __ldcs(av + s + (tid - 32));
+    t.c[(tid - 32) + oc] = __ldcs(ci + s + (tid - 32));
+  }
+  if (tid >= 64 && tid < 67 && tbeg + (tid - 64) < e) {
+    t.v[(tbeg + (tid - 64) - s) + oc] = __ldcs(av + tbeg + (tid - 64));
+    t.c[(tbeg + (tid - 64) - s) + oc] = __ldcs(ci + tbeg + (tid - 64));
+  }
+  cp_wait_all();
+  __syncthreads();
+}
+
+template <int NR, typename IT>
+__device__ __forceinline__ int64_t tile_rows32(const IT *__restrict__ rp, const int *__restrict__ ci,
+                                               const float *__restrict__ av, const float *x, int64_t t0, int64_t t1,
+                                               int G, const TileSmem32 &t, float (&acc)[NR]) {
+  const int64_t s = (int64_t)__ldg(rp + t0), e = (int64_t)__ldg(rp + t1);
+  const bool staged = (e - s) <= kTileCap;
+  if (staged) stage32(t, av, ci, s, e);
+  const int lr = threadIdx.x / G, sub = threadIdx.x % G;
+  const int64_t row = t0 + lr;
+#pragma unroll
+  for (int j = 0; j < NR; ++j) acc[j] = 0.0f;
+  if (row < t1) {
+    const int64_t rs = (int64_t)__ldg(rp + row), re = (int64_t)__ldg(rp + row + 1);
+    if (staged) {
+      const int oc = (int)(s & 3);
+      const float *vv = t.v + oc - s;
+      const int *cc = t.c + oc - s;
+#pragma unroll 4
+      for (int64_t k = rs + sub; k < re; k += G) {
+        const float a = vv[k];
+        const int64_t c = cc[k];
+#pragma unroll
+        for (int j = 0; j < NR; ++j) acc[j] = fmaf(a, x[c * NR + j], acc[j]);
+      }
+    } else {
+      for (int64_t k = rs + sub; k < re; k += G) {
+        const float a = __ldcs(av + k);
+        const int64_t c = __ldcs(ci + k);
+#pragma unroll
+        for (int j = 0; j < NR; ++j) acc[j] = fmaf(a, x[c * NR + j], acc[j]);
       }
     }
   }

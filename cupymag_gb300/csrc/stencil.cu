@@ -48,7 +48,7 @@ struct StencilCG {
   cpm_cg_info *info;
   unsigned long long timeout_ns;
   int64_t dofs_per_cta;
-  int quads;  // nz % 4 == 0 and 4-byte aligned flags: the FP32 product runs on quads (apply4_c)
+  int quads;  // nz % 4 == 0, 4-byte aligned flags, 16-byte aligned x: the FP32 phases run on quads
 };
 
 // Number of independent systems (each with its own CG scalars).
@@ -316,16 +316,16 @@ __global__ void __launch_bounds__(kIRThreads, 4) cg_stencil_ir_kernel(const __gr
       pt[2 * NS + j] = 0.0;
     }
     if (needm) {
+      const XPlusD xd{x, d32};
       for (int64_t dof = d0 + threadIdx.x; dof < d1; dof += TH) {
-        double yx[U], yd[U];
-        apply<double, NC, NR>(a.S, x, (int)dof, yx);
-        apply_c<double, NC, NR>(a.S, a.S.c64, d32, (int)dof, yd);
+        double yt[U];
+        apply_c<double, NC, NR>(a.S, a.S.c64, xd, (int)dof, yt);
 #pragma unroll
         for (int u = 0; u < U; ++u) {
           const int s = sys_of<NC, NR>(u);
           if (!((needm >> s) & 1)) continue;
           const int64_t i = uidx<NC, NR>(n, dof, u);
-          const double t = b[i] - (yx[u] + yd[u]);
+          const double t = b[i] - yt[u];
           r32[i] = (float)t;
           pt[NS + s] = fma(t, t, pt[NS + s]);
           pt[2 * NS + s] = fma(t, (double)p32[i], pt[2 * NS + s]);
@@ -355,25 +355,30 @@ __global__ void __launch_bounds__(kIRThreads, 4) cg_stencil_ir_kernel(const __gr
     float rrf[NS];
 #pragma unroll
     for (int j = 0; j < NS; ++j) rrf[j] = 0.0f;
-    for (int64_t dof = d0 + threadIdx.x; dof < d1; dof += TH) {
+    if (quads) {
+      for (int64_t qd = d0 + 4 * threadIdx.x; qd < d1; qd += 4 * TH)
+        quad_update<NC, NR, NS>(n, qd, needm, activem, af, x, d32, p32, q32, r32, rrf);
+    } else {
+      for (int64_t dof = d0 + threadIdx.x; dof < d1; dof += TH) {
 #pragma unroll
-      for (int u = 0; u < U; ++u) {
-        const int s = sys_of<NC, NR>(u);
-        const bool nd = (needm >> s) & 1, ac = (activem >> s) & 1;
-        if (!nd && !ac) continue;
-        const int64_t i = uidx<NC, NR>(n, dof, u);
-        float dd = d32[i];
-        if (nd) {
-          x[i] += (double)dd;
-          dd = 0.0f;
+        for (int u = 0; u < U; ++u) {
+          const int s = sys_of<NC, NR>(u);
+          const bool nd = (needm >> s) & 1, ac = (activem >> s) & 1;
+          if (!nd && !ac) continue;
+          const int64_t i = uidx<NC, NR>(n, dof, u);
+          float dd = d32[i];
+          if (nd) {
+            x[i] += (double)dd;
+            dd = 0.0f;
+          }
+          if (ac) {
+            dd = fmaf(af[s], p32[i], dd);
+            const float rn = fmaf(-af[s], q32[i], r32[i]);
+            r32[i] = rn;
+            rrf[s] = fmaf(rn, rn, rrf[s]);
+          }
+          d32[i] = dd;
         }
-        if (ac) {
-          dd = fmaf(af[s], p32[i], dd);
-          const float rn = fmaf(-af[s], q32[i], r32[i]);
-          r32[i] = rn;
-          rrf[s] = fmaf(rn, rn, rrf[s]);
-        }
-        d32[i] = dd;
       }
     }
     double rr[NS];
@@ -399,13 +404,18 @@ __global__ void __launch_bounds__(kIRThreads, 4) cg_stencil_ir_kernel(const __gr
 #pragma unroll
     for (int j = 0; j < NS; ++j) beta[j] = s_ab[j];
     // ---- phase 3: p = r32 + beta p
-    for (int64_t dof = d0 + threadIdx.x; dof < d1; dof += TH) {
+    if (quads) {
+      for (int64_t qd = d0 + 4 * threadIdx.x; qd < d1; qd += 4 * TH)
+        quad_direction<NC, NR, NS>(n, qd, activem, beta, p32, r32);
+    } else {
+      for (int64_t dof = d0 + threadIdx.x; dof < d1; dof += TH) {
 #pragma unroll
-      for (int u = 0; u < U; ++u) {
-        const int s = sys_of<NC, NR>(u);
-        if (!((activem >> s) & 1)) continue;
-        const int64_t i = uidx<NC, NR>(n, dof, u);
-        p32[i] = fmaf(beta[s], p32[i], r32[i]);
+        for (int u = 0; u < U; ++u) {
+          const int s = sys_of<NC, NR>(u);
+          if (!((activem >> s) & 1)) continue;
+          const int64_t i = uidx<NC, NR>(n, dof, u);
+          p32[i] = fmaf(beta[s], p32[i], r32[i]);
+        }
       }
     }
   }
@@ -525,7 +535,7 @@ static int launch_stencil_cg(const cpm_stencil *s, const double *b, double *x, c
   per = (per + 31) / 32 * 32;
   G = (n + per - 1) / per;
   a.dofs_per_cta = per;
-  a.quads = quads_ok(s) ? 1 : 0;
+  a.quads = quads_ok(s) && ((uintptr_t)x & 15) == 0 ? 1 : 0;
   CPM_TRY(cudaMemsetAsync(w.bar, 0, sizeof(GridBarrier), st));
   CPM_TRY(cudaMemsetAsync(info, 0, sizeof(cpm_cg_info), st));
   void *args[] = {&a};

@@ -53,52 +53,6 @@ __device__ __forceinline__ const double *coefs<double>(const StencilOp &S) { ret
 template <>
 __device__ __forceinline__ const float *coefs<float>(const StencilOp &S) { return S.c32; }
 
-template <typename T>
-struct Vec4;
-template <>
-struct Vec4<float> {
-  static __device__ __forceinline__ void load(const float *p, float *v) {
-    const float4 t = *reinterpret_cast<const float4 *>(p);
-    v[0] = t.x;
-    v[1] = t.y;
-    v[2] = t.z;
-    v[3] = t.w;
-  }
-  static __device__ __forceinline__ void store(float *p, const float *v) {
-    *reinterpret_cast<float4 *>(p) = make_float4(v[0], v[1], v[2], v[3]);
-  }
-};
-template <>
-struct Vec4<double> {
-  static __device__ __forceinline__ void load(const double *p, double *v) {
-    const double2 a = *reinterpret_cast<const double2 *>(p);
-    const double2 b = *reinterpret_cast<const double2 *>(p + 2);
-    v[0] = a.x;
-    v[1] = a.y;
-    v[2] = b.x;
-    v[3] = b.y;
-  }
-  static __device__ __forceinline__ void store(double *p, const double *v) {
-    *reinterpret_cast<double2 *>(p) = make_double2(v[0], v[1]);
-    *reinterpret_cast<double2 *>(p + 2) = make_double2(v[2], v[3]);
-  }
-};
-
-// ---------------------------------------------------------------- operand loaders
-// The products read their operand through ld / ld4: element i (component c:
-// the right-hand side of an interleaved scalar vector, or the displacement
-// component) of a vector of any storage type, converted to T.
-template <typename T, typename TX>
-__device__ __forceinline__ T ld(const TX *x, int64_t i, int) { return (T)x[i]; }
-
-template <typename T, typename TX>
-__device__ __forceinline__ void ld4(const TX *x, int64_t i, int, T *v) {
-  TX t[4];
-  Vec4<TX>::load(x + i, t);
-#pragma unroll
-  for (int e = 0; e < 4; ++e) v[e] = (T)t[e];
-}
-
 // y = A x at one DOF for a scalar operator (nc = 1), NR interleaved vectors.
 // CHECK selects the path that tests every neighbour's column flag.
 template <typename T, int NR, bool CHECK, typename Geo, typename XS>
@@ -344,66 +298,84 @@ __device__ __forceinline__ void quad_dot(const float *v, int64_t n, int64_t d0, 
   }
 }
 
-// ---------------------------------------------------------------- reliable-update CG state
-// State of one system of the FP32 CG with lagged FP64 reliable updates
-// (csrc/stencil.cu, csrc/batched.cu).  The transitions below are the whole
-// scalar logic of that solver; the kernels call them once per reduction.
-struct IRState {
-  double atol, resid, rho, r0;
-  int active, need, iters, unconv, updates, pad;
-};
-
-__device__ __forceinline__ void ir_init(IRState &s, double bnorm, double rr0, double tol) {
-  s.atol = tol * bnorm;
-  s.rho = rr0;
-  s.resid = sqrt(rr0);
-  s.r0 = s.resid;
-  s.active = bnorm != 0.0;
-  s.need = 0;
-  s.iters = 0;
-  s.unconv = 0;
-  s.updates = 0;
+// ---------------------------------------------------------------- vectorised update phases on quads
+// The unknowns of quad d0..d0+3 in aligned groups of 4: group h starts at
+// (NC == 3: h * n + d0; else d0 * NR + 4 h) and element e belongs to system
+// (NC == 1 && NR == 3 ? (4h + e) % 3 : 0).
+template <int NC, int NR>
+__device__ __forceinline__ int64_t quad_base(int64_t n, int64_t d0, int h) {
+  return NC == 3 ? h * n + d0 : d0 * NR + 4 * h;
+}
+template <int NC, int NR>
+__device__ __forceinline__ int quad_sys(int h, int e) {
+  return (NC == 1 && NR == 3) ? (4 * h + e) % 3 : 0;
 }
 
-// After the p.q reduction (pq) with, for a pending update, the true residual
-// norm tt = t.t and tp = t.p: decide convergence on t and return alpha
-// (exact line search along p when t replaced the residual).  Returns true on
-// a non-finite value.
-__device__ __forceinline__ bool ir_after_pq(IRState &s, double pq, double tt, double tp, int maxiter, double &alpha) {
-  bool bad = false;
-  alpha = 0.0;
-  if (s.need) {
-    s.resid = sqrt(tt);
-    s.r0 = s.resid;
-    s.rho = tt;
-    if (!isfinite(s.resid)) bad = true;
-    if (s.resid <= s.atol) s.active = 0;
-    else if (s.iters >= maxiter) {
-      s.active = 0;
-      s.unconv = 1;
+// Pending reliable updates: x += d, d = 0; active systems: d += alpha p,
+// r -= alpha q, rr += r^2 (FP32 per thread).
+template <int NC, int NR, int NS>
+__device__ __forceinline__ void quad_update(int64_t n, int64_t d0, int needm, int activem, const float (&af)[NS],
+                                            double *x, float *d32, const float *p32, const float *q32, float *r32,
+                                            float (&rrf)[NS]) {
+  constexpr int H = NC == 3 ? 3 : NR;
+#pragma unroll
+  for (int h = 0; h < H; ++h) {
+    const int64_t i0 = quad_base<NC, NR>(n, d0, h);
+    float dd[4], pp[4], qq[4], rr[4];
+    Vec4<float>::load(d32 + i0, dd);
+    bool fold = false, upd = false;
+#pragma unroll
+    for (int e = 0; e < 4; ++e) {
+      fold |= (needm >> quad_sys<NC, NR>(h, e)) & 1;
+      upd |= (activem >> quad_sys<NC, NR>(h, e)) & 1;
     }
+    if (fold) {
+      double xv[4];
+      Vec4<double>::load(x + i0, xv);
+#pragma unroll
+      for (int e = 0; e < 4; ++e)
+        if ((needm >> quad_sys<NC, NR>(h, e)) & 1) {
+          xv[e] += (double)dd[e];
+          dd[e] = 0.0f;
+        }
+      Vec4<double>::store(x + i0, xv);
+    }
+    if (upd) {
+      Vec4<float>::load(p32 + i0, pp);
+      Vec4<float>::load(q32 + i0, qq);
+      Vec4<float>::load(r32 + i0, rr);
+#pragma unroll
+      for (int e = 0; e < 4; ++e) {
+        const int s = quad_sys<NC, NR>(h, e);
+        if (!((activem >> s) & 1)) continue;
+        dd[e] = fmaf(af[s], pp[e], dd[e]);
+        rr[e] = fmaf(-af[s], qq[e], rr[e]);
+        rrf[s] = fmaf(rr[e], rr[e], rrf[s]);
+      }
+      Vec4<float>::store(r32 + i0, rr);
+    }
+    if (fold || upd) Vec4<float>::store(d32 + i0, dd);
   }
-  if (s.active) {
-    alpha = (s.need ? tp : s.rho) / pq;
-    if (!isfinite(alpha)) bad = true;
-  }
-  return bad;
 }
 
-// After the r.r reduction: count the iteration, schedule a reliable update
-// (residual fell by delta since the last true residual, reached the
-// threshold, or maxiter) and return beta.  Returns true on a non-finite value.
-__device__ __forceinline__ bool ir_after_rr(IRState &s, double rr, double delta, int maxiter, float &beta) {
-  s.need = 0;
-  beta = 0.0f;
-  if (!s.active) return false;
-  const bool bad = !isfinite(rr);
-  s.iters += 1;
-  const double rn = sqrt(rr);
-  s.need = (rn < delta * s.r0) || (rn <= s.atol) || (s.iters >= maxiter);
-  beta = (float)(rr / s.rho);
-  s.rho = rr;
-  return bad;
+// p = r + beta p for the active systems.
+template <int NC, int NR, int NS>
+__device__ __forceinline__ void quad_direction(int64_t n, int64_t d0, int activem, const float (&beta)[NS],
+                                               float *p32, const float *r32) {
+  constexpr int H = NC == 3 ? 3 : NR;
+#pragma unroll
+  for (int h = 0; h < H; ++h) {
+    const int64_t i0 = quad_base<NC, NR>(n, d0, h);
+    float pp[4], rr[4];
+    Vec4<float>::load(p32 + i0, pp);
+    Vec4<float>::load(r32 + i0, rr);
+#pragma unroll
+    for (int e = 0; e < 4; ++e) {
+      const int s = quad_sys<NC, NR>(h, e);
+      if ((activem >> s) & 1) pp[e] = fmaf(beta[s], pp[e], rr[e]);
+    }
+    Vec4<float>::store(p32 + i0, pp);
+  }
 }
 
 // y at one DOF with the operator's own (launch-parameter) coefficients.
