@@ -106,6 +106,36 @@ class ClockSampler:
                 "reasons": reasons, "samples": len(rows)}
 
 
+def max_over_ranks(x: float) -> float:
+    """The maximum of x over the process group (x itself without one); NCCL on GPUs, gloo on the host."""
+    import torch
+    import torch.distributed as dist
+    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size() == 1:
+        return float(x)
+    dev = torch.device("cuda", torch.cuda.current_device()) if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([float(x)], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def sum_over_ranks(x: float) -> float:
+    import torch
+    import torch.distributed as dist
+    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size() == 1:
+        return float(x)
+    dev = torch.device("cuda", torch.cuda.current_device()) if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([float(x)], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.SUM)
+    return float(t.item())
+
+
+def replica_throughput(steps_per_rank: int, seconds: float) -> float:
+    """Whole-job steps/s of independent replicas: all ranks' steps over the slowest rank's time."""
+    import torch.distributed as dist
+    world = dist.get_world_size() if dist.is_available() and dist.is_initialized() else 1
+    return world * steps_per_rank / max_over_ranks(seconds)
+
+
 def dist_env():
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -220,8 +250,13 @@ def serving_sample(args):
     steps, extrapolated to the full sweep with its own setup time)."""
     import numpy as np
     from cupymag_gb300.serving import ServingEngine, run_sequential, serving_requests
-    reqs = serving_requests()[:args.serve_requests]
+    import torch.distributed as dist
+    from cupymag_gb300.serving.router import combine_stats, shard_requests
+    world = dist.get_world_size() if dist.is_available() and dist.is_initialized() else 1
+    rank = dist.get_rank() if world > 1 else 0
+    reqs = shard_requests(serving_requests()[:args.serve_requests], world, rank)
     res, st = ServingEngine("IR", hbm_budget_gb=args.hbm_budget_gb).serve(reqs, realtime=True)
+    agg = combine_stats(st, [r.latency for r in res.values() if r.error is None]) if world > 1 else None
     seq, _ = run_sequential(reqs, precision="DP", max_steps=args.seq_steps)
     t_seq, steps, errs = 0.0, 0, []
     for r in reqs:
@@ -233,8 +268,15 @@ def serving_sample(args):
         if len(a) == len(b) and len(b):
             errs.append(float(np.abs(a - b).max() / np.abs(b).max()))
     seq_sps = steps / t_seq if t_seq > 0 else None
+    if world > 1:
+        # sequential baseline of the whole job: every rank's requests one after another on its own GPU
+        seq_sps = sum_over_ranks(steps) / max_over_ranks(t_seq) if t_seq > 0 else None
+        st.makespan_s, st.steps = agg["makespan_s"], agg["steps"]
+        st.latency_p50_s, st.latency_p99_s, st.failed = agg["latency_p50_s"], agg["latency_p99_s"], agg["failed"]
     edges = [r.edge for r in reqs]
-    return {"requests": len(reqs), "arrivals": "Poisson 20/s", "edges": f"{min(edges)}..{max(edges)}",
+    return {"requests": len(reqs) if world == 1 else agg["requests"], "ranks": world,
+            "sharding": "whole requests, greedy least-loaded by estimated work, no data-path collective",
+            "arrivals": "Poisson 20/s", "edges": f"{min(edges)}..{max(edges)}",
             "magnetoelastic": sum(r.ME for r in reqs), "steps_per_request": reqs[0].steps,
             "precision": "f32+f64", "makespan_s": round(st.makespan_s, 3), "steps_per_s": round(st.steps_per_s, 2),
             "latency_p50_s": round(st.latency_p50_s, 3), "latency_p99_s": round(st.latency_p99_s, 3),
@@ -319,11 +361,8 @@ def run_ours(args):
     m_timed, avg_timed = L.m.clone(), L.avg_m.clone()
     ms = t0.elapsed_time(t1)
     # max over ranks
-    t_tensor = torch.tensor([ms], device="cuda")
-    if world > 1:
-        dist.all_reduce(t_tensor, op=dist.ReduceOp.MAX)
-    ms_max = float(t_tensor.item())
-    value = world * args.steps / (ms_max / 1e3)
+    ms_max = 1e3 * max_over_ranks(ms / 1e3)
+    value = replica_throughput(args.steps, ms / 1e3)
 
     # roofline of the CG kernel
     from cupymag_gb300.solvers.linear_solvers import decode_info
@@ -385,10 +424,7 @@ def run_ours(args):
         torch.cuda.current_stream().synchronize()
     e2e_s = time.perf_counter() - tw
     L.check()
-    e2e_t = torch.tensor([e2e_s], device="cuda")
-    if world > 1:
-        dist.all_reduce(e2e_t, op=dist.ReduceOp.MAX)
-    e2e_value = world * args.steps / float(e2e_t.item())
+    e2e_value = replica_throughput(args.steps, e2e_s)
 
     fp64 = None
     if args.precision != "DP" and not args.no_fp64_check:
@@ -404,13 +440,14 @@ def run_ours(args):
 
     op_gb = sum(x.nbytes() for x in [L.A_demag, L.A1, L.A2, L.F1, L.Fx, L.F_el] + ([L.A_el] if L.ME else [])
                 if hasattr(x, "nbytes")) / 1e9
+    serving = None
+    if args.serve_requests > 0 and S.structured:
+        # every rank serves its share of the request stream (no data-path collective)
+        del L
+        torch.cuda.empty_cache()
+        serving = serving_sample(args)
     line = None
     if rank == 0:
-        serving = None
-        if world == 1 and args.serve_requests > 0:
-            del L
-            torch.cuda.empty_cache()
-            serving = serving_sample(args)
         cpu = None
         if world == 1 and not args.no_cpu_baseline:
             try:
