@@ -20,9 +20,9 @@
 // FP32 CG with FP64 reliable updates in a form that needs no extra barrier:
 // when the FP32 recursive residual has fallen by inner_tol (or below the
 // stopping threshold, or at maxiter), the next iteration's first phase also
-// computes the true residual t = b - A64 (x + d) in FP64 beside q = A32 p;
-// t replaces the FP32 residual and rho, decides convergence, and the second
-// phase folds d into x.  The direction p of that iteration was formed from
+// computes the true residual t = b - A64 x in FP64 beside q = A32 p (the
+// direction phase before it folded d into x); t replaces the FP32 residual
+// and rho and decides convergence.  The direction p of that iteration was formed from
 // the recursive residual, so its step length is the exact line search
 // alpha = (t.p) / (p.A p) rather than (t.t) / (p.A p).  The stopping test is
 // only ever decided on the FP64 true residual.
@@ -387,7 +387,7 @@ __global__ void __launch_bounds__(kCGThreads, (NC == 1 && NR == 3) ? 3 : 4) cg_b
       if (__ldcg(a.live) == 0) break;
     }
     const bool busy = activem != 0;  // pending updates belong to active systems
-    // ---- q = A32 p, p.q (FP32 per thread); pending updates: t = b - A64 (x + d), r32 = t, t.t, t.p
+    // ---- q = A32 p, p.q (FP32 per thread); pending updates: t = b - A64 x, r32 = t, t.t, t.p
     double pt[3 * NS];
     if (!seg_reduce<3 * NS>(a, S, l, busy, par, s_red, pt, [&](int d0, int d1, double (&w)[3 * NS]) {
           float pqf[NS];
@@ -415,10 +415,10 @@ __global__ void __launch_bounds__(kCGThreads, (NC == 1 && NR == 3) ? 3 : 4) cg_b
 #pragma unroll
           for (int j = 0; j < NS; ++j) w[j] += (double)pqf[j];
           if (needm) {
-            const XPlusD xd{x, d32};
+            // d was folded into x by the previous direction phase
             for (int dof = d0 + threadIdx.x; dof < d1; dof += kCGThreads) {
               double yt[U];
-              apply_c<double, NC, NR>(g, a.c64, xd, dof, yt);
+              apply_c<double, NC, NR>(g, a.c64, x, dof, yt);
 #pragma unroll
               for (int u = 0; u < U; ++u) {
                 const int s = b_sys<NC, NR>(u);
@@ -465,36 +465,26 @@ __global__ void __launch_bounds__(kCGThreads, (NC == 1 && NR == 3) ? 3 : 4) cg_b
 #pragma unroll
       for (int j = 0; j < NS; ++j) af[j] = s_ab[j];
     }
-    // ---- pending: x += d, d = 0; active: d += alpha p, r32 -= alpha q, r32.r32
-    const bool fold = (needm | activem) != 0;
+    // ---- active: d += alpha p, r32 -= alpha q, r32.r32
     double rr[NS];
-    if (!seg_reduce<NS>(a, S, l, fold, par, s_red, rr, [&](int d0, int d1, double (&w)[NS]) {
+    if (!seg_reduce<NS>(a, S, l, activem != 0, par, s_red, rr, [&](int d0, int d1, double (&w)[NS]) {
           float rrf[NS];
 #pragma unroll
           for (int j = 0; j < NS; ++j) rrf[j] = 0.0f;
           if (quads) {
             for (int qd = d0 + 4 * threadIdx.x; qd < d1; qd += 4 * kCGThreads)
-              quad_update<NC, NR, NS>(n, qd, needm, activem, af, x, d32, p32, q32, r32, rrf);
+              quad_update<NC, NR, NS>(n, qd, activem, af, d32, p32, q32, r32, rrf);
           } else {
             for (int dof = d0 + threadIdx.x; dof < d1; dof += kCGThreads) {
 #pragma unroll
               for (int u = 0; u < U; ++u) {
                 const int s = b_sys<NC, NR>(u);
-                const bool nd = (needm >> s) & 1, ac = (activem >> s) & 1;
-                if (!nd && !ac) continue;
+                if (!((activem >> s) & 1)) continue;
                 const int64_t i = uidx<NC, NR>(n, dof, u);
-                float dd = d32[i];
-                if (nd) {
-                  x[i] += (double)dd;
-                  dd = 0.0f;
-                }
-                if (ac) {
-                  dd = fmaf(af[s], p32[i], dd);
-                  const float rn = fmaf(-af[s], q32[i], r32[i]);
-                  r32[i] = rn;
-                  rrf[s] = fmaf(rn, rn, rrf[s]);
-                }
-                d32[i] = dd;
+                d32[i] = fmaf(af[s], p32[i], d32[i]);
+                const float rn = fmaf(-af[s], q32[i], r32[i]);
+                r32[i] = rn;
+                rrf[s] = fmaf(rn, rn, rrf[s]);
               }
             }
           }
@@ -533,20 +523,23 @@ __global__ void __launch_bounds__(kCGThreads, (NC == 1 && NR == 3) ? 3 : 4) cg_b
     float beta[NS];
 #pragma unroll
     for (int j = 0; j < NS; ++j) beta[j] = s_ab[j];
-    // ---- p = r32 + beta p
+    // ---- p = r32 + beta p; pending updates: x += d, d = 0
     for (int cc = l; cc < S.nchunks; cc += S.ncta) {
       const int d1 = min(g.n, (cc + 1) * S.chunk_dofs);
       if (quads) {
         for (int qd = cc * S.chunk_dofs + 4 * threadIdx.x; qd < d1; qd += 4 * kCGThreads)
-          quad_direction<NC, NR, NS>(n, qd, activem, beta, p32, r32);
+          quad_direction<NC, NR, NS>(n, qd, activem, needm, beta, p32, r32, x, d32);
       } else {
         for (int dof = cc * S.chunk_dofs + threadIdx.x; dof < d1; dof += kCGThreads)
 #pragma unroll
           for (int u = 0; u < U; ++u) {
             const int s = b_sys<NC, NR>(u);
-            if (!((activem >> s) & 1)) continue;
             const int64_t i = uidx<NC, NR>(n, dof, u);
-            p32[i] = fmaf(beta[s], p32[i], r32[i]);
+            if ((activem >> s) & 1) p32[i] = fmaf(beta[s], p32[i], r32[i]);
+            if ((needm >> s) & 1) {
+              x[i] += (double)d32[i];
+              d32[i] = 0.0f;
+            }
           }
       }
     }

@@ -237,10 +237,10 @@ __global__ void __launch_bounds__(kCGThreads) cg_fp64_kernel(CGArgs<NR, IT> a) {
 // (p, q, the correction d, the recursive residual r) with FP32 per-thread dot
 // partials summed in FP64 across threads; when the recursive residual has
 // fallen by inner_tol (or below the threshold, or at maxiter) the next
-// iteration's first phase also computes the true residual t = b - A64 (x + d)
-// with the FP64 values (staged tiles), t replaces r and rho and decides
-// convergence, the second phase folds d into x, and that iteration's step is
-// the exact line search (t.p) / (p.A p).  Three grid barriers per iteration;
+// iteration's first phase also computes the true residual t = b - A64 x with
+// the FP64 values (staged tiles; the direction phase before it folded d into
+// x), t replaces r and rho and decides convergence, and that iteration's step
+// is the exact line search (t.p) / (p.A p).  Three grid barriers per iteration;
 // the FP32 product uses the same staged tiles and thread groups per row as
 // the FP64 solver.  The CG state lives in shared memory (IRState).
 template <int NR, typename IT>
@@ -325,7 +325,7 @@ __global__ void __launch_bounds__(kCGThreads) cg_ir_kernel(CGArgs<NR, IT> a) {
   int status = CPM_OK;
   for (int k = 0; activem && k <= a.maxiter; ++k) {
     if (k > 0 && !grid_sync(a.bar, gridDim.x, tns)) { status = CPM_BARRIER_TIMEOUT; break; }
-    // ---- phase 1: q = A32 p (staged FP32 tiles), p.q; pending: t = b - A64 (x + d), r32 = t, t.t, t.p
+    // ---- phase 1: q = A32 p (staged FP32 tiles), p.q; pending: t = b - A64 x, r32 = t, t.t, t.p
     float pqf[NR];
 #pragma unroll
     for (int j = 0; j < NR; ++j) pqf[j] = 0.0f;
@@ -348,10 +348,10 @@ __global__ void __launch_bounds__(kCGThreads) cg_ir_kernel(CGArgs<NR, IT> a) {
       pt[2 * NR + j] = 0.0;
     }
     if (needm) {
-      const XPlusD xd{x, d32};
+      // d was folded into x by the previous direction phase
       for (int64_t t0 = r0; t0 < r1; t0 += R) {
         double acc[NR];
-        const int64_t row = tile_rows<NR, IT>(a.rp, a.ci, a.av, xd, t0, min(r1, t0 + R), G, tile, acc);
+        const int64_t row = tile_rows<NR, IT>(a.rp, a.ci, a.av, x, t0, min(r1, t0 + R), G, tile, acc);
         if (row >= 0 && lead) {
 #pragma unroll
           for (int j = 0; j < NR; ++j) {
@@ -383,28 +383,19 @@ __global__ void __launch_bounds__(kCGThreads) cg_ir_kernel(CGArgs<NR, IT> a) {
 #pragma unroll
     for (int j = 0; j < NR; ++j) af[j] = s_ab[j];
     activem = s_mask[0];
-    // ---- phase 2: pending: x += d, d = 0; active: d += alpha p, r32 -= alpha q, r32.r32
+    // ---- phase 2: active: d += alpha p, r32 -= alpha q, r32.r32
     float rrf[NR];
 #pragma unroll
     for (int j = 0; j < NR; ++j) rrf[j] = 0.0f;
     for (int64_t row = r0 + threadIdx.x; row < r1; row += kCGThreads) {
 #pragma unroll
       for (int j = 0; j < NR; ++j) {
-        const bool nd = (needm >> j) & 1, ac = (activem >> j) & 1;
-        if (!nd && !ac) continue;
+        if (!((activem >> j) & 1)) continue;
         const int64_t i = row * NR + j;
-        float dd = d32[i];
-        if (nd) {
-          x[i] += (double)dd;
-          dd = 0.0f;
-        }
-        if (ac) {
-          dd = fmaf(af[j], p32[i], dd);
-          const float rn = fmaf(-af[j], q32[i], r32[i]);
-          r32[i] = rn;
-          rrf[j] = fmaf(rn, rn, rrf[j]);
-        }
-        d32[i] = dd;
+        d32[i] = fmaf(af[j], p32[i], d32[i]);
+        const float rn = fmaf(-af[j], q32[i], r32[i]);
+        r32[i] = rn;
+        rrf[j] = fmaf(rn, rn, rrf[j]);
       }
     }
     double rr[NR];
@@ -429,13 +420,16 @@ __global__ void __launch_bounds__(kCGThreads) cg_ir_kernel(CGArgs<NR, IT> a) {
     float beta[NR];
 #pragma unroll
     for (int j = 0; j < NR; ++j) beta[j] = s_ab[j];
-    // ---- phase 3: p = r32 + beta p
+    // ---- phase 3: p = r32 + beta p; pending updates: x += d, d = 0
     for (int64_t row = r0 + threadIdx.x; row < r1; row += kCGThreads)
 #pragma unroll
       for (int j = 0; j < NR; ++j) {
-        if (!((activem >> j) & 1)) continue;
         const int64_t i = row * NR + j;
-        p32[i] = fmaf(beta[j], p32[i], r32[i]);
+        if ((activem >> j) & 1) p32[i] = fmaf(beta[j], p32[i], r32[i]);
+        if ((needm >> j) & 1) {
+          x[i] += (double)d32[i];
+          d32[i] = 0.0f;
+        }
       }
   }
   if (blockIdx.x == 0 && threadIdx.x == 0) {

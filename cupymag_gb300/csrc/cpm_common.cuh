@@ -92,15 +92,6 @@ __device__ __forceinline__ void ld4(const TX *x, int64_t i, int, T *v) {
   for (int e = 0; e < 4; ++e) v[e] = (T)t[e];
 }
 
-// x + d on the fly (FP64 x, FP32 correction d): the operand of the reliable
-// update's true residual b - A64 (x + d), one FP64 product instead of two.
-struct XPlusD {
-  const double *x;
-  const float *d;
-};
-template <typename T>
-__device__ __forceinline__ double ld(const XPlusD &v, int64_t i, int) { return v.x[i] + (double)v.d[i]; }
-
 // ---------------------------------------------------------------- reductions
 // Fixed shuffle pattern: the result is a deterministic function of the inputs.
 __device__ __forceinline__ double warp_sum(double v) {

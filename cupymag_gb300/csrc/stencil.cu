@@ -25,6 +25,7 @@
 // coefficients and FP64 dot accumulation.  GB300 issues FP32 FMAs at many
 // times its FP64 rate, so the FP32 iterations are bound by vector traffic.
 #include <algorithm>
+#include <cstdlib>
 #include <cmath>
 
 #include "stencil_ops.cuh"
@@ -202,10 +203,10 @@ __global__ void __launch_bounds__(kCGThreads) cg_stencil_fp64_kernel(const __gri
 // accumulation across threads.  When the recursive residual has fallen by a
 // factor delta (inner_tol) below the last true residual -- or below the
 // stopping threshold, or at maxiter -- the next iteration's first phase also
-// computes the true residual t = b - A64 (x + d) with the FP64 coefficients
-// and the FP64 x: t replaces r and rho, decides convergence (the stopping
-// test ||b - A x|| <= tol ||b|| is only ever decided on t), and the second
-// phase folds d into x (FP64).  That iteration's direction p was formed from
+// computes the true residual t = b - A64 x with the FP64 coefficients and the
+// FP64 x (the direction phase before it folded d into x, own unknowns only):
+// t replaces r and rho and decides convergence (the stopping test
+// ||b - A x|| <= tol ||b|| is only ever decided on t).  That iteration's direction p was formed from
 // the recursive residual, so its step length is the exact line search
 // alpha = (t.p) / (p.A p).  The update costs no extra grid barrier.
 // info->outer counts the reliable updates.  With nz % 4 == 0 the FP32
@@ -285,7 +286,7 @@ __global__ void __launch_bounds__(kIRThreads, 4) cg_stencil_ir_kernel(const __gr
   int status = CPM_OK;
   for (int k = 0; activem && k <= a.maxiter; ++k) {
     if (k > 0 && !grid_sync(a.bar, gridDim.x, tns)) { status = CPM_BARRIER_TIMEOUT; break; }
-    // ---- phase 1: q = A32 p, p.q (FP32 per thread); pending: t = b - A64 (x + d), r32 = t, t.t, t.p
+    // ---- phase 1: q = A32 p, p.q (FP32 per thread); pending: t = b - A64 x, r32 = t, t.t, t.p
     float pqf[NS];
 #pragma unroll
     for (int j = 0; j < NS; ++j) pqf[j] = 0.0f;
@@ -316,10 +317,10 @@ __global__ void __launch_bounds__(kIRThreads, 4) cg_stencil_ir_kernel(const __gr
       pt[2 * NS + j] = 0.0;
     }
     if (needm) {
-      const XPlusD xd{x, d32};
+      // d was folded into x by the previous direction phase
       for (int64_t dof = d0 + threadIdx.x; dof < d1; dof += TH) {
         double yt[U];
-        apply_c<double, NC, NR>(a.S, a.S.c64, xd, (int)dof, yt);
+        apply<double, NC, NR>(a.S, x, (int)dof, yt);
 #pragma unroll
         for (int u = 0; u < U; ++u) {
           const int s = sys_of<NC, NR>(u);
@@ -351,33 +352,24 @@ __global__ void __launch_bounds__(kIRThreads, 4) cg_stencil_ir_kernel(const __gr
 #pragma unroll
     for (int j = 0; j < NS; ++j) af[j] = s_ab[j];
     activem = s_mask[0];
-    // ---- phase 2: pending: x += d, d = 0; active: d += alpha p, r32 -= alpha q, r32.r32
+    // ---- phase 2: active: d += alpha p, r32 -= alpha q, r32.r32
     float rrf[NS];
 #pragma unroll
     for (int j = 0; j < NS; ++j) rrf[j] = 0.0f;
     if (quads) {
       for (int64_t qd = d0 + 4 * threadIdx.x; qd < d1; qd += 4 * TH)
-        quad_update<NC, NR, NS>(n, qd, needm, activem, af, x, d32, p32, q32, r32, rrf);
+        quad_update<NC, NR, NS>(n, qd, activem, af, d32, p32, q32, r32, rrf);
     } else {
       for (int64_t dof = d0 + threadIdx.x; dof < d1; dof += TH) {
 #pragma unroll
         for (int u = 0; u < U; ++u) {
           const int s = sys_of<NC, NR>(u);
-          const bool nd = (needm >> s) & 1, ac = (activem >> s) & 1;
-          if (!nd && !ac) continue;
+          if (!((activem >> s) & 1)) continue;
           const int64_t i = uidx<NC, NR>(n, dof, u);
-          float dd = d32[i];
-          if (nd) {
-            x[i] += (double)dd;
-            dd = 0.0f;
-          }
-          if (ac) {
-            dd = fmaf(af[s], p32[i], dd);
-            const float rn = fmaf(-af[s], q32[i], r32[i]);
-            r32[i] = rn;
-            rrf[s] = fmaf(rn, rn, rrf[s]);
-          }
-          d32[i] = dd;
+          d32[i] = fmaf(af[s], p32[i], d32[i]);
+          const float rn = fmaf(-af[s], q32[i], r32[i]);
+          r32[i] = rn;
+          rrf[s] = fmaf(rn, rn, rrf[s]);
         }
       }
     }
@@ -403,18 +395,21 @@ __global__ void __launch_bounds__(kIRThreads, 4) cg_stencil_ir_kernel(const __gr
     float beta[NS];
 #pragma unroll
     for (int j = 0; j < NS; ++j) beta[j] = s_ab[j];
-    // ---- phase 3: p = r32 + beta p
+    // ---- phase 3: p = r32 + beta p; pending updates: x += d, d = 0
     if (quads) {
       for (int64_t qd = d0 + 4 * threadIdx.x; qd < d1; qd += 4 * TH)
-        quad_direction<NC, NR, NS>(n, qd, activem, beta, p32, r32);
+        quad_direction<NC, NR, NS>(n, qd, activem, needm, beta, p32, r32, x, d32);
     } else {
       for (int64_t dof = d0 + threadIdx.x; dof < d1; dof += TH) {
 #pragma unroll
         for (int u = 0; u < U; ++u) {
           const int s = sys_of<NC, NR>(u);
-          if (!((activem >> s) & 1)) continue;
           const int64_t i = uidx<NC, NR>(n, dof, u);
-          p32[i] = fmaf(beta[s], p32[i], r32[i]);
+          if ((activem >> s) & 1) p32[i] = fmaf(beta[s], p32[i], r32[i]);
+          if ((needm >> s) & 1) {
+            x[i] += (double)d32[i];
+            d32[i] = 0.0f;
+          }
         }
       }
     }
@@ -527,6 +522,14 @@ static int launch_stencil_cg(const cpm_stencil *s, const double *b, double *x, c
   }
   const int64_t n = a.S.n;
   int64_t gmax = (int64_t)occ * sm_count();
+  if (!fp64) {
+    static int cap = -1;  // launch-shape experiment: CTAs per SM of the FP32 solver
+    if (cap < 0) {
+      const char *e = getenv("CPM_IR_CTAS_PER_SM");
+      cap = e ? atoi(e) : 0;
+    }
+    if (cap > 0 && cap < occ) gmax = (int64_t)cap * sm_count();
+  }
   if (gmax > kMaxGrid) gmax = kMaxGrid;
   int64_t G = (n + threads - 1) / threads;
   if (G > gmax) G = gmax;

@@ -311,26 +311,62 @@ __device__ __forceinline__ int quad_sys(int h, int e) {
   return (NC == 1 && NR == 3) ? (4 * h + e) % 3 : 0;
 }
 
-// Pending reliable updates: x += d, d = 0; active systems: d += alpha p,
-// r -= alpha q, rr += r^2 (FP32 per thread).
+// Active systems: d += alpha p, r -= alpha q, rr += r^2 (FP32 per thread).
 template <int NC, int NR, int NS>
-__device__ __forceinline__ void quad_update(int64_t n, int64_t d0, int needm, int activem, const float (&af)[NS],
-                                            double *x, float *d32, const float *p32, const float *q32, float *r32,
-                                            float (&rrf)[NS]) {
+__device__ __forceinline__ void quad_update(int64_t n, int64_t d0, int activem, const float (&af)[NS], float *d32,
+                                            const float *p32, const float *q32, float *r32, float (&rrf)[NS]) {
+  constexpr int H = NC == 3 ? 3 : NR;
+#pragma unroll
+  for (int h = 0; h < H; ++h) {
+    bool upd = false;
+#pragma unroll
+    for (int e = 0; e < 4; ++e) upd |= (activem >> quad_sys<NC, NR>(h, e)) & 1;
+    if (!upd) continue;
+    const int64_t i0 = quad_base<NC, NR>(n, d0, h);
+    float dd[4], pp[4], qq[4], rr[4];
+    Vec4<float>::load(d32 + i0, dd);
+    Vec4<float>::load(p32 + i0, pp);
+    Vec4<float>::load(q32 + i0, qq);
+    Vec4<float>::load(r32 + i0, rr);
+#pragma unroll
+    for (int e = 0; e < 4; ++e) {
+      const int s = quad_sys<NC, NR>(h, e);
+      if (!((activem >> s) & 1)) continue;
+      dd[e] = fmaf(af[s], pp[e], dd[e]);
+      rr[e] = fmaf(-af[s], qq[e], rr[e]);
+      rrf[s] = fmaf(rr[e], rr[e], rrf[s]);
+    }
+    Vec4<float>::store(r32 + i0, rr);
+    Vec4<float>::store(d32 + i0, dd);
+  }
+}
+
+// p = r + beta p for the active systems; for systems with a pending reliable
+// update also x += d, d = 0 (own unknowns only, so the next phase's true
+// residual is a plain FP64 product on x).
+template <int NC, int NR, int NS>
+__device__ __forceinline__ void quad_direction(int64_t n, int64_t d0, int activem, int needm,
+                                               const float (&beta)[NS], float *p32, const float *r32, double *x,
+                                               float *d32) {
   constexpr int H = NC == 3 ? 3 : NR;
 #pragma unroll
   for (int h = 0; h < H; ++h) {
     const int64_t i0 = quad_base<NC, NR>(n, d0, h);
-    float dd[4], pp[4], qq[4], rr[4];
-    Vec4<float>::load(d32 + i0, dd);
-    bool fold = false, upd = false;
+    float pp[4], rr[4];
+    Vec4<float>::load(p32 + i0, pp);
+    Vec4<float>::load(r32 + i0, rr);
+    bool fold = false;
 #pragma unroll
     for (int e = 0; e < 4; ++e) {
-      fold |= (needm >> quad_sys<NC, NR>(h, e)) & 1;
-      upd |= (activem >> quad_sys<NC, NR>(h, e)) & 1;
+      const int s = quad_sys<NC, NR>(h, e);
+      if ((activem >> s) & 1) pp[e] = fmaf(beta[s], pp[e], rr[e]);
+      fold |= (needm >> s) & 1;
     }
+    Vec4<float>::store(p32 + i0, pp);
     if (fold) {
+      float dd[4];
       double xv[4];
+      Vec4<float>::load(d32 + i0, dd);
       Vec4<double>::load(x + i0, xv);
 #pragma unroll
       for (int e = 0; e < 4; ++e)
@@ -339,42 +375,8 @@ __device__ __forceinline__ void quad_update(int64_t n, int64_t d0, int needm, in
           dd[e] = 0.0f;
         }
       Vec4<double>::store(x + i0, xv);
+      Vec4<float>::store(d32 + i0, dd);
     }
-    if (upd) {
-      Vec4<float>::load(p32 + i0, pp);
-      Vec4<float>::load(q32 + i0, qq);
-      Vec4<float>::load(r32 + i0, rr);
-#pragma unroll
-      for (int e = 0; e < 4; ++e) {
-        const int s = quad_sys<NC, NR>(h, e);
-        if (!((activem >> s) & 1)) continue;
-        dd[e] = fmaf(af[s], pp[e], dd[e]);
-        rr[e] = fmaf(-af[s], qq[e], rr[e]);
-        rrf[s] = fmaf(rr[e], rr[e], rrf[s]);
-      }
-      Vec4<float>::store(r32 + i0, rr);
-    }
-    if (fold || upd) Vec4<float>::store(d32 + i0, dd);
-  }
-}
-
-// p = r + beta p for the active systems.
-template <int NC, int NR, int NS>
-__device__ __forceinline__ void quad_direction(int64_t n, int64_t d0, int activem, const float (&beta)[NS],
-                                               float *p32, const float *r32) {
-  constexpr int H = NC == 3 ? 3 : NR;
-#pragma unroll
-  for (int h = 0; h < H; ++h) {
-    const int64_t i0 = quad_base<NC, NR>(n, d0, h);
-    float pp[4], rr[4];
-    Vec4<float>::load(p32 + i0, pp);
-    Vec4<float>::load(r32 + i0, rr);
-#pragma unroll
-    for (int e = 0; e < 4; ++e) {
-      const int s = quad_sys<NC, NR>(h, e);
-      if ((activem >> s) & 1) pp[e] = fmaf(beta[s], pp[e], rr[e]);
-    }
-    Vec4<float>::store(p32 + i0, pp);
   }
 }
 

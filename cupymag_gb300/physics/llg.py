@@ -42,6 +42,13 @@ from ..utils.sigma_matrices import get_Ebar_sigma
 SOLVE_NAMES = ["elasticity", "demag", "Gauss-Seidel g1n/g2n/g3n", "Gauss-Seidel g1star", "Gauss-Seidel g2star",
                "Gauss-Seidel m1starstar/m2starstar/m3starstar"]
 
+# Reliable-update factor of the FP32 solver per solve (an FP64 true residual whenever the FP32
+# residual has fallen by this factor).  Measured on GB300 at 64^3-128^3: the ill-conditioned
+# elasticity solve converges in the fewest iterations with 0.1 (smaller factors add 25-40 %
+# iterations); the Gauss-Seidel solves (A1, A2; ~30-55 iterations) converge in the same
+# iterations with any factor, so fewer FP64 products win (1e-4); demag is best near 1e-3.
+INNER_TOL = [0.1, 1e-3, 1e-4, 1e-4, 1e-4, 1e-4]
+
 
 class LLGSolver:
     """Device-resident state and operators of one LLG run."""
@@ -158,7 +165,7 @@ class LLGSolver:
     def _cg(self, A, b, x, k):
         self.launches += 1
         self.solver.launch(A, b, x, self.info[k], tol=self.p.tol, maxiter=self.p.maxiter,
-                           use_init_dev=self.use_init, precision=self.precision)
+                           use_init_dev=self.use_init, precision=self.precision, inner_tol=INNER_TOL[k])
 
     def cg_request(self, A, b, x, k):
         """A solve of this step, for an executor that batches solves of several runs."""

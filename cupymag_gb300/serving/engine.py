@@ -39,7 +39,7 @@ import torch
 
 from .. import _native as N
 from ..core.assemble_simulation_operators import SimulationOperators
-from ..physics.llg import SOLVE_NAMES, LLGSolver
+from ..physics.llg import INNER_TOL, SOLVE_NAMES, LLGSolver
 from ..solvers.linear_solvers import decode_info
 from ..workloads import seeded_m0
 from .blockdiag import BlockDiagPlan, BlockSystem, coef_key, work_bytes
@@ -205,7 +205,7 @@ class ServingEngine:
                     BlockSystem(A, b, x, L.info[k], run.work, L.p.tol, L.p.maxiter, L.use_init))
         plans = {k: [] for k in range(NSLOTS)}
         for key, systems in sys_by_key.items():
-            plans[key[0]].append(BlockDiagPlan(systems, self.precision, device=self.dev))
+            plans[key[0]].append(BlockDiagPlan(systems, self.precision, device=self.dev, inner_tol=INNER_TOL[key[0]]))
         g.plans = plans
 
     def _step_runs(self, g):

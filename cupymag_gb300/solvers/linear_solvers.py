@@ -44,7 +44,7 @@ class CGSolver:
         return ws
 
     def launch(self, A: DeviceCSR, b: torch.Tensor, x: torch.Tensor, info: torch.Tensor, *, tol, maxiter,
-               use_init=False, use_init_dev: torch.Tensor = None, precision="DP"):
+               use_init=False, use_init_dev: torch.Tensor = None, precision="DP", inner_tol=None):
         """Asynchronous solve; x is read as x0 when use_init, and overwritten."""
         prec = PRECISIONS[precision] if isinstance(precision, str) else int(precision)
         if prec == 1:
@@ -63,7 +63,7 @@ class CGSolver:
         o.use_init_host = 1 if use_init else 0
         o.use_init_dev = use_init_dev.data_ptr() if use_init_dev is not None else None
         o.precision = prec
-        o.inner_tol = self.inner_tol
+        o.inner_tol = self.inner_tol if inner_tol is None else float(inner_tol)
         o.max_outer = self.max_outer
         o.barrier_timeout_s = self.barrier_timeout_s
         fn = N.lib().cpm_cg_solve_stencil if stencil else N.lib().cpm_cg_solve
