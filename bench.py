@@ -165,7 +165,7 @@ def stencil_launch_bytes(A, nvec, iters, outer, fp32):
 # (dram__bytes_read.sum + dram__bytes_write.sum of a 300-iteration elastic 128^3 launch / (300 x unknowns));
 # the vectors fit the L2 about half way, so this is below the 44 algorithmic bytes.  Traffic of a launch
 # is this figure times its unknowns and iterations (it grows in proportion at a fixed grid size).
-IR_STENCIL_DRAM_BYTES_PER_UNKNOWN_ITER = 21.4
+IR_STENCIL_DRAM_BYTES_PER_UNKNOWN_ITER = 23.0
 
 
 def cg_launch_bytes(A, nvec, iters, warm):

@@ -623,6 +623,8 @@ static int assign(const cpm_batch_system *sys, int nsys, int ncomp, int nrhs, in
     set_error("%s: kernel cannot be resident on an SM", who);
     return CPM_CUDA_ERROR;
   }
+  // all resident CTAs: a batch's chunk reductions spread over more CTAs (fewer CTAs, as the
+  // single-system solver uses for small grids, measured slower for batches)
   int64_t gmax = (int64_t)occ * sm_count();
   if (gmax > kMaxGrid) gmax = kMaxGrid;
   if (nsys > gmax) {

@@ -134,6 +134,22 @@ struct Workspace {
 
 inline size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
 
+// CTAs per SM of the FP32 solvers: fewer, fuller CTAs while the work is small
+// (fewer grid-barrier arrivals and partial sums, more independent loads per
+// thread), up to the resident limit.  Measured on GB300 (elastic 48^3..128^3,
+// scalar 64^3..128^3): the best shapes hold about 4500 DOFs per CTA for
+// operators with 3 unknowns per DOF and about 6500 for scalar ones.
+inline int ir_ctas_per_sm(int64_t dofs, int unknowns_per_dof, int occ) {
+  const int64_t per_sm = dofs / (sm_count() > 0 ? sm_count() : 1);
+  const int64_t target = unknowns_per_dof >= 3 ? 4500 : 6500;
+  int64_t c = per_sm / target;
+  if (c < 1) c = 1;
+  if (c > occ) c = occ;
+  return (int)c;
+}
+
+
+
 
 inline size_t layout(int64_t n, int nrhs, int precision, char *base, Workspace *w) {
   size_t off = 0;

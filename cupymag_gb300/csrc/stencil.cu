@@ -25,7 +25,6 @@
 // coefficients and FP64 dot accumulation.  GB300 issues FP32 FMAs at many
 // times its FP64 rate, so the FP32 iterations are bound by vector traffic.
 #include <algorithm>
-#include <cstdlib>
 #include <cmath>
 
 #include "stencil_ops.cuh"
@@ -522,14 +521,7 @@ static int launch_stencil_cg(const cpm_stencil *s, const double *b, double *x, c
   }
   const int64_t n = a.S.n;
   int64_t gmax = (int64_t)occ * sm_count();
-  if (!fp64) {
-    static int cap = -1;  // launch-shape experiment: CTAs per SM of the FP32 solver
-    if (cap < 0) {
-      const char *e = getenv("CPM_IR_CTAS_PER_SM");
-      cap = e ? atoi(e) : 0;
-    }
-    if (cap > 0 && cap < occ) gmax = (int64_t)cap * sm_count();
-  }
+  if (!fp64) gmax = (int64_t)ir_ctas_per_sm(s->nx * (int64_t)s->ny * s->nz, NC * NR, occ) * sm_count();
   if (gmax > kMaxGrid) gmax = kMaxGrid;
   int64_t G = (n + threads - 1) / threads;
   if (G > gmax) G = gmax;

@@ -311,9 +311,8 @@ class ServingEngine:
         clock = lambda: time.perf_counter() - t0  # noqa: E731
 
         def admit_arrived():
-            now = clock()
-            while pending and (not realtime or pending[0].arrival <= now) and self.fits(pending[0]):
-                self.admit(pending.popleft(), now)
+            while pending and (not realtime or pending[0].arrival <= clock()) and self.fits(pending[0]):
+                self.admit(pending.popleft(), clock())
 
         while pending or any(g.runs for g in self.groups.values()):
             admit_arrived()
@@ -325,7 +324,9 @@ class ServingEngine:
             g = min(live, key=lambda h: (h.gpu_s, h.cls))
             ts = time.perf_counter()
             self.step(g)
-            # requests that arrived meanwhile are set up while the step runs
+            # requests that arrived meanwhile are set up while the step runs on the GPU (all of
+            # them at once: spreading admissions over turns churns group compositions, and every
+            # change costs a plan build, an eager step and a graph capture)
             admit_arrived()
             torch.cuda.synchronize(self.dev)
             g.gpu_s += time.perf_counter() - ts
