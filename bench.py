@@ -506,6 +506,11 @@ def run_reference(args):
     # setup only (not timed): the structured assembly builds the same CSR matrices
     S = SimulationOperators(p, device=dev, mesh=w.get("mesh"))
     its = REFERENCE_ITERS.get(args.workload)
+    if its is None:
+        print(json.dumps({"impl": "reference", "metric": METRIC, "unavailable":
+                          f"no measured FP64 iteration counts for workload {args.workload} to extrapolate the "
+                          f"sampled CPU step (known: {sorted(REFERENCE_ITERS)})"}))
+        return None
     times = []
     for s in range(args.warmup + args.steps):
         cs = cpu_sample(p, S, its)

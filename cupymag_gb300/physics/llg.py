@@ -147,6 +147,37 @@ class LLGSolver:
         self.hstep = torch.zeros(1, dtype=torch.int32, device=self.dev)
         self.hist = torch.zeros((f.shape[0], 4), dtype=torch.float64, device=self.dev)
 
+    # ------------------------------------------------------------------ checkpoint / resume
+    def _state_tensors(self):
+        """Every device tensor that carries over from one step to the next: m, m_prev, <m>, sumsq,
+        the warm-start flag, the previous solutions the warm-started solves start from (U, the g's,
+        m**, and u with magnetoelastic coupling) and the field-schedule position."""
+        t = {"m": self.m, "m_prev": self.m_prev, "avg_m": self.avg_m, "sumsq": self.sumsq, "use_init": self.use_init,
+             "U": self.U, "g": self.g, "g1s": self.g1s, "g2s": self.g2s, "mss": self.mss}
+        if self.ME:
+            t["u"] = self.u
+        if self.hsched is not None:
+            t.update(hsched=self.hsched, hstep=self.hstep, hist=self.hist)
+        return t
+
+    def save_state(self, path):
+        """Write the run's state (.npz) so that load_state + further steps reproduce an uninterrupted run
+        bit for bit (the reference restarts from m alone, magnetization_io.py:80-124)."""
+        arrays = {k: v.detach().cpu().numpy() for k, v in self._state_tensors().items()}
+        np.savez(path, nstep=np.int64(self.nstep), n=np.int64(self.n), ME=np.int8(self.ME), **arrays)
+
+    def load_state(self, path):
+        d = np.load(path)
+        if int(d["n"]) != self.n or bool(d["ME"]) != self.ME:
+            raise ValueError(f"checkpoint of a different run (n={int(d['n'])}, ME={bool(d['ME'])})")
+        if "hsched" in d and self.hsched is None:
+            self.set_field_schedule(d["hsched"])
+        for k, t in self._state_tensors().items():
+            if k not in d:
+                raise ValueError(f"checkpoint lacks {k}")
+            t.copy_(torch.as_tensor(d[k], device=self.dev))
+        self.nstep = int(d["nstep"])
+
     # ------------------------------------------------------------------ building blocks
     def _field_params(self, Hext):
         P = N.FieldParams()
