@@ -71,9 +71,10 @@ _PROTOS = {
     "cpm_cg_solve": (C.c_int, [C.POINTER(CSR), vp, vp, C.c_int, C.POINTER(CGOpts), vp, C.c_size_t, vp, vp]),
     "cpm_cg_solve_noalloc": (C.c_int, [C.POINTER(CSR), vp, vp, C.c_int, C.POINTER(CGOpts), vp, vp]),
     "cpm_stencil_apply": (C.c_int, [C.POINTER(Stencil), vp, vp, dbl, C.c_int, vp]),
+    "cpm_stencil_apply32": (C.c_int, [C.POINTER(Stencil), vp, vp, C.c_int, C.c_int, vp]),
     "cpm_cg_solve_stencil": (C.c_int, [C.POINTER(Stencil), vp, vp, C.c_int, C.POINTER(CGOpts), vp, C.c_size_t, vp,
                                        vp]),
-    "cpm_batch_work_bytes": (i64, [i64, i32, i32, i32]),
+    "cpm_batch_work_bytes": (i64, [i32, i32, i32, i32, i32, i32]),
     "cpm_batch_plan_bytes": (C.c_int, [C.POINTER(BatchSystem), i32, i32, i32, i32, C.POINTER(i64)]),
     "cpm_batch_plan_build": (C.c_int, [C.POINTER(BatchSystem), i32, i32, i32, i32, vp, vp, i64, C.POINTER(BatchPlan),
                                        vp]),

@@ -5,16 +5,17 @@
 // (scalar with 1 or 3 right-hand sides, or elastic) on periodic hex grids of
 // different sizes that share one coefficient table (requests with the same
 // material and time step).  Each system's DOFs are cut into chunks whose size
-// depends only on the operator kind; a chunk's partial dot products are
-// reduced in a fixed order, and a system's totals add its own chunks'
-// partials in a fixed order.  A system's iterates are therefore bit-for-bit
-// the same whether it is solved alone or together with any other systems:
-// the batch only changes which CTA works on which chunk.
+// depends only on the operator kind and the system's own size; a chunk's
+// partial dot products are reduced in a fixed order, and a system's totals add
+// its own chunks' partials in a fixed order.  A system's iterates are
+// therefore bit-for-bit the same whether it is solved alone or together with
+// any other systems: the batch only changes which CTA works on which chunk.
 //
 // CTAs are given to systems in proportion to their chunks (equal load per
-// CTA).  All CTAs pass the same grid barriers; a system that has converged
-// idles, and the launch ends when a device counter of systems that are still
-// iterating drops to zero.  Every wait is bounded (GridBarrier).
+// CTA; CTA l of a system takes its chunks l, l + ncta, ...).  All CTAs pass
+// the same grid barriers; a system that has converged idles, and the launch
+// ends when a device counter of systems that are still iterating drops to
+// zero.  Every wait is bounded (GridBarrier).
 //
 // Precision 0 is the three-phase FP64 CG of csrc/stencil.cu.  Precision 1 is
 // FP32 CG with FP64 reliable updates in a form that needs no extra barrier:
@@ -34,7 +35,8 @@
 
 namespace cpm {
 
-constexpr int kSlot = 12;  // doubles per chunk partial (>= 3 values x 3 systems)
+constexpr int kSlot = 12;        // doubles per chunk partial (>= 3 values x 3 systems)
+constexpr int kMaxChunks = 1024;  // chunks of one system (a multiple of kCGThreads)
 
 // Grid geometry of one system in registers.
 struct Geo {
@@ -76,11 +78,21 @@ __host__ __device__ constexpr int b_systems() { return NC == 1 ? NR : 1; }
 template <int NC, int NR>
 __device__ __forceinline__ int b_sys(int comp) { return NC == 1 ? comp : 0; }
 
+// Chunks whose warp sums a CTA stages in shared memory before one flush.
+constexpr int kStage = 8;
+constexpr int kStageDoubles = kStage * 9 * kCGWarps;
+
 // Partials of this CTA's chunks: body(d0, d1, v) accumulates the calling
-// thread's DOFs of [d0, d1) (stride kCGThreads) into v.
+// thread's DOFs of [d0, d1) (stride kCGThreads) into v.  A chunk's partial is
+// the sum, in warp order, of its warps' shuffle sums: the same value whichever
+// CTA computes the chunk.  The warp sums of up to kStage chunks wait in
+// `stage` and are added and written together, so a chunk costs shuffles but
+// no block barrier.
 template <int NV, typename Body>
-__device__ __forceinline__ void chunk_partials(const BSeg &S, int l, double *half, double (*sred)[kCGWarps],
-                                               Body body) {
+__device__ __forceinline__ void chunk_partials(const BSeg &S, int l, double *half, double *stage, Body body) {
+  static_assert(NV <= 9, "stage holds at most 9 sums per chunk");
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  int held = 0, first = l;
   for (int c = l; c < S.nchunks; c += S.ncta) {
     double v[NV];
 #pragma unroll
@@ -88,11 +100,25 @@ __device__ __forceinline__ void chunk_partials(const BSeg &S, int l, double *hal
     const int d0 = c * S.chunk_dofs;
     const int d1 = min(S.n, d0 + S.chunk_dofs);
     body(d0, d1, v);
-    block_sum<NV>(v, sred);
-    double *dst = half + (size_t)(S.chunk0 + c) * kSlot;
 #pragma unroll
-    for (int j = 0; j < NV; ++j)
-      if (threadIdx.x == j) dst[j] = v[j];
+    for (int j = 0; j < NV; ++j) {
+      const double t = warp_sum(v[j]);
+      if (lane == 0) stage[(held * NV + j) * kCGWarps + w] = t;
+    }
+    if (++held == kStage || c + S.ncta >= S.nchunks) {
+      __syncthreads();
+      for (int t = threadIdx.x; t < held * NV; t += kCGThreads) {
+        const double *src = stage + t * kCGWarps;
+        double s = 0.0;
+#pragma unroll
+        for (int k = 0; k < kCGWarps; ++k) s += src[k];
+        const int cl = t / NV;
+        half[(size_t)(S.chunk0 + first + cl * S.ncta) * kSlot + (t - cl * NV)] = s;
+      }
+      __syncthreads();
+      held = 0;
+      first = c + S.ncta;
+    }
   }
 }
 
@@ -101,14 +127,15 @@ __device__ __forceinline__ void chunk_partials(const BSeg &S, int l, double *hal
 // partial buffer alternates halves as in grid_sum.
 template <int NV, typename Body>
 __device__ __forceinline__ bool seg_reduce(const BatchArgs &a, const BSeg &S, int l, bool work, int &par,
-                                           double (*sred)[kCGWarps], double (&v)[NV], Body body) {
+                                           double (*sred)[kCGWarps], double *stage, double (&v)[NV], Body body) {
   double *half = a.part + (size_t)par * (size_t)a.half;
   par ^= 1;
-  if (work) chunk_partials<NV>(S, l, half, sred, body);
+  if (work) chunk_partials<NV>(S, l, half, stage, body);
   if (!grid_sync(a.bar, gridDim.x, a.timeout_ns)) return false;
   if (work) {
 #pragma unroll
     for (int j = 0; j < NV; ++j) v[j] = 0.0;
+    // at most kMaxChunks / kCGThreads = 4 chunk partials per thread, in chunk order
     for (int c = threadIdx.x; c < S.nchunks; c += kCGThreads) {
       const double *src = half + (size_t)(S.chunk0 + c) * kSlot;
 #pragma unroll
@@ -138,7 +165,12 @@ __global__ void __launch_bounds__(kCGThreads, 2) cg_batched_fp64_kernel(const __
   constexpr int U = NC * NR;
   constexpr int NS = b_systems<NC, NR>();
   __shared__ double s_red[9][kCGWarps];
-  const BSeg &S = a.segs[a.cta_seg[blockIdx.x]];
+  __shared__ double s_stage[kStageDoubles];
+  // the CTA's system record, read once into shared memory (its fields are re-read cheaply there)
+  __shared__ BSeg s_seg;
+  if (threadIdx.x == 0) s_seg = a.segs[a.cta_seg[blockIdx.x]];
+  __syncthreads();
+  const BSeg &S = s_seg;
   const int l = blockIdx.x - S.cta0;
   const bool lead = l == 0 && threadIdx.x == 0;
   const Geo g{S.nx, S.ny, S.nz, S.n, S.flags};
@@ -152,7 +184,7 @@ __global__ void __launch_bounds__(kCGThreads, 2) cg_batched_fp64_kernel(const __
   int par = 0;
 
   double v[2 * NS];
-  bool ok = seg_reduce<2 * NS>(a, S, l, true, par, s_red, v, [&](int d0, int d1, double (&w)[2 * NS]) {
+  bool ok = seg_reduce<2 * NS>(a, S, l, true, par, s_red, s_stage, v, [&](int d0, int d1, double (&w)[2 * NS]) {
     for (int dof = d0 + threadIdx.x; dof < d1; dof += kCGThreads) {
       double y[U];
       if (use_init) apply_c<double, NC, NR>(g, c, x, dof, y);
@@ -207,7 +239,7 @@ __global__ void __launch_bounds__(kCGThreads, 2) cg_batched_fp64_kernel(const __
     }
     // ---- q = A p, p.q
     double pq[NS];
-    if (!seg_reduce<NS>(a, S, l, any, par, s_red, pq, [&](int d0, int d1, double (&w)[NS]) {
+    if (!seg_reduce<NS>(a, S, l, any, par, s_red, s_stage, pq, [&](int d0, int d1, double (&w)[NS]) {
           for (int dof = d0 + threadIdx.x; dof < d1; dof += kCGThreads) {
             double y[U];
             apply_c<double, NC, NR>(g, c, p, dof, y);
@@ -238,7 +270,7 @@ __global__ void __launch_bounds__(kCGThreads, 2) cg_batched_fp64_kernel(const __
     }
     // ---- x += alpha p, r -= alpha q, r.r
     double rr[NS];
-    if (!seg_reduce<NS>(a, S, l, any, par, s_red, rr, [&](int d0, int d1, double (&w)[NS]) {
+    if (!seg_reduce<NS>(a, S, l, any, par, s_red, s_stage, rr, [&](int d0, int d1, double (&w)[NS]) {
           for (int dof = d0 + threadIdx.x; dof < d1; dof += kCGThreads) {
 #pragma unroll
             for (int u = 0; u < U; ++u) {
@@ -315,10 +347,15 @@ __global__ void __launch_bounds__(kCGThreads, (NC == 1 && NR == 3) ? 3 : 4) cg_b
   constexpr int U = NC * NR;
   constexpr int NS = b_systems<NC, NR>();
   __shared__ double s_red[9][kCGWarps];
+  __shared__ double s_stage[kStageDoubles];
   __shared__ IRState st[NS];
   __shared__ float s_ab[NS];
   __shared__ int s_mask[3];  // active, need, status
-  const BSeg &S = a.segs[a.cta_seg[blockIdx.x]];
+  // the CTA's system record, read once into shared memory (its fields are re-read cheaply there)
+  __shared__ BSeg s_seg;
+  if (threadIdx.x == 0) s_seg = a.segs[a.cta_seg[blockIdx.x]];
+  __syncthreads();
+  const BSeg &S = s_seg;
   const int l = blockIdx.x - S.cta0;
   const bool lead = l == 0;
   const Geo g{S.nx, S.ny, S.nz, S.n, S.flags};
@@ -332,7 +369,7 @@ __global__ void __launch_bounds__(kCGThreads, (NC == 1 && NR == 3) ? 3 : 4) cg_b
 
   // ---- r = b - A64 x, r32 = p32 = r, d = 0; ||b||, ||r||
   double v[2 * NS];
-  bool ok = seg_reduce<2 * NS>(a, S, l, true, par, s_red, v, [&](int d0, int d1, double (&w)[2 * NS]) {
+  bool ok = seg_reduce<2 * NS>(a, S, l, true, par, s_red, s_stage, v, [&](int d0, int d1, double (&w)[2 * NS]) {
     for (int dof = d0 + threadIdx.x; dof < d1; dof += kCGThreads) {
       double y[U];
       if (use_init) apply_c<double, NC, NR>(g, a.c64, x, dof, y);
@@ -389,7 +426,7 @@ __global__ void __launch_bounds__(kCGThreads, (NC == 1 && NR == 3) ? 3 : 4) cg_b
     const bool busy = activem != 0;  // pending updates belong to active systems
     // ---- q = A32 p, p.q (FP32 per thread); pending updates: t = b - A64 x, r32 = t, t.t, t.p
     double pt[3 * NS];
-    if (!seg_reduce<3 * NS>(a, S, l, busy, par, s_red, pt, [&](int d0, int d1, double (&w)[3 * NS]) {
+    if (!seg_reduce<3 * NS>(a, S, l, busy, par, s_red, s_stage, pt, [&](int d0, int d1, double (&w)[3 * NS]) {
           float pqf[NS];
 #pragma unroll
           for (int j = 0; j < NS; ++j) pqf[j] = 0.0f;
@@ -467,7 +504,7 @@ __global__ void __launch_bounds__(kCGThreads, (NC == 1 && NR == 3) ? 3 : 4) cg_b
     }
     // ---- active: d += alpha p, r32 -= alpha q, r32.r32
     double rr[NS];
-    if (!seg_reduce<NS>(a, S, l, activem != 0, par, s_red, rr, [&](int d0, int d1, double (&w)[NS]) {
+    if (!seg_reduce<NS>(a, S, l, activem != 0, par, s_red, s_stage, rr, [&](int d0, int d1, double (&w)[NS]) {
           float rrf[NS];
 #pragma unroll
           for (int j = 0; j < NS; ++j) rrf[j] = 0.0f;
@@ -559,7 +596,15 @@ __global__ void __launch_bounds__(kCGThreads, (NC == 1 && NR == 3) ? 3 : 4) cg_b
 }
 
 // ---------------------------------------------------------------- host side
-static int chunk_dofs_for(int ncomp, int nrhs) { return ncomp == 3 ? 1024 : (nrhs == 3 ? 2048 : 4096); }
+// DOFs per chunk of one system: a base size per operator kind, doubled until
+// the system has at most kMaxChunks chunks.  It depends on the system alone,
+// never on the rest of the batch, so the chunk partials (and every iterate)
+// are the same alone and in any mix.
+static int chunk_dofs_for(int ncomp, int nrhs, int64_t n) {
+  int64_t cd = ncomp == 3 ? 1024 : (nrhs == 3 ? 2048 : 4096);
+  while ((n + cd - 1) / cd > kMaxChunks) cd *= 2;
+  return (int)cd;
+}
 
 static const void *batched_kernel(int ncomp, int nrhs, int precision) {
   if (precision == 0) {
@@ -601,7 +646,6 @@ static int assign(const cpm_batch_system *sys, int nsys, int ncomp, int nrhs, in
     set_error("%s: bad batch (nsys >= 1, ncomp 1 or 3, nrhs 1 or 3 with ncomp 1, precision 0 or 1)", who);
     return CPM_BAD_ARG;
   }
-  const int cd = chunk_dofs_for(ncomp, nrhs);
   A.nchunks.assign(nsys, 0);
   A.total_chunks = 0;
   for (int s = 0; s < nsys; ++s) {
@@ -613,6 +657,7 @@ static int assign(const cpm_batch_system *sys, int nsys, int ncomp, int nrhs, in
                 "256-byte aligned work buffer set, maxiter >= 1, tol >= 0)", who, s);
       return CPM_BAD_ARG;
     }
+    const int cd = chunk_dofs_for(ncomp, nrhs, n);
     A.nchunks[s] = (int)((n + cd - 1) / cd);
     A.total_chunks += A.nchunks[s];
   }
@@ -650,8 +695,11 @@ static int assign(const cpm_batch_system *sys, int nsys, int ncomp, int nrhs, in
 
 }  // namespace cpm
 
-extern "C" int64_t cpm_batch_work_bytes(int64_t n, int32_t ncomp, int32_t nrhs, int32_t precision) {
+extern "C" int64_t cpm_batch_work_bytes(int32_t nx, int32_t ny, int32_t nz, int32_t ncomp, int32_t nrhs,
+                                        int32_t precision) {
   using namespace cpm;
+  if (nx < 1 || ny < 1 || nz < 1 || (ncomp != 1 && ncomp != 3) || (nrhs != 1 && nrhs != 3)) return 0;
+  const int64_t n = (int64_t)nx * ny * nz;
   return (int64_t)((precision ? 4 : 3) * vec_bytes(n, ncomp, nrhs, precision));
 }
 
@@ -680,7 +728,6 @@ extern "C" int cpm_batch_plan_build(const cpm_batch_system *sys, int32_t nsys, i
               "%zu bytes)", L.total);
     return CPM_BAD_ARG;
   }
-  const int cd = chunk_dofs_for(ncomp, nrhs);
   std::vector<BSeg> segs(nsys);
   std::vector<int> cmap(A.grid);
   int chunk0 = 0, cta0 = 0;
@@ -703,7 +750,9 @@ extern "C" int cpm_batch_plan_build(const cpm_batch_system *sys, int32_t nsys, i
     S.nchunks = A.nchunks[s];
     S.cta0 = cta0;
     S.ncta = A.ncta[s];
-    S.chunk_dofs = cd;
+    S.chunk_dofs = chunk_dofs_for(ncomp, nrhs, S.n);
+    // quads need whole quads per z-line, 4-byte aligned flags and an aligned x; other grids take the
+    // per-DOF product (scalar-load quads and quads on a padded copy of p measured slower in this kernel)
     S.quads = (y.nz & 3) == 0 && ((uintptr_t)y.flags & 3) == 0 && ((uintptr_t)y.x & 15) == 0;
     const size_t vb = vec_bytes(S.n, ncomp, nrhs, precision);
     char *w = (char *)y.work;

@@ -92,6 +92,17 @@ __device__ __forceinline__ void ld4(const TX *x, int64_t i, int, T *v) {
   for (int e = 0; e < 4; ++e) v[e] = (T)t[e];
 }
 
+// Elements i..i+3: one aligned vector load (VEC) or four scalar loads.
+template <typename T, bool VEC, typename TX>
+__device__ __forceinline__ void ldq(const TX *x, int64_t i, int c, T *v) {
+  if (VEC) {
+    ld4<T>(x, i, c, v);
+  } else {
+#pragma unroll
+    for (int e = 0; e < 4; ++e) v[e] = ld<T>(x, i + e, c);
+  }
+}
+
 // ---------------------------------------------------------------- reductions
 // Fixed shuffle pattern: the result is a deterministic function of the inputs.
 __device__ __forceinline__ double warp_sum(double v) {

@@ -455,6 +455,30 @@ __global__ void __launch_bounds__(256) stencil_apply_kernel(const __grid_constan
   }
 }
 
+// ---------------------------------------------------------------- y = A x (FP32, the refinement form's product)
+// FORM 0: per DOF (apply_c); 1: quads with aligned vector loads (nz % 4 == 0);
+// 2: quads with scalar loads (any nz).  The same products the FP32 CG phases run.
+template <int NC, int NR, int FORM>
+__global__ void __launch_bounds__(256) stencil_apply32_kernel(const __grid_constant__ StencilOp S, const float *x,
+                                                              float *y) {
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  if (FORM == 0) {
+    for (int64_t dof = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; dof < S.n; dof += stride) {
+      float t[NC * NR];
+      apply_c<float, NC, NR>(S, S.c32, x, (int)dof, t);
+#pragma unroll
+      for (int u = 0; u < NC * NR; ++u) y[uidx<NC, NR>(S.n, dof, u)] = t[u];
+    }
+  } else {
+    const int64_t nq = (S.n + 3) / 4;
+    for (int64_t qd = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; qd < nq; qd += stride) {
+      float t[4][NC * NR];
+      apply4_c<float, NC, NR, FORM == 1>(S, S.c32, x, (int)(4 * qd), t);
+      quad_store<float, NC, NR, FORM == 1>(y, S.n, 4 * qd, t);
+    }
+  }
+}
+
 static StencilOp to_op(const cpm_stencil *s) {
   StencilOp S;
   S.nx = s->nx;
@@ -520,8 +544,16 @@ static int launch_stencil_cg(const cpm_stencil *s, const double *b, double *x, c
     return CPM_CUDA_ERROR;
   }
   const int64_t n = a.S.n;
+  // vector quads need whole quads per z-line, aligned flags and an aligned x
+  a.quads = quads_ok(s) && ((uintptr_t)x & 15) == 0 ? 1 : 0;
+  // The FP32 quad product (4 outputs and 27 independent loads per thread) runs best on few, full
+  // CTAs.  The elastic per-DOF product (grids with nz % 4 != 0) needs every resident CTA to hide its
+  // gather latency; the scalar ones do not.  Measured on GB300: elastic 81^3 per DOF 80 us per
+  // iteration on one CTA per SM, 64.6 us on all of them (80^3 in quads: 45.7 us); demag 81^3 and the
+  // 3-RHS A1 81^3 per DOF slower on all CTAs (53 and 178 us).
   int64_t gmax = (int64_t)occ * sm_count();
-  if (!fp64) gmax = (int64_t)ir_ctas_per_sm(s->nx * (int64_t)s->ny * s->nz, NC * NR, occ) * sm_count();
+  if (!fp64 && (a.quads || NC == 1))
+    gmax = (int64_t)ir_ctas_per_sm(s->nx * (int64_t)s->ny * s->nz, NC * NR, occ) * sm_count();
   if (gmax > kMaxGrid) gmax = kMaxGrid;
   int64_t G = (n + threads - 1) / threads;
   if (G > gmax) G = gmax;
@@ -530,7 +562,6 @@ static int launch_stencil_cg(const cpm_stencil *s, const double *b, double *x, c
   per = (per + 31) / 32 * 32;
   G = (n + per - 1) / per;
   a.dofs_per_cta = per;
-  a.quads = quads_ok(s) && ((uintptr_t)x & 15) == 0 ? 1 : 0;
   CPM_TRY(cudaMemsetAsync(w.bar, 0, sizeof(GridBarrier), st));
   CPM_TRY(cudaMemsetAsync(info, 0, sizeof(cpm_cg_info), st));
   void *args[] = {&a};
@@ -595,4 +626,37 @@ extern "C" int cpm_stencil_apply(const cpm_stencil *S, const double *x, double *
   else
     stencil_apply_kernel<1, 3><<<(int)g, 256, 0, st>>>(op, x, y, alpha);
   return check_launch("cpm_stencil_apply");
+}
+
+extern "C" int cpm_stencil_apply32(const cpm_stencil *S, const float *x, float *y, int nvec, int form, void *stream) {
+  using namespace cpm;
+  if (int e = check_stencil(S, "cpm_stencil_apply32")) return e;
+  if (!x || !y || (nvec != 1 && nvec != 3) || (S->ncomp == 3 && nvec != 1) || form < 0 || form > 2) {
+    set_error("cpm_stencil_apply32: bad vectors or form (0 per DOF, 1 aligned quads, 2 scalar-load quads)");
+    return CPM_BAD_ARG;
+  }
+  if ((form == 1 && !(quads_ok(S) && (((uintptr_t)x | (uintptr_t)y) & 15) == 0)) ||
+      (form == 2 && ((uintptr_t)S->flags & 3) != 0)) {
+    set_error("cpm_stencil_apply32: form %d needs %s", form,
+              form == 1 ? "nz % 4 == 0, 4-byte aligned flags and 16-byte aligned x and y" : "4-byte aligned flags");
+    return CPM_BAD_ARG;
+  }
+  const StencilOp op = to_op(S);
+  const int64_t units = form == 0 ? op.n : (op.n + 3) / 4;
+  const int64_t g = std::max<int64_t>(1, std::min<int64_t>((units + 255) / 256, (int64_t)sm_count() * 8));
+  cudaStream_t st = (cudaStream_t)stream;
+#define CPM_APPLY32(F)                                                                    \
+  do {                                                                                    \
+    if (S->ncomp == 3)                                                                    \
+      stencil_apply32_kernel<3, 1, F><<<(int)g, 256, 0, st>>>(op, x, y);                  \
+    else if (nvec == 1)                                                                   \
+      stencil_apply32_kernel<1, 1, F><<<(int)g, 256, 0, st>>>(op, x, y);                  \
+    else                                                                                  \
+      stencil_apply32_kernel<1, 3, F><<<(int)g, 256, 0, st>>>(op, x, y);                  \
+  } while (0)
+  if (form == 0) CPM_APPLY32(0);
+  else if (form == 1) CPM_APPLY32(1);
+  else CPM_APPLY32(2);
+#undef CPM_APPLY32
+  return check_launch("cpm_stencil_apply32");
 }

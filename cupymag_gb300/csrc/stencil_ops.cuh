@@ -131,32 +131,46 @@ __device__ __forceinline__ void apply_c(const Geo &S, const T *c, const XS &x, i
 }
 
 // ---------------------------------------------------------------- four DOFs along z
-// Register-blocked application to the quad of DOFs d0..d0+3 (d0 % 4 == 0,
-// nz % 4 == 0, so the quad lies in one z-line at k0..k0+3).  Each of the 9
-// (x, y) neighbour columns is read once per component as an aligned vector
-// of 4 plus the two wrapped edge values k0-1 and k0+4, and serves all three
-// z offsets of all four DOFs: 6 loads where the per-DOF form makes 12.  The
-// FMAs run in the per-DOF order (neighbour d = (dx, dy, dz) lexicographic,
-// then components), so every y is bit-identical to apply_c's.  A quad with a
+// Register-blocked application to the quad of DOFs d0..d0+3 (d0 % 4 == 0).
+// When the quad lies in one z-line (at k0..k0+3), each of the 9 (x, y)
+// neighbour columns is read once per component as 4 consecutive values plus
+// the two wrapped edge values k0-1 and k0+4, and serves all three z offsets
+// of all four DOFs: 6 loads where the per-DOF form makes 12.  The FMAs run in
+// the per-DOF order (neighbour d = (dx, dy, dz) lexicographic, then
+// components), so every y is bit-identical to apply_c's.  A quad with a
 // flagged DOF (unit / empty row or a neighbour of an excluded column) takes
 // apply_c per DOF.
-template <typename T, int NC, int NR, typename Geo, typename XS>
-__device__ __forceinline__ void apply4_c(const Geo &S, const T *c, const XS &x, int d0,
-                                         T (&y)[4][NC * NR]) {
-  if (S.flags && *reinterpret_cast<const uint32_t *>(S.flags + d0) != 0u) {
+//
+// VEC: nz % 4 == 0 and 16-byte aligned operands, so every quad lies in one
+// z-line and each group of 4 is one aligned vector load.  Otherwise (any nz)
+// the groups of 4 are scalar loads, and a quad that crosses the end of its
+// z-line takes apply_c per DOF; outputs past the end of the grid are zero.
+// The quad DOF by DOF (flagged quads; for the scalar form also quads that
+// leave their z-line); outputs past the end of the grid are zero.
+template <typename T, int NC, int NR, bool VEC, typename Geo, typename XS>
+__device__ __forceinline__ void apply4_per_dof(const Geo &S, const T *c, const XS &x, int d0,
+                                               T (&y)[4][NC * NR]) {
 #pragma unroll
-    for (int kk = 0; kk < 4; ++kk) {
-      T t[NC * NR];
+  for (int kk = 0; kk < 4; ++kk) {
+    T t[NC * NR];
+    if (VEC || d0 + kk < S.n) {
       apply_c<T, NC, NR>(S, c, x, d0 + kk, t);
+    } else {
 #pragma unroll
-      for (int u = 0; u < NC * NR; ++u) y[kk][u] = t[u];
+      for (int u = 0; u < NC * NR; ++u) t[u] = T(0);
     }
-    return;
+#pragma unroll
+    for (int u = 0; u < NC * NR; ++u) y[kk][u] = t[u];
   }
-  const Nbr b = neighbours(S, d0);
-  const int k0 = b.zk[1];
-  const int km = b.zk[0];                                  // k0 - 1 (wrapped)
-  const int kp = (k0 + 4 == S.nz) ? 0 : k0 + 4;            // k0 + 4 (wrapped)
+}
+
+// The FMAs of the quad at z = k0..k0+3 of the z-lines whose first elements
+// are xo[ia] + yo[ib] (the 9 (x, y) neighbour columns) in vector x, with the
+// wrapped edge positions km (k0 - 1) and kp (k0 + 4); cs is the component
+// stride of the elastic layout.
+template <typename T, int NC, int NR, bool VEC, typename XS>
+__device__ __forceinline__ void quad_columns(const T *c, const XS &x, const int (&xo)[3], const int (&yo)[3], int k0,
+                                             int km, int kp, int64_t cs, T (&y)[4][NC * NR]) {
 #pragma unroll
   for (int kk = 0; kk < 4; ++kk)
 #pragma unroll
@@ -165,13 +179,13 @@ __device__ __forceinline__ void apply4_c(const Geo &S, const T *c, const XS &x, 
   for (int ia = 0; ia < 3; ++ia)
 #pragma unroll
     for (int ib = 0; ib < 3; ++ib) {
-      const int col = b.xi[ia] + b.yj[ib];
+      const int col = xo[ia] + yo[ib];
       if (NC == 1) {
         // w[z][r]: z = 0 is k0 - 1, 1..4 the quad, 5 is k0 + 4
         T w[6][NR];
         if (NR == 1) {
           T v[4];
-          ld4<T>(x, (int64_t)col + k0, 0, v);
+          ldq<T, VEC>(x, (int64_t)col + k0, 0, v);
           w[0][0] = ld<T>(x, (int64_t)col + km, 0);
 #pragma unroll
           for (int e = 0; e < 4; ++e) w[1 + e][0] = v[e];
@@ -180,7 +194,7 @@ __device__ __forceinline__ void apply4_c(const Geo &S, const T *c, const XS &x, 
 #pragma unroll
           for (int h = 0; h < NR; ++h) {
             T v[4];
-            ld4<T>(x, (int64_t)(col + k0) * NR + 4 * h, (4 * h) % NR, v);
+            ldq<T, VEC>(x, (int64_t)(col + k0) * NR + 4 * h, (4 * h) % NR, v);
 #pragma unroll
             for (int e = 0; e < 4; ++e) w[1 + (4 * h + e) / NR][(4 * h + e) % NR] = v[e];
           }
@@ -199,13 +213,12 @@ __device__ __forceinline__ void apply4_c(const Geo &S, const T *c, const XS &x, 
             for (int r = 0; r < NR; ++r) y[kk][r] = fma(cw, w[kk + ic][r], y[kk][r]);
         }
       } else {
-        const int n = S.n;
         T w[3][6];
 #pragma unroll
         for (int cm = 0; cm < 3; ++cm) {
-          const int64_t xc = (int64_t)cm * n + col;
+          const int64_t xc = (int64_t)cm * cs + col;
           T v[4];
-          ld4<T>(x, xc + k0, cm, v);
+          ldq<T, VEC>(x, xc + k0, cm, v);
           w[cm][0] = ld<T>(x, xc + km, cm);
 #pragma unroll
           for (int e = 0; e < 4; ++e) w[cm][1 + e] = v[e];
@@ -227,6 +240,24 @@ __device__ __forceinline__ void apply4_c(const Geo &S, const T *c, const XS &x, 
         }
       }
     }
+}
+
+template <typename T, int NC, int NR, bool VEC = true, typename Geo, typename XS>
+__device__ __forceinline__ void apply4_c(const Geo &S, const T *c, const XS &x, int d0,
+                                         T (&y)[4][NC * NR]) {
+  if (VEC && S.flags && *reinterpret_cast<const uint32_t *>(S.flags + d0) != 0u) {
+    apply4_per_dof<T, NC, NR, VEC>(S, c, x, d0, y);
+    return;
+  }
+  const Nbr b = neighbours(S, d0);
+  const int k0 = b.zk[1];
+  if (!VEC && (k0 + 4 > S.nz || (S.flags && *reinterpret_cast<const uint32_t *>(S.flags + d0) != 0u))) {
+    apply4_per_dof<T, NC, NR, VEC>(S, c, x, d0, y);
+    return;
+  }
+  const int km = b.zk[0];                                  // k0 - 1 (wrapped)
+  const int kp = (k0 + 4 == S.nz) ? 0 : k0 + 4;            // k0 + 4 (wrapped)
+  quad_columns<T, NC, NR, VEC>(c, x, b.xi, b.yj, k0, km, kp, (int64_t)S.n, y);
 }
 
 // The NC*NR unknowns of the quad d0..d0+3 of a vector, as o[kk][u] (aligned vector accesses).
@@ -251,8 +282,18 @@ __device__ __forceinline__ void quad_load(const T *v, int64_t n, int64_t d0, T (
   }
 }
 
-template <typename T, int NC, int NR>
+template <typename T, int NC, int NR, bool VEC = true>
 __device__ __forceinline__ void quad_store(T *v, int64_t n, int64_t d0, const T (&o)[4][NC * NR]) {
+  if (!VEC) {
+    // scalar stores of the DOFs of the quad inside the grid (any alignment)
+#pragma unroll
+    for (int kk = 0; kk < 4; ++kk)
+      if (d0 + kk < n) {
+#pragma unroll
+        for (int u = 0; u < NC * NR; ++u) v[NC == 3 ? (int64_t)u * n + d0 + kk : (d0 + kk) * NR + u] = o[kk][u];
+      }
+    return;
+  }
   if (NC == 3) {
 #pragma unroll
     for (int cm = 0; cm < 3; ++cm) {
@@ -272,10 +313,28 @@ __device__ __forceinline__ void quad_store(T *v, int64_t n, int64_t d0, const T 
   }
 }
 
-// acc[sys(u)] += v[quad, u] * y[kk][u] over the quad, reading v in aligned groups of 4.
-template <int NC, int NR>
+// acc[sys(u)] += v[quad, u] * y[kk][u] over the quad, reading v in aligned groups
+// of 4 (VEC) or element by element for the DOFs inside the grid.
+template <int NC, int NR, bool VEC = true>
 __device__ __forceinline__ void quad_dot(const float *v, int64_t n, int64_t d0, const float (&y)[4][NC * NR],
                                          float (&acc)[NC == 1 ? NR : 1]) {
+  if (!VEC) {
+    if (NC == 3) {
+#pragma unroll
+      for (int cm = 0; cm < 3; ++cm)
+#pragma unroll
+        for (int kk = 0; kk < 4; ++kk)
+          if (d0 + kk < n) acc[0] = fmaf(v[(int64_t)cm * n + d0 + kk], y[kk][cm], acc[0]);
+    } else {
+#pragma unroll
+      for (int kk = 0; kk < 4; ++kk)
+        if (d0 + kk < n) {
+#pragma unroll
+          for (int r = 0; r < NR; ++r) acc[r] = fmaf(v[(d0 + kk) * NR + r], y[kk][r], acc[r]);
+        }
+    }
+    return;
+  }
   if (NC == 3) {
 #pragma unroll
     for (int cm = 0; cm < 3; ++cm) {

@@ -35,9 +35,14 @@ class BlockSystem:
         return 1 if self.b.dim() == 1 else int(self.b.shape[1])
 
 
-def work_bytes(n, ncomp, nrhs, precision) -> int:
+def work_bytes(dims, ncomp, nrhs, precision) -> int:
+    """Device work bytes of one system on a grid of dims = (nx, ny, nz) cells (cpm_batch_work_bytes)."""
     prec = PRECISIONS[precision] if isinstance(precision, str) else int(precision)
-    return int(N.lib().cpm_batch_work_bytes(int(n), int(ncomp), int(nrhs), prec))
+    nx, ny, nz = (int(v) for v in dims)
+    nb = int(N.lib().cpm_batch_work_bytes(nx, ny, nz, int(ncomp), int(nrhs), prec))
+    if nb <= 0:
+        raise ValueError(f"bad grid {dims} / ncomp {ncomp} / nrhs {nrhs}")
+    return nb
 
 
 def coef_key(op) -> bytes:
@@ -59,7 +64,8 @@ class BlockDiagPlan:
             if s.b.shape[0] != n or s.x.shape != s.b.shape or s.b.dtype != torch.float64 or not s.b.is_contiguous() \
                     or not s.x.is_contiguous():
                 raise ValueError(f"system {i}: b, x must be contiguous float64 of {n} rows")
-            if s.work.numel() < work_bytes(s.op.n, ncomp, nrhs, self.precision) or s.work.data_ptr() % 256:
+            if s.work.numel() < work_bytes((s.op.nx, s.op.ny, s.op.nz), ncomp, nrhs, self.precision) or \
+                    s.work.data_ptr() % 256:
                 raise ValueError(f"system {i}: work buffer too small or not 256-byte aligned")
             e = arr[i]
             e.nx, e.ny, e.nz = s.op.nx, s.op.ny, s.op.nz

@@ -179,7 +179,8 @@ class ServingEngine:
         L = LLGSolver(S, p, precision=self.precision, operators="stencil", info=self.infos[slot])
         L.set_field_schedule(req.fields(p))
         L.set_magnetization(torch.as_tensor(seeded_m0(S.n_dof, S.DefDOF, req.seed)))
-        work = torch.empty(work_bytes(S.n_dof, 3, 1, self.precision), dtype=torch.uint8, device=self.dev)
+        work = torch.empty(work_bytes((p.Nx, p.Ny, p.Nz), 3, 1, self.precision), dtype=torch.uint8,
+                           device=self.dev)
         run = Run(req, L, slot, work, est, now)
         cls = self._cls(L.n)
         g = self.groups.get(cls)
@@ -329,7 +330,13 @@ class ServingEngine:
             # change costs a plan build, an eager step and a graph capture)
             admit_arrived()
             torch.cuda.synchronize(self.dev)
-            g.gpu_s += time.perf_counter() - ts
+            dt = time.perf_counter() - ts
+            g.gpu_s += dt
+            # per size class: seconds, batched steps and run-steps (where the makespan goes)
+            gs = self.stats.extra.setdefault("groups", {}).setdefault(str(g.cls), [0.0, 0, 0])
+            gs[0] += dt
+            gs[1] += 1
+            gs[2] += len(g.runs)
             self._poll(clock(), results, [g])
         st = self.stats
         done = [r for r in results.values() if r.completed > 0]

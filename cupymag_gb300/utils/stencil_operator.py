@@ -68,6 +68,19 @@ class StencilOperator:
                                           N.stream_ptr()), "cpm_stencil_apply")
         return out
 
+    def spmv32(self, x: torch.Tensor, form: int = 2, out: torch.Tensor = None) -> torch.Tensor:
+        """y = A x in FP32 (the refinement form's product); form 0 per DOF, 1 aligned quads, 2 scalar-load quads."""
+        x = x.contiguous()
+        nvec = 1 if x.dim() == 1 else x.shape[1]
+        if x.dtype != torch.float32 or x.shape[0] != self.shape[1] or nvec not in (1, 3) or \
+                (self.ncomp == 3 and nvec != 1):
+            raise ValueError(f"shape/dtype mismatch: {self.shape} @ {tuple(x.shape)} {x.dtype}")
+        if out is None:
+            out = torch.empty_like(x)
+        N.check(N.lib().cpm_stencil_apply32(self.struct(), x.data_ptr(), out.data_ptr(), nvec, int(form),
+                                            N.stream_ptr()), "cpm_stencil_apply32")
+        return out
+
     def __matmul__(self, x):
         return self.spmv(x)
 

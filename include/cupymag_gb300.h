@@ -144,6 +144,14 @@ typedef struct {
 /* y = alpha * A x (FP64); nvec 1 or 3 ((n,nvec) layout) for ncomp = 1. */
 int cpm_stencil_apply(const cpm_stencil *S, const double *x, double *y, double alpha, int nvec, void *stream);
 
+/* y = A x in FP32 with FP32 coefficients: the product of the FP32 refinement
+ * form's inner iterations (the A @ p of the CG loop, cupymag/solvers/CG.py).
+ * form 0: per DOF; 1: quads of 4 DOFs along z with aligned vector loads
+ * (nz % 4 == 0, 4-byte aligned flags, 16-byte aligned x and y); 2: quads
+ * with scalar loads (any nz; 4-byte aligned flags).  Every form gives the
+ * same bits per output. */
+int cpm_stencil_apply32(const cpm_stencil *S, const float *x, float *y, int nvec, int form, void *stream);
+
 /* cpm_cg_solve on a stencil operator: same semantics, options and info;
  * workspace size cpm_cg_workspace_bytes(n * ncomp, nrhs, precision). */
 int cpm_cg_solve_stencil(const cpm_stencil *S, const double *b, double *x, int nrhs, const cpm_cg_opts *opts,
@@ -178,8 +186,8 @@ typedef struct {
   double coef[243];
 } cpm_batch_plan;
 
-/* Work-vector bytes of one system of n DOFs. */
-int64_t cpm_batch_work_bytes(int64_t n, int32_t ncomp, int32_t nrhs, int32_t precision);
+/* Work-vector bytes of one system on an nx x ny x nz grid; 0 for invalid dimensions. */
+int64_t cpm_batch_work_bytes(int32_t nx, int32_t ny, int32_t nz, int32_t ncomp, int32_t nrhs, int32_t precision);
 
 /* Device bytes of the plan for these systems (CTA assignment, partial sums, tables). */
 int cpm_batch_plan_bytes(const cpm_batch_system *sys, int32_t nsys, int32_t ncomp, int32_t nrhs,

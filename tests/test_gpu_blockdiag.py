@@ -34,7 +34,7 @@ def _systems(kind, edges, prec, seed=0, maxiter=20000):
         bd = torch.as_tensor(b, device="cuda").contiguous()
         x = torch.zeros_like(bd)
         info = new_info(1)[0]
-        work = torch.empty(work_bytes(op.n, op.ncomp, nrhs, prec), dtype=torch.uint8, device="cuda")
+        work = torch.empty(work_bytes((op.nx, op.ny, op.nz), op.ncomp, nrhs, prec), dtype=torch.uint8, device="cuda")
         out.append((BlockSystem(op, bd, x, info, work, 1e-10, maxiter), A, b))
     return out
 

@@ -53,6 +53,28 @@ def test_quad_product_is_bitwise_the_per_dof_product(dims):
             assert torch.equal(ya, yv), (name, nvec)
 
 
+@pytest.mark.parametrize("dims", [(8, 8, 8), (6, 5, 12), (7, 5, 9), (5, 6, 11), (6, 7, 5), (9, 4, 3)])
+def test_fp32_quad_forms_are_bitwise_the_per_dof_product(dims):
+    """The FP32 product of the refinement form: scalar-load quads (any nz, quads that cross a z-line end or
+    the end of the grid go per DOF) and, for nz % 4 == 0, aligned quads give the per-DOF bits; all three
+    agree with the FP64 product to FP32 rounding."""
+    S, p = _sim(Nx=dims[0], Ny=dims[1], Nz=dims[2], Ndx=2, Ndy=2, Ndz=2)
+    rng = np.random.default_rng(11)
+    for name, op in S.stencil_operators().items():
+        for nvec in ((1, 3) if op.ncomp == 1 else (1,)):
+            shape = (op.shape[1],) if nvec == 1 else (op.shape[1], nvec)
+            x64 = torch.as_tensor(rng.normal(size=shape), device="cuda")
+            x = x64.float()
+            y0 = op.spmv32(x, form=0)
+            y2 = op.spmv32(x, form=2)
+            assert torch.equal(y0, y2), (name, nvec, dims)
+            if dims[2] % 4 == 0:
+                assert torch.equal(y0, op.spmv32(x, form=1)), (name, nvec, dims)
+            ref = op.spmv(x.double())
+            scale = float(ref.abs().max())
+            assert float((y0.double() - ref).abs().max()) <= 1e-4 * scale, (name, nvec, dims)
+
+
 @pytest.mark.parametrize("edge", [12, 11])
 @pytest.mark.parametrize("prec", ["DP", "IR"])
 def test_stencil_cg_converges_like_csr(prec, edge):
