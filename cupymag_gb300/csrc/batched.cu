@@ -89,7 +89,8 @@ constexpr int kStageDoubles = kStage * 9 * kCGWarps;
 // `stage` and are added and written together, so a chunk costs shuffles but
 // no block barrier.
 template <int NV, typename Body>
-__device__ __forceinline__ void chunk_partials(const BSeg &S, int l, double *half, double *stage, Body body) {
+__device__ __forceinline__ void chunk_partials(const BSeg &S, int l, double *half, double *stage, int nv,
+                                               Body body) {
   static_assert(NV <= 9, "stage holds at most 9 sums per chunk");
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   int held = 0, first = l;
@@ -102,18 +103,20 @@ __device__ __forceinline__ void chunk_partials(const BSeg &S, int l, double *hal
     body(d0, d1, v);
 #pragma unroll
     for (int j = 0; j < NV; ++j) {
+      if (j >= nv) break;
       const double t = warp_sum(v[j]);
       if (lane == 0) stage[(held * NV + j) * kCGWarps + w] = t;
     }
     if (++held == kStage || c + S.ncta >= S.nchunks) {
       __syncthreads();
       for (int t = threadIdx.x; t < held * NV; t += kCGThreads) {
+        const int cl = t / NV, j = t - cl * NV;
+        if (j >= nv) continue;
         const double *src = stage + t * kCGWarps;
         double s = 0.0;
 #pragma unroll
         for (int k = 0; k < kCGWarps; ++k) s += src[k];
-        const int cl = t / NV;
-        half[(size_t)(S.chunk0 + first + cl * S.ncta) * kSlot + (t - cl * NV)] = s;
+        half[(size_t)(S.chunk0 + first + cl * S.ncta) * kSlot + j] = s;
       }
       __syncthreads();
       held = 0;
@@ -122,15 +125,17 @@ __device__ __forceinline__ void chunk_partials(const BSeg &S, int l, double *hal
   }
 }
 
-// One reduction: this CTA's chunk partials (when `work`), a grid barrier, the
-// segment's totals in chunk order.  Every CTA calls it equally often; the
-// partial buffer alternates halves as in grid_sum.
+// One reduction of the first nv of NV values: this CTA's chunk partials (when
+// `work`), a grid barrier, the segment's totals in chunk order (values nv..
+// come back zero).  Every CTA calls it equally often; the partial buffer
+// alternates halves as in grid_sum.
 template <int NV, typename Body>
 __device__ __forceinline__ bool seg_reduce(const BatchArgs &a, const BSeg &S, int l, bool work, int &par,
-                                           double (*sred)[kCGWarps], double *stage, double (&v)[NV], Body body) {
+                                           double (*sred)[kCGWarps], double *stage, double (&v)[NV], Body body,
+                                           int nv = NV) {
   double *half = a.part + (size_t)par * (size_t)a.half;
   par ^= 1;
-  if (work) chunk_partials<NV>(S, l, half, stage, body);
+  if (work) chunk_partials<NV>(S, l, half, stage, nv, body);
   if (!grid_sync(a.bar, gridDim.x, a.timeout_ns)) return false;
   if (work) {
 #pragma unroll
@@ -139,9 +144,10 @@ __device__ __forceinline__ bool seg_reduce(const BatchArgs &a, const BSeg &S, in
     for (int c = threadIdx.x; c < S.nchunks; c += kCGThreads) {
       const double *src = half + (size_t)(S.chunk0 + c) * kSlot;
 #pragma unroll
-      for (int j = 0; j < NV; ++j) v[j] += __ldcg(src + j);
+      for (int j = 0; j < NV; ++j)
+        if (j < nv) v[j] += __ldcg(src + j);
     }
-    block_sum<NV>(v, sred);
+    block_sum<NV>(v, sred, nv);
   }
   return true;
 }
@@ -468,7 +474,7 @@ __global__ void __launch_bounds__(kCGThreads, (NC == 1 && NR == 3) ? 3 : 4) cg_b
               }
             }
           }
-        })) {
+        }, needm ? 3 * NS : NS)) {  // t.t and t.p only on an iteration with a pending update
       status = CPM_BARRIER_TIMEOUT;
       break;
     }

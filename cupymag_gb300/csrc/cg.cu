@@ -364,7 +364,11 @@ __global__ void __launch_bounds__(kCGThreads) cg_ir_kernel(CGArgs<NR, IT> a) {
         }
       }
     }
-    if (!grid_sum<3 * NR>(pt, a.part, par, a.bar, tns, s_red)) { status = CPM_BARRIER_TIMEOUT; break; }
+    // t.t and t.p only on an iteration with a pending update (FP64 adds are slow on GB300)
+    if (!grid_sum<3 * NR>(pt, a.part, par, a.bar, tns, s_red, needm ? 3 * NR : NR)) {
+      status = CPM_BARRIER_TIMEOUT;
+      break;
+    }
     if (threadIdx.x == 0) {
       int am = 0, bad = 0;
       for (int j = 0; j < NR; ++j) {

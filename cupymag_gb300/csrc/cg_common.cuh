@@ -10,51 +10,64 @@ constexpr int kCGWarps = kCGThreads / kWarp;
 constexpr int kMaxGrid = 4096;                 // CTAs of one cooperative launch (upper bound)
 constexpr size_t kPartHalf = (size_t)9 * kMaxGrid;  // doubles per half of the partials buffer (<= 9 sums per CTA)
 
-// Block-wide sum of NV values per thread over NW warps, deterministic; result broadcast.
+// Block-wide sum of the first nv of NV values per thread over NW warps,
+// deterministic; result broadcast (values nv.. are left as they are).  A
+// GB300 SM issues FP64 adds at about 1/64 of its FP32 rate (one warp
+// instruction holds the FP64 pipe for ~64 cycles), so the reductions count
+// FP64 instructions: they skip values not in use, and one thread per value
+// adds the warp sums (in warp order) for the whole block.
 template <int NV, int NW>
-__device__ __forceinline__ void block_sum(double (&v)[NV], double (*s)[NW]) {
+__device__ __forceinline__ void block_sum(double (&v)[NV], double (*s)[NW], int nv = NV) {
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
 #pragma unroll
   for (int j = 0; j < NV; ++j) {
-    double t = warp_sum(v[j]);
+    if (j >= nv) break;
+    const double t = warp_sum(v[j]);
     if (lane == 0) s[j][w] = t;
+  }
+  __syncthreads();
+  if (threadIdx.x < nv) {
+    double t = 0.0;
+#pragma unroll
+    for (int k = 0; k < NW; ++k) t += s[threadIdx.x][k];
+    s[threadIdx.x][0] = t;
   }
   __syncthreads();
 #pragma unroll
   for (int j = 0; j < NV; ++j) {
-    double t = 0.0;
-#pragma unroll
-    for (int k = 0; k < NW; ++k) t += s[j][k];
-    v[j] = t;
+    if (j >= nv) break;
+    v[j] = s[j][0];
   }
   __syncthreads();
 }
 
-// Write this CTA's NV partials, barrier, and reduce all CTAs' partials.
-// The partials buffer alternates between two halves: a CTA may start writing
-// the next reduction's partials while slower CTAs still read this one's, and
-// the barrier of the next reduction orders the reuse of a half.
+// Write this CTA's partials of the first nv of NV values, barrier, and reduce
+// all CTAs' partials.  The partials buffer alternates between two halves: a
+// CTA may start writing the next reduction's partials while slower CTAs still
+// read this one's, and the barrier of the next reduction orders the reuse of
+// a half.
 template <int NV, int NW>
 __device__ __forceinline__ bool grid_sum(double (&v)[NV], double *part, int &parity, GridBarrier *bar,
-                                         unsigned long long tns, double (*s)[NW]) {
-  block_sum<NV>(v, s);
+                                         unsigned long long tns, double (*s)[NW], int nv = NV) {
+  block_sum<NV>(v, s, nv);
   const int G = gridDim.x;
   part += (size_t)parity * kPartHalf;
   parity ^= 1;
 #pragma unroll
   for (int j = 0; j < NV; ++j)
-    if (threadIdx.x == j) part[(size_t)blockIdx.x * NV + j] = v[j];
+    if (threadIdx.x == j && j < nv) part[(size_t)blockIdx.x * NV + j] = v[j];
   if (!grid_sync(bar, G, tns)) return false;
   double acc[NV];
 #pragma unroll
   for (int j = 0; j < NV; ++j) acc[j] = 0.0;
   for (int g = threadIdx.x; g < G; g += blockDim.x) {
 #pragma unroll
-    for (int j = 0; j < NV; ++j) acc[j] += __ldcg(&part[(size_t)g * NV + j]);
+    for (int j = 0; j < NV; ++j)
+      if (j < nv) acc[j] += __ldcg(&part[(size_t)g * NV + j]);
   }
-  block_sum<NV>(acc, s);
+  block_sum<NV>(acc, s, nv);
 #pragma unroll
-  for (int j = 0; j < NV; ++j) v[j] = acc[j];
+  for (int j = 0; j < NV; ++j) v[j] = j < nv ? acc[j] : 0.0;
   return true;
 }
 

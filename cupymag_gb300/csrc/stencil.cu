@@ -332,7 +332,11 @@ __global__ void __launch_bounds__(kIRThreads, 4) cg_stencil_ir_kernel(const __gr
         }
       }
     }
-    if (!grid_sum<3 * NS>(pt, a.part, par, a.bar, tns, s_red)) { status = CPM_BARRIER_TIMEOUT; break; }
+    // t.t and t.p only on an iteration with a pending update (FP64 adds are slow on GB300)
+    if (!grid_sum<3 * NS>(pt, a.part, par, a.bar, tns, s_red, needm ? 3 * NS : NS)) {
+      status = CPM_BARRIER_TIMEOUT;
+      break;
+    }
     if (threadIdx.x == 0) {
       int am = 0, bad = 0;
       for (int j = 0; j < NS; ++j) {
