@@ -10,29 +10,33 @@ constexpr int kCGWarps = kCGThreads / kWarp;
 constexpr int kMaxGrid = 4096;                 // CTAs of one cooperative launch (upper bound)
 constexpr size_t kPartHalf = (size_t)9 * kMaxGrid;  // doubles per half of the partials buffer (<= 9 sums per CTA)
 
-// Block-wide sum of the first nv of NV values per thread over NW warps,
-// deterministic; result broadcast (values nv.. are left as they are).  A
-// GB300 SM issues FP64 adds at about 1/64 of its FP32 rate (one warp
+// Block-wide sum of the first nv of NV values per thread, deterministic;
+// result broadcast (values nv.. are left as they are; s[j][0] holds total j).
+// A GB300 SM issues FP64 adds at about 1/64 of its FP32 rate (one warp
 // instruction holds the FP64 pipe for ~64 cycles), so the reductions count
-// FP64 instructions: they skip values not in use, and one thread per value
-// adds the warp sums (in warp order) for the whole block.
+// FP64 instructions: they skip values not in use, and one warp adds a
+// block's values (13 FP64 warp instructions per value, where shuffles in
+// every warp and a per-thread sum of the warp sums took 48).
 template <int NV, int NW>
 __device__ __forceinline__ void block_sum(double (&v)[NV], double (*s)[NW], int nv = NV) {
-  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  // per value: every thread stores its value, one warp adds 8 per lane (threads
+  // 8l..8l+7, in order) and then the 32 lane sums with a fixed shuffle tree
+  __shared__ double s_all[kCGThreads];
+  const int lane = threadIdx.x & 31;
 #pragma unroll
   for (int j = 0; j < NV; ++j) {
     if (j >= nv) break;
-    const double t = warp_sum(v[j]);
-    if (lane == 0) s[j][w] = t;
-  }
-  __syncthreads();
-  if (threadIdx.x < nv) {
-    double t = 0.0;
+    s_all[threadIdx.x] = v[j];
+    __syncthreads();
+    if (threadIdx.x < kWarp) {
+      double t = 0.0;
 #pragma unroll
-    for (int k = 0; k < NW; ++k) t += s[threadIdx.x][k];
-    s[threadIdx.x][0] = t;
+      for (int k = 0; k < kCGThreads / kWarp; ++k) t += s_all[lane * (kCGThreads / kWarp) + k];
+      t = warp_sum(t);
+      if (lane == 0) s[j][0] = t;
+    }
+    __syncthreads();
   }
-  __syncthreads();
 #pragma unroll
   for (int j = 0; j < NV; ++j) {
     if (j >= nv) break;
