@@ -145,7 +145,8 @@ typedef struct {
 int cpm_stencil_apply(const cpm_stencil *S, const double *x, double *y, double alpha, int nvec, void *stream);
 
 /* y = A x in FP32 with FP32 coefficients: the product of the FP32 refinement
- * form's inner iterations (the A @ p of the CG loop, cupymag/solvers/CG.py).
+ * form's inner iterations (the A @ p of the cupyx CG that solve_cg calls,
+ * cupymag/solvers/linear_solvers.py:60-62).
  * form 0: per DOF; 1: quads of 4 DOFs along z with aligned vector loads
  * (nz % 4 == 0, 4-byte aligned flags, 16-byte aligned x and y); 2: quads
  * with scalar loads (any nz; 4-byte aligned flags).  Every form gives the
