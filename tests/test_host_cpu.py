@@ -188,6 +188,43 @@ def test_library_exports_every_header_symbol():
     assert lib.cpm_cg_workspace_bytes(1000, 3, 1) > lib.cpm_cg_workspace_bytes(10, 1, 1)
 
 
+def test_batch_work_bytes_follow_the_grid():
+    """cpm_batch_work_bytes sizes a system's work vectors from its grid (host arithmetic, no GPU)."""
+    from cupymag_gb300 import _native as N
+    from cupymag_gb300.build import build
+    from cupymag_gb300.serving.blockdiag import work_bytes
+    build()
+    N.load()
+    al = lambda b: (b + 255) // 256 * 256  # noqa: E731
+    assert work_bytes((10, 11, 12), 3, 1, "IR") == 4 * al(10 * 11 * 12 * 3 * 4)   # r, p, q, d in FP32
+    assert work_bytes((10, 11, 12), 1, 3, "DP") == 3 * al(10 * 11 * 12 * 3 * 8)   # r, p, q in FP64
+    assert work_bytes((9, 9, 9), 1, 1, "IR") == 4 * al(729 * 4)
+    for dims, ncomp, nrhs in (((0, 4, 4), 1, 1), ((4, 4, 4), 2, 1), ((4, 4, 4), 1, 2)):
+        with pytest.raises(ValueError):
+            work_bytes(dims, ncomp, nrhs, "IR")
+
+
+def test_fp32_product_rejects_what_its_form_cannot_take():
+    """cpm_stencil_apply32 checks its arguments on the host before any launch (no GPU needed)."""
+    from cupymag_gb300 import _native as N
+    from cupymag_gb300.build import build
+    build()
+    lib = N.load()
+    s = N.Stencil()
+    s.nx, s.ny, s.nz, s.ncomp = 5, 5, 7, 1
+    s.flags = None
+    fake = 1 << 20  # a device address that the rejected calls never touch
+    assert lib.cpm_stencil_apply32(s, fake, fake, 1, 1, None) == N.CPM_BAD_ARG   # nz = 7: no aligned quads
+    assert "form 1 needs nz % 4 == 0" in N.last_error()
+    for nvec, form in ((1, 3), (1, -1), (2, 0)):
+        assert lib.cpm_stencil_apply32(s, fake, fake, nvec, form, None) == N.CPM_BAD_ARG, (nvec, form)
+    s.ncomp = 3
+    assert lib.cpm_stencil_apply32(s, fake, fake, 3, 0, None) == N.CPM_BAD_ARG   # elastic takes one vector
+    s.nz = 2
+    assert lib.cpm_stencil_apply32(s, fake, fake, 1, 0, None) == N.CPM_BAD_ARG   # fewer than 3 cells
+    assert lib.cpm_stencil_apply32(None, fake, fake, 1, 0, None) == N.CPM_BAD_ARG
+
+
 # ------------------------------------------------------------------ serving (host side)
 def test_serving_workload_shape():
     from cupymag_gb300.serving.workload import serving_requests
