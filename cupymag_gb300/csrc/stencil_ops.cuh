@@ -131,22 +131,8 @@ __device__ __forceinline__ void apply_c(const Geo &S, const T *c, const XS &x, i
 }
 
 // ---------------------------------------------------------------- four DOFs along z
-// Register-blocked application to the quad of DOFs d0..d0+3 (d0 % 4 == 0).
-// When the quad lies in one z-line (at k0..k0+3), each of the 9 (x, y)
-// neighbour columns is read once per component as 4 consecutive values plus
-// the two wrapped edge values k0-1 and k0+4, and serves all three z offsets
-// of all four DOFs: 6 loads where the per-DOF form makes 12.  The FMAs run in
-// the per-DOF order (neighbour d = (dx, dy, dz) lexicographic, then
-// components), so every y is bit-identical to apply_c's.  A quad with a
-// flagged DOF (unit / empty row or a neighbour of an excluded column) takes
-// apply_c per DOF.
-//
-// VEC: nz % 4 == 0 and 16-byte aligned operands, so every quad lies in one
-// z-line and each group of 4 is one aligned vector load.  Otherwise (any nz)
-// the groups of 4 are scalar loads, and a quad that crosses the end of its
-// z-line takes apply_c per DOF; outputs past the end of the grid are zero.
-// The quad DOF by DOF (flagged quads; for the scalar form also quads that
-// leave their z-line); outputs past the end of the grid are zero.
+// The quad DOF by DOF (flagged quads; for the scalar form of apply4_c also
+// quads that leave their z-line); outputs past the end of the grid are zero.
 template <typename T, int NC, int NR, bool VEC, typename Geo, typename XS>
 __device__ __forceinline__ void apply4_per_dof(const Geo &S, const T *c, const XS &x, int d0,
                                                T (&y)[4][NC * NR]) {
@@ -242,6 +228,23 @@ __device__ __forceinline__ void quad_columns(const T *c, const XS &x, const int 
     }
 }
 
+// Register-blocked application to the quad of DOFs d0..d0+3 (d0 % 4 == 0).
+// When the quad lies in one z-line (at k0..k0+3), each of the 9 (x, y)
+// neighbour columns is read once per component as 4 consecutive values plus
+// the two wrapped edge values k0-1 and k0+4, and serves all three z offsets
+// of all four DOFs: 6 loads where the per-DOF form makes 12.  The FMAs run in
+// the per-DOF order (neighbour d = (dx, dy, dz) lexicographic, then
+// components), so every y is bit-identical to apply_c's.  A quad with a
+// flagged DOF (unit / empty row or a neighbour of an excluded column) takes
+// apply_c per DOF.
+//
+// VEC: nz % 4 == 0 and 16-byte aligned operands, so every quad lies in one
+// z-line and each group of 4 is one aligned vector load; the solvers use this
+// form.  Otherwise (any nz) the groups of 4 are scalar loads and a quad that
+// crosses the end of its z-line takes apply_c per DOF.  On GB300 the scalar
+// form is slower than the per-DOF product (each lane's loads are 16 bytes
+// apart, so every load instruction moves four cache lines through L1); only
+// the FP32 product entry point offers it.
 template <typename T, int NC, int NR, bool VEC = true, typename Geo, typename XS>
 __device__ __forceinline__ void apply4_c(const Geo &S, const T *c, const XS &x, int d0,
                                          T (&y)[4][NC * NR]) {
