@@ -149,3 +149,32 @@ def test_driver_sweep_matches_reference_main():
     np.testing.assert_array_equal(rows[:, :3], g["hysteresis"][:, :3])
     np.testing.assert_allclose(rows[:, 3:], g["hysteresis"][:, 3:], rtol=0, atol=1e-14)
     np.testing.assert_allclose(m, g["final_m"], rtol=0, atol=1e-14)
+
+
+def test_threaded_operators_give_the_oracle_step_bit_for_bit():
+    """The CPU baseline's row-blocked threaded products (oracle/threaded.py) leave the oracle's step
+    bit-identical to the single-threaded one, and the blocks share the matrix's arrays."""
+    import oracle.llg as OL
+    from oracle.threaded import threaded_operators
+    from oracle.volume_average import VolumeAverage as OVA
+    from cupymag_gb300.core.assemble_simulation_operators import SimulationOperators
+    from cupymag_gb300.workloads import seeded_m0
+
+    p = G.params(G.load("hex_me_rot"))
+    S = SimulationOperators(p, device="cpu")
+    ops = S.host_operators()
+    tops, pool, threads = threaded_operators(ops, 4)
+    try:
+        blk = tops["A_el"].blocks[-1][2]
+        assert np.shares_memory(blk.data, ops["A_el"].data)
+        Avg = OVA(S.node_coords_np, S.elements_np, S.global_id_np)
+        m0 = seeded_m0(S.n_dof, S.DefDOF, seed=5)
+        out = []
+        for o in (ops, tops):
+            st = OL.LLGState(m0.copy(), Avg.average)
+            for _ in range(2):
+                OL.llg_step(st, o, Avg.average, p, p.Hext, S.DefDOF)
+            out.append(st.m.copy())
+        assert np.array_equal(out[0], out[1])
+    finally:
+        pool.shutdown()
