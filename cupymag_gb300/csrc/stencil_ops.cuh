@@ -263,28 +263,8 @@ __device__ __forceinline__ void apply4_c(const Geo &S, const T *c, const XS &x, 
   quad_columns<T, NC, NR, VEC>(c, x, b.xi, b.yj, k0, km, kp, (int64_t)S.n, y);
 }
 
-// The NC*NR unknowns of the quad d0..d0+3 of a vector, as o[kk][u] (aligned vector accesses).
-template <typename T, int NC, int NR>
-__device__ __forceinline__ void quad_load(const T *v, int64_t n, int64_t d0, T (&o)[4][NC * NR]) {
-  if (NC == 3) {
-#pragma unroll
-    for (int cm = 0; cm < 3; ++cm) {
-      T t[4];
-      Vec4<T>::load(v + cm * n + d0, t);
-#pragma unroll
-      for (int kk = 0; kk < 4; ++kk) o[kk][cm] = t[kk];
-    }
-  } else {
-#pragma unroll
-    for (int h = 0; h < NR; ++h) {
-      T t[4];
-      Vec4<T>::load(v + d0 * NR + 4 * h, t);
-#pragma unroll
-      for (int e = 0; e < 4; ++e) o[(4 * h + e) / NR][(4 * h + e) % NR] = t[e];
-    }
-  }
-}
-
+// The NC*NR unknowns o[kk][u] of the quad d0..d0+3 into a vector (aligned vector stores, or scalar
+// stores of the DOFs inside the grid).
 template <typename T, int NC, int NR, bool VEC = true>
 __device__ __forceinline__ void quad_store(T *v, int64_t n, int64_t d0, const T (&o)[4][NC * NR]) {
   if (!VEC) {

@@ -12,8 +12,6 @@ from __future__ import annotations
 
 import numpy as np
 
-from .engine import estimate_bytes
-
 
 def request_work(req) -> float:
     """Relative cost of a request: steps x DOFs x (elastic solve weight when coupled)."""
@@ -64,8 +62,3 @@ def combine_stats(stats, latencies, group=None):
             "makespan_s": makespan, "steps_per_s": steps / makespan if makespan > 0 else 0.0,
             "latency_p50_s": float(np.percentile(lat, 50)) if lat.size else 0.0,
             "latency_p99_s": float(np.percentile(lat, 99)) if lat.size else 0.0, "ranks": world}
-
-
-def fits_budget(requests, hbm_budget_gb, precision="IR"):
-    """Requests whose estimated device bytes exceed the per-GPU budget (they are rejected by the engine)."""
-    return [r for r in requests if estimate_bytes(r.params(), precision) > hbm_budget_gb * 1e9]
