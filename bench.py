@@ -45,6 +45,20 @@ REFERENCE_ITERS = {"hex128_me": [1930, 375, 22, 30, 30, 22, 29, 30, 44, 44],
                    "hex32_plain": [95, 22, 30, 30, 22, 29, 30, 44, 44]}
 
 
+def elastic_launch_traffic(n_dof, elastic, steps):
+    """DRAM bytes per elasticity-solve launch (ncu bytes per unknown-iteration x this run's iterations)
+    and a description with the algorithmic bytes of the same launch; elastic = [bytes, ms, iterations]
+    summed over `steps` steps."""
+    its = elastic[2] / steps
+    traffic = float(round(IR_STENCIL_DRAM_BYTES_PER_UNKNOWN_ITER * 3 * n_dof * its))
+    detail = {"unit": "bytes per elasticity launch", "launch_iterations": round(its, 1),
+              "algorithmic_bytes_per_launch": float(round(elastic[0] / steps)),
+              "source": f"ncu dram__bytes_read.sum + dram__bytes_write.sum per unknown-iteration "
+                        f"({IR_STENCIL_DRAM_BYTES_PER_UNKNOWN_ITER} B, profiles/cg_batched_vs_single__A_el_hex128.md) "
+                        f"x 3 n unknowns x this run's iterations"}
+    return traffic, detail
+
+
 def peaks():
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
@@ -162,10 +176,11 @@ def stencil_launch_bytes(A, nvec, iters, outer, fp32):
 
 
 # DRAM bytes (read + write) per unknown and iteration of the FP32 stencil CG, measured with ncu on a GB300
-# (dram__bytes_read.sum + dram__bytes_write.sum of a 300-iteration elastic 128^3 launch / (300 x unknowns));
-# the vectors fit the L2 about half way, so this is below the 44 algorithmic bytes.  Traffic of a launch
-# is this figure times its unknowns and iterations (it grows in proportion at a fixed grid size).
-IR_STENCIL_DRAM_BYTES_PER_UNKNOWN_ITER = 23.0
+# (dram__bytes_read.sum + dram__bytes_write.sum of a 300-iteration elastic 128^3 launch / (300 x unknowns):
+# (10.91 + 28.00) GB / 300 / 6.29 M for the current kernel); the vectors fit the L2 about half way, so this
+# is below the 44 algorithmic bytes.  Traffic of a launch is this figure times its unknowns and iterations
+# (it grows in proportion at a fixed grid size).
+IR_STENCIL_DRAM_BYTES_PER_UNKNOWN_ITER = 20.6
 
 
 def cg_launch_bytes(A, nvec, iters, warm):
@@ -399,15 +414,13 @@ def run_ours(args):
     achieved = tot_bytes / (tot_ms / 1e3) / 1e9
     kname = {("csr", "DP"): "cg_fp64_kernel", ("csr", "IR"): "cg_ir_kernel",
              ("stencil", "DP"): "cg_stencil_fp64_kernel", ("stencil", "IR"): "cg_stencil_ir_kernel"}[(ops_kind, args.precision)]
-    traffic = None
+    traffic, traffic_detail = None, None
     if kname == "cg_stencil_ir_kernel" and "elasticity" in dom and args.workload == "hex128_me":
-        # per elasticity launch, scaled from the ncu capture of the same kernel on this grid
-        traffic = {"bytes_per_launch": round(IR_STENCIL_DRAM_BYTES_PER_UNKNOWN_ITER * 3 * S.n_dof *
-                                             dom["elasticity"][2] / args.steps / 1e9, 2), "unit": "GB",
-                   "source": "ncu dram bytes per unknown-iteration x this run's elasticity iterations"}
+        # DRAM bytes per elasticity launch, scaled from the ncu capture of the same kernel on this grid
+        traffic, traffic_detail = elastic_launch_traffic(S.n_dof, dom["elasticity"], args.steps)
     roof = {"kernel": kname, "bound": "hbm",
             "achieved": round(achieved, 1), "peak": peak, "peak_kind": peak_kind, "unit": "GB/s",
-            "frac": round(achieved / peak, 4), "traffic": traffic,
+            "frac": round(achieved / peak, 4), "traffic": traffic, "traffic_detail": traffic_detail,
             "share_of_step": round(tot_ms / ms, 4),
             "per_solve": {k: {"GB/s": round(v[0] / (v[1] / 1e3) / 1e9, 1), "ms": round(v[1] / args.steps, 3),
                               "iters": round(v[2] / args.steps, 1)} for k, v in dom.items()}}
