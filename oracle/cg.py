@@ -20,7 +20,13 @@ with the residual ||b - A x|| when info != 0 (linear_solvers.py:59-74).
 import numpy as np
 
 
-def cg(A, b, x0=None, tol=1e-5, maxiter=None, record=None):
+def _axpy(x, a, y):
+    return x + a * y
+
+
+def cg(A, b, x0=None, tol=1e-5, maxiter=None, record=None, axpy=None):
+    """axpy(x, a, y) -> x + a * y (element-wise; a threaded one must round the same way)."""
+    axpy = axpy or _axpy
     n = A.shape[0]
     if maxiter is None:
         maxiter = n * 10
@@ -42,11 +48,11 @@ def cg(A, b, x0=None, tol=1e-5, maxiter=None, record=None):
         if iters == 0:
             p = r.copy()
         else:
-            p = r + (rho / rho1) * p
+            p = axpy(r, rho / rho1, p)
         q = A @ p
         alpha = rho / np.dot(p, q)
-        x = x + alpha * p
-        r = r - alpha * q
+        x = axpy(x, alpha, p)
+        r = axpy(r, -alpha, q)
         iters += 1
         resid = np.linalg.norm(r)
         if resid <= atol:

@@ -56,6 +56,28 @@ class ThreadedCSR:
         return self @ x
 
 
+class ThreadedAxpy:
+    """x + a * y in row blocks on a pool: element by element the same multiply and add as NumPy's
+    `x + a * y` (and `x - a * y` as a = -a), so the result is bit-identical."""
+
+    def __init__(self, pool: ThreadPoolExecutor, threads: int):
+        self.pool = pool
+        self.threads = max(1, threads)
+
+    def __call__(self, x, a, y):
+        n = x.shape[0]
+        out = np.empty_like(x)
+        bounds = np.linspace(0, n, self.threads + 1).astype(np.int64)
+
+        def run(k):
+            lo, hi = int(bounds[k]), int(bounds[k + 1])
+            np.multiply(y[lo:hi], a, out=out[lo:hi])
+            np.add(x[lo:hi], out[lo:hi], out=out[lo:hi])
+
+        list(self.pool.map(run, range(self.threads)))
+        return out
+
+
 def host_threads() -> int:
     """Host cores this process may run on."""
     try:

@@ -152,8 +152,9 @@ def test_driver_sweep_matches_reference_main():
 
 
 def test_threaded_operators_give_the_oracle_step_bit_for_bit():
-    """The CPU baseline's row-blocked threaded products (oracle/threaded.py) leave the oracle's step
-    bit-identical to the single-threaded one, and the blocks share the matrix's arrays."""
+    """The CPU baseline's row-blocked threaded products and CG updates (oracle/threaded.py) leave the
+    oracle's step and CG bit-identical to the single-threaded ones, and the blocks share the matrix's
+    arrays."""
     import oracle.llg as OL
     from oracle.threaded import threaded_operators
     from oracle.volume_average import VolumeAverage as OVA
@@ -176,5 +177,13 @@ def test_threaded_operators_give_the_oracle_step_bit_for_bit():
                 OL.llg_step(st, o, Avg.average, p, p.Hext, S.DefDOF)
             out.append(st.m.copy())
         assert np.array_equal(out[0], out[1])
+        # the CG with threaded element-wise updates, as the CPU baseline runs it
+        from oracle.cg import cg
+        from oracle.threaded import ThreadedAxpy
+        b = np.random.default_rng(3).standard_normal(ops["A_el"].shape[0])
+        b[[0, S.n_dof, 2 * S.n_dof]] = 0.0
+        x1, i1 = cg(ops["A_el"], b, tol=1e-10, maxiter=400)
+        x2, i2 = cg(tops["A_el"], b, tol=1e-10, maxiter=400, axpy=ThreadedAxpy(pool, threads))
+        assert i1 == i2 and np.array_equal(x1, x2)
     finally:
         pool.shutdown()
