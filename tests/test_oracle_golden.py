@@ -187,3 +187,24 @@ def test_threaded_operators_give_the_oracle_step_bit_for_bit():
         assert i1 == i2 and np.array_equal(x1, x2)
     finally:
         pool.shutdown()
+
+
+def test_threaded_csr_with_64_bit_indices():
+    """Row blocks of a CSR matrix with int64 indices (F_el at 192^3 needs them) keep the index type and
+    the product's bits."""
+    import scipy.sparse as sp
+    from concurrent.futures import ThreadPoolExecutor
+    from oracle.threaded import ThreadedCSR
+    rng = np.random.default_rng(4)
+    n, k = 5000, 7
+    A = sp.csr_matrix((rng.standard_normal(n * k), rng.integers(0, n, n * k), np.arange(0, n * k + 1, k)),
+                      shape=(n, n))
+    A.indices = A.indices.astype(np.int64)
+    A.indptr = A.indptr.astype(np.int64)
+    with ThreadPoolExecutor(3) as pool:
+        T = ThreadedCSR(A, pool, 3)
+        assert all(b[2].indptr.dtype == np.int64 and b[2].indices.dtype == np.int64 for b in T.blocks)
+        x = rng.standard_normal(n)
+        X = rng.standard_normal((n, 3))
+        assert np.array_equal(T @ x, A @ x) and np.array_equal(T @ X, A @ X)
+
