@@ -1,24 +1,30 @@
 """Benchmark: LLG steps/s of the GSPM step on one GB300 (replicas across GPUs).
 
 Default workload: 128^3 hex with magnetoelastic coupling and the [111]
-rotation (plain FP64), the configuration the headline metric is quoted on.
-A "step" is one Gauss-Seidel-projection LLG step at the next field of the
-500-step sweep, with all operators and state resident in HBM.
+rotation (cfg "hex128_me"), in the precision form: FP32 CG with FP64
+reliable updates on the matrix-free stencil operators.  A "step" is one
+Gauss-Seidel-projection LLG step at the next field of the 500-step sweep,
+with all operators and state resident in HBM.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--workload NAME]
-                  [--precision DP|IR] [--impl ours|reference]
+                  [--precision DP|IR] [--operators csr|stencil] [--impl ours|reference]
 
 value:  steps/s over K steps timed with CUDA events (device-resident inputs;
-        operators of 18 GB > L2, so no flush is needed); max over ranks.
+        about 12.9 GB resident at 128^3, far above the L2, so no flush is
+        needed); max over ranks.
 e2e:    the same steps through the public API with the magnetisation copied in
         from pinned host memory and the new m and <m> read back every step.
-roofline: the persistent CG kernel (dominant): algorithmic bytes per launch
-        (B_spmv + iterations * (B_spmv + 6 n s)) / measured launch time.
+fp64:   the same steps from the same m0 in plain FP64 on the same GPU, with
+        max |m - m_FP64| and the relative <m> error.
+roofline: the CG launches (dominant kernel): algorithmic bytes per launch
+        (stencil CG: 44 B per unknown-iteration in FP32, 88 B in FP64) / the
+        CUDA-event launch time, against MEASURED_PEAKS.json.
+serving: a sample of the 256-request serving stream through the engine,
+        beside the same requests run one at a time in plain FP64.
 cpu_baseline: the CPU oracle (NumPy/SciPy restatement of the reference's step)
-        sampled on this machine's host cores: one step with every CG capped at 3
-        iterations, timed per solve, extrapolated with this run's iteration counts.
---impl reference: the same CPU sample as the whole measurement (the reference
-        itself needs CuPy + a CUDA GPU and is Python; its CPU path is the oracle).
+        on this machine's host cores.
+--impl reference: the oracle's CPU step as the whole measurement (the
+        reference itself needs CuPy and a CUDA GPU; its CPU path is the oracle).
 Multi-GPU: independent replicas (one per rank, no collective on the data path).
 """
 from __future__ import annotations
@@ -54,8 +60,8 @@ def elastic_launch_traffic(n_dof, elastic, steps):
     detail = {"unit": "bytes per elasticity launch", "launch_iterations": round(its, 1),
               "algorithmic_bytes_per_launch": float(round(elastic[0] / steps)),
               "source": f"ncu dram__bytes_read.sum + dram__bytes_write.sum per unknown-iteration "
-                        f"({IR_STENCIL_DRAM_BYTES_PER_UNKNOWN_ITER} B, profiles/cg_batched_vs_single__A_el_hex128.md) "
-                        f"x 3 n unknowns x this run's iterations"}
+                        f"({IR_STENCIL_DRAM_BYTES_PER_UNKNOWN_ITER} B, one capture of a 300-iteration elastic "
+                        f"128^3 launch) x 3 n unknowns x this run's iterations"}
     return traffic, detail
 
 

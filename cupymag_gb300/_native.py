@@ -15,6 +15,8 @@ _lock = threading.Lock()
 _lib = None
 
 CPM_OK, CPM_NOT_CONVERGED, CPM_BARRIER_TIMEOUT, CPM_NONFINITE, CPM_BAD_ARG, CPM_CUDA_ERROR = range(6)
+# iteration forms of the FP32 stencil CG (cpm_cg_opts.form)
+CG_FORM_DEFAULT, CG_FORM_THREE_BARRIER, CG_FORM_TWO_BARRIER = 0, 1, 2
 STATUS_NAMES = {0: "ok", 1: "not converged", 2: "grid barrier timeout", 3: "non-finite value", 4: "bad argument",
                 5: "CUDA error"}
 
@@ -40,7 +42,7 @@ class CGInfo(C.Structure):
 
 class CGOpts(C.Structure):
     _fields_ = [("tol", dbl), ("maxiter", i32), ("use_init_host", i32), ("use_init_dev", vp), ("precision", i32),
-                ("inner_tol", dbl), ("max_outer", i32), ("pad", i32), ("barrier_timeout_s", dbl)]
+                ("inner_tol", dbl), ("max_outer", i32), ("form", i32), ("barrier_timeout_s", dbl)]
 
 
 class FieldParams(C.Structure):

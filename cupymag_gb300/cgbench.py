@@ -3,6 +3,7 @@
     python -m cupymag_gb300.cgbench [--edge 128] [--op A_el|A_demag|A1|A2] [--nrhs 1|3]
                                     [--precision IR|DP] [--operators stencil|csr]
                                     [--solves 3] [--maxiter 20000] [--batch 1] [--batched]
+                                    [--form 0|1|2]
 
 Builds only the requested operator (the magnetoelastic 128^3 material), a
 seeded right-hand side with the reference's pins (b[0] = 0 for A_demag,
@@ -47,6 +48,8 @@ def main(argv=None):
                     help="solve through the block-diagonal (serving) kernel even for --batch 1")
     ap.add_argument("--inner-tol", type=float, default=0.1,
                     help="reliable-update factor of the FP32 solver (residual drop between FP64 updates)")
+    ap.add_argument("--form", type=int, default=0, choices=[0, 1, 2],
+                    help="FP32 stencil solver: 0 default (two barriers), 1 three-barrier, 2 two-barrier")
     args = ap.parse_args(argv)
 
     from . import _native as N
@@ -94,7 +97,8 @@ def main(argv=None):
         info = new_info(1)
 
         def launch():
-            solver.launch(op, bd, x, info[0], tol=p.tol, maxiter=args.maxiter, precision=args.precision)
+            solver.launch(op, bd, x, info[0], tol=p.tol, maxiter=args.maxiter, precision=args.precision,
+                          form=args.form)
         info_of = lambda: info[0]  # noqa: E731
     for _ in range(args.solves):
         e0 = torch.cuda.Event(enable_timing=True)
@@ -111,7 +115,7 @@ def main(argv=None):
     ms = float(np.median(times))
     nb = _bytes(op, nrhs, its, d["outer"], args.precision == "IR", csr) * args.batch
     print(json.dumps({"op": args.op, "edge": args.edge, "n": n, "nrhs": nrhs, "precision": args.precision,
-                      "inner_tol": args.inner_tol,
+                      "inner_tol": args.inner_tol, "form": args.form,
                       "operators": args.operators, "batch": args.batch,
                       "kernel": "blockdiag" if args.batch > 1 or args.batched else "single",
                       "status": N.STATUS_NAMES[d["status"]],

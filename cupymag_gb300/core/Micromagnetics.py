@@ -30,13 +30,14 @@ from .parameters import load_parameters
 def run(params, fields=None, max_steps=None, precision=None, verbose=True, device=None):
     from ..physics.llg import LLGSolver
     from ..utils.magnetization_io import initialize_m, write_array
+    from ..utils.precision_select import solver_precision
 
     p = params
     out_dir = p.output_dir or "."
     os.makedirs(out_dir, exist_ok=True)
     t_start = time.time()
     S = SimulationOperators(p, device=device)
-    prec = precision or ("DP" if p.precision == "DP" else "IR")
+    prec = precision or solver_precision(p.precision)
     L = LLGSolver(S, p, precision=prec)
     m0 = initialize_m(p.restart_m, p.restart, p.initial_magnetization, S.n_dof, S.DefDOF)
     L.set_magnetization(torch.as_tensor(m0))

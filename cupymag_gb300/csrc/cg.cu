@@ -450,6 +450,10 @@ __global__ void __launch_bounds__(kCGThreads) cg_ir_kernel(CGArgs<NR, IT> a) {
   }
 }
 
+constexpr int kOccDevices = 64;
+static std::mutex g_occ_mu;
+static int g_occ[kOccDevices][2][2][2] = {};
+
 template <int NR, typename IT>
 static int launch_cg(const cpm_csr *A, const double *b, double *x, const cpm_cg_opts *o, Workspace &w,
                      cpm_cg_info *info, cudaStream_t st) {
@@ -485,18 +489,25 @@ static int launch_cg(const cpm_csr *A, const double *b, double *x, const cpm_cg_
   const bool fp64 = o->precision == 0;
   const void *fn = fp64 ? (const void *)cg_fp64_kernel<NR, IT> : (const void *)cg_ir_kernel<NR, IT>;
   const int smem = kTileSmemBytes;
-  static int cached_dev[2][2][2] = {};
-  static int cached_occ[2][2][2] = {};
+  // occupancy (and the shared-memory attribute, a per-device setting) resolved once per device and
+  // kernel variant, under a lock: host threads may launch on different devices at once
   const int dev = device_id();
+  if (dev < 0 || dev >= kOccDevices) {
+    set_error("cg: device ordinal %d out of range", dev);
+    return CPM_BAD_ARG;
+  }
   const int pi = o->precision ? 1 : 0, ri = NR == 3, ii = sizeof(IT) == 8;
-  int &occ = cached_occ[pi][ri][ii];
-  int &occ_dev = cached_dev[pi][ri][ii];
-  if (occ == 0 || occ_dev != dev + 1) {
-    if (smem) CPM_TRY(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
-    int blocks = 0;
-    CPM_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, fn, kCGThreads, smem));
-    occ = blocks;
-    occ_dev = dev + 1;
+  int occ = 0;
+  {
+    std::lock_guard<std::mutex> lock(g_occ_mu);
+    int &cached = g_occ[dev][pi][ri][ii];  // occupancy + 1, 0 = not resolved
+    if (cached == 0) {
+      if (smem) CPM_TRY(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+      int blocks = 0;
+      CPM_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, fn, kCGThreads, smem));
+      cached = blocks + 1;
+    }
+    occ = cached - 1;
   }
   if (occ < 1) {
     set_error("cg: kernel cannot be resident on an SM");

@@ -137,6 +137,130 @@ __device__ __forceinline__ bool ir_after_rr(IRState &s, double rr, double delta,
   return bad;
 }
 
+// ---------------------------------------------------------------- two-barrier reliable-update CG state
+// One system of the FP32 CG with two grid barriers per iteration
+// (csrc/stencil.cu, cg_stencil_ir2_kernel).  The iteration keeps s ~ A p
+// beside p and forms w = A r in its only product, so each iteration needs one
+// reduction of four sums of the current residual r:
+//   g = r.r, dl = r.w, e = r.s_prev, f = r.p_prev
+// from which (A symmetric, so p_prev.w = s_prev.r)
+//   beta = g / g_prev,  p.s = dl + 2 beta e + beta^2 (p.s)_prev,  r.p = g + beta f,
+//   alpha = (r.p) / (p.s)
+// (alpha as an exact line search along p, which keeps the iteration sound after
+// r is replaced).  A reliable update is a replacement pass: the true residual
+// t = b - A64 (x + d) replaces r, the next product forms w = A t, and the
+// convergence test ||b - A x|| <= tol ||b|| is decided on t alone.
+struct IR2State {
+  double atol, resid, r0, gprev, psprev;
+  int active, rep, first, iters, unconv, updates;
+};
+
+__device__ __forceinline__ void ir2_init(IR2State &s, double bnorm, double rr0, double tol) {
+  s.atol = tol * bnorm;
+  s.resid = sqrt(rr0);
+  s.r0 = s.resid;
+  s.gprev = 0.0;
+  s.psprev = 0.0;
+  s.active = bnorm != 0.0;
+  s.rep = 0;
+  s.first = 1;
+  s.iters = 0;
+  s.unconv = 0;
+  s.updates = 0;
+}
+
+// After the reduction of (g, dl, e, f): mode 0 = idle (converged or stopped),
+// 1 = update with alpha and beta, 2 = replacement pass (the product of this
+// pass is discarded).  Returns true on a non-finite value.
+__device__ __forceinline__ bool ir2_after(IR2State &s, double g, double dl, double e, double f, double delta,
+                                          int maxiter, float &alpha, float &beta, int &mode) {
+  mode = 0;
+  alpha = beta = 0.0f;
+  if (!s.active) return false;
+  if (!isfinite(g)) return true;
+  if (s.rep) {
+    // g = t.t of the true residual: decide convergence on it
+    s.rep = 0;
+    s.resid = sqrt(g);
+    s.r0 = s.resid;
+    if (s.resid <= s.atol) {
+      s.active = 0;
+      return false;
+    }
+    if (s.iters >= maxiter) {
+      s.active = 0;
+      s.unconv = 1;
+      return false;
+    }
+  } else if (!s.first) {
+    // g = r.r of the recursive residual left by the last update
+    s.iters += 1;
+    const double rn = sqrt(g);
+    if (rn < delta * s.r0 || rn <= s.atol || s.iters >= maxiter) {
+      s.rep = 1;
+      s.updates += 1;
+      mode = 2;
+      return false;
+    }
+  }
+  const double b = s.first ? 0.0 : g / s.gprev;
+  const double ps = s.first ? dl : dl + 2.0 * b * e + b * b * s.psprev;
+  const double rp = s.first ? g : g + b * f;
+  const double a = rp / ps;
+  if (!isfinite(a) || !isfinite(b)) return true;
+  s.first = 0;
+  s.gprev = g;
+  s.psprev = ps;
+  alpha = (float)a;
+  beta = (float)b;
+  mode = 1;
+  return false;
+}
+
+// Block-wide sums of the first nv of NV values per thread, up to eight values
+// at a time (warp w adds value w): per value the order of block_sum (lane l
+// adds threads 8l..8l+7 in order, then the fixed shuffle tree), with two block
+// barriers per eight values.  The totals land in tot[0..nv) (shared) and in v.
+// s_w: the kernel's one shared staging array of 8 x kCGThreads doubles.
+template <int NV>
+__device__ __forceinline__ void block_sum_wide(double (&v)[NV], double *tot, double (*s_w)[kCGThreads],
+                                               int nv = NV) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+  for (int j0 = 0; j0 < NV; j0 += 8) {
+    if (j0 >= nv) break;
+#pragma unroll
+    for (int jj = 0; jj < 8; ++jj)
+      if (j0 + jj < NV && j0 + jj < nv) s_w[jj][threadIdx.x] = v[j0 + jj];
+    __syncthreads();
+    if (j0 + warp < nv && j0 + warp < NV) {
+      double t = 0.0;
+#pragma unroll
+      for (int k = 0; k < kCGThreads / kWarp; ++k) t += s_w[warp][lane * (kCGThreads / kWarp) + k];
+      t = warp_sum(t);
+      if (lane == 0) tot[j0 + warp] = t;
+    }
+    __syncthreads();
+  }
+#pragma unroll
+  for (int j = 0; j < NV; ++j)
+    if (j < nv) v[j] = tot[j];
+}
+
+// Totals over all CTAs of records of NV values (record of CTA g at half + g*NV),
+// added in CTA order by every CTA after a grid barrier.
+template <int NV>
+__device__ __forceinline__ void sum_records(const double *half, int G, double (&v)[NV], double *tot,
+                                            double (*s_w)[kCGThreads]) {
+#pragma unroll
+  for (int j = 0; j < NV; ++j) v[j] = 0.0;
+  for (int g = threadIdx.x; g < G; g += blockDim.x) {
+#pragma unroll
+    for (int j = 0; j < NV; ++j) v[j] += __ldcg(&half[(size_t)g * NV + j]);
+  }
+  block_sum_wide<NV>(v, tot, s_w);
+}
+
 __device__ __forceinline__ void set_status(cpm_cg_info *info, int st) {
   atomicMax(&info->status, st);
 }

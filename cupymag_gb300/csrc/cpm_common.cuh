@@ -92,6 +92,15 @@ __device__ __forceinline__ void ld4(const TX *x, int64_t i, int, T *v) {
   for (int e = 0; e < 4; ++e) v[e] = (T)t[e];
 }
 
+// The operand x + d of an FP64 product: the FP64 iterate x plus the FP32
+// correction d of the refinement form (element i, converted to double).
+struct XPlusD {
+  const double *x;
+  const float *d;
+};
+template <typename T>
+__device__ __forceinline__ T ld(const XPlusD &s, int64_t i, int) { return (T)(s.x[i] + (double)s.d[i]); }
+
 // Elements i..i+3: one aligned vector load (VEC) or four scalar loads.
 template <typename T, bool VEC, typename TX>
 __device__ __forceinline__ void ldq(const TX *x, int64_t i, int c, T *v) {

@@ -42,7 +42,8 @@ struct StencilCG {
   double inner_tol;
   int max_outer;
   double *r, *p, *q;           // FP64 vectors (precision 0)
-  float *r32, *p32, *q32, *d32;  // FP32 vectors (precision 1)
+  float *r32, *p32, *q32, *d32;  // FP32 vectors (precision 1); the two-barrier form uses q32 as w = A r
+  float *s32;                    // two-barrier form: s ~ A p
   double *part;
   GridBarrier *bar;
   cpm_cg_info *info;
@@ -431,6 +432,245 @@ __global__ void __launch_bounds__(kIRThreads, 4) cg_stencil_ir_kernel(const __gr
   }
 }
 
+
+// ---------------------------------------------------------------- FP32 CG with two grid barriers per iteration
+// The refinement form of cg_stencil_ir_kernel rearranged so that an iteration
+// passes two grid barriers instead of three (IR2State in cg_common.cuh has
+// the recurrences).  Per iteration:
+//   phase B: w = A32 r (the only product), partial r.w; a system in its
+//            replacement pass also folds x += d, d = 0 here;
+//            -> reduction barrier: g, dl, e, f of every system;
+//   phase A: p = r + beta p, s = w + beta s, d += alpha p, r -= alpha s, and the
+//            next reduction's partials r.r, r.s, r.p of the new r (own unknowns
+//            only); a system due for a reliable update instead computes
+//            t = b - A64 (x + d) in FP64, r = t, and the partials of t;
+//            -> barrier (the next product reads r at neighbouring DOFs).
+// The vector traffic is that of the three-barrier form (44 B per unknown and
+// iteration: r gathered and w written in B; r, p, w, s, d read and r, p, s, d
+// written in A).  A replacement pass costs one extra pass of both phases with
+// an FP64 product; the stopping test is decided on t only, as in the
+// three-barrier form.
+template <int NC, int NR>
+__global__ void __launch_bounds__(kIRThreads, 4) cg_stencil_ir2_kernel(const __grid_constant__ StencilCG a) {
+  constexpr int U = NC * NR;
+  constexpr int NS = n_systems<NC, NR>();
+  constexpr int NV = 4 * NS;  // per system: g, dl, e, f (record slots g: [0,NS), dl: [NS,2NS), e, f after)
+  constexpr int TH = kIRThreads;
+  __shared__ double s_tot[NV];
+  __shared__ double s_w[8][kCGThreads];  // staging of the block sums
+  __shared__ IR2State st[NS];
+  __shared__ float s_al[NS], s_be[NS];
+  __shared__ int s_mask[4];  // update mask, replacement mask, active mask, status
+  const int64_t n = a.S.n;
+  const int64_t d0 = min(n, (int64_t)blockIdx.x * a.dofs_per_cta);
+  const int64_t d1 = min(n, d0 + a.dofs_per_cta);
+  const bool quads = a.quads != 0;
+  const bool use_init = a.use_init_dev ? (__ldcg(a.use_init_dev) != 0) : (a.use_init_host != 0);
+  const unsigned long long tns = a.timeout_ns;
+  const int G = gridDim.x;
+  const double *__restrict__ b = a.b;
+  double *x = a.x;
+  float *r32 = a.r32, *p32 = a.p32, *w32 = a.q32, *s32 = a.s32, *d32 = a.d32;
+  double *half0 = a.part, *half1 = a.part + kPartHalf;
+
+  // ---- prologue: r = b - A64 x (FP64), r32 = r, p = s = d = 0; ||b||^2, ||r||^2
+  double v[2 * NS];
+#pragma unroll
+  for (int j = 0; j < 2 * NS; ++j) v[j] = 0.0;
+  for (int64_t dof = d0 + threadIdx.x; dof < d1; dof += TH) {
+    double y[U];
+    if (use_init) apply<double, NC, NR>(a.S, x, (int)dof, y);
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      const int64_t i = uidx<NC, NR>(n, dof, u);
+      const double bi = b[i];
+      const double ri = use_init ? bi - y[u] : bi;
+      if (!use_init) x[i] = 0.0;
+      r32[i] = (float)ri;
+      p32[i] = 0.0f;
+      s32[i] = 0.0f;
+      d32[i] = 0.0f;
+      const int sy = sys_of<NC, NR>(u);
+      v[sy] = fma(bi, bi, v[sy]);
+      v[NS + sy] = fma(ri, ri, v[NS + sy]);
+    }
+  }
+  block_sum_wide<2 * NS>(v, s_tot, s_w);
+  // this CTA's record of the prologue reduction (half 0) and the g slots of the
+  // first product's reduction (half 1: g = r.r, e = f = 0 since p = s = 0)
+  if (threadIdx.x < 2 * NS) half0[(size_t)blockIdx.x * 2 * NS + threadIdx.x] = s_tot[threadIdx.x];
+  if (threadIdx.x < NV) {
+    const int j = threadIdx.x;
+    half1[(size_t)blockIdx.x * NV + j] = j < NS ? s_tot[NS + j] : 0.0;
+  }
+  if (!grid_sync(a.bar, G, tns)) {
+    set_status(a.info, CPM_BARRIER_TIMEOUT);
+    return;
+  }
+  sum_records<2 * NS>(half0, G, v, s_tot, s_w);
+  if (threadIdx.x == 0) {
+    int am = 0;
+    for (int j = 0; j < NS; ++j) {
+      ir2_init(st[j], sqrt(v[j]), v[NS + j], a.tol);
+      am |= st[j].active << j;
+      if (blockIdx.x == 0) a.info->bnorm[j] = sqrt(v[j]);
+    }
+    s_mask[2] = am;
+  }
+  __syncthreads();
+  int activem = s_mask[2], repm = 0;
+  if (use_init) {
+    for (int64_t dof = d0 + threadIdx.x; dof < d1; dof += TH)
+#pragma unroll
+      for (int u = 0; u < U; ++u)
+        if (!((activem >> sys_of<NC, NR>(u)) & 1)) x[uidx<NC, NR>(n, dof, u)] = b[uidx<NC, NR>(n, dof, u)];
+  }
+  int status = CPM_OK;
+  const int max_pass = 2 * a.maxiter + 8;
+  for (int pass = 0; activem && pass < max_pass; ++pass) {
+    // ---- phase B: w = A32 r, r.w; replacement passes fold x += d, d = 0
+    float dlf[NS];
+#pragma unroll
+    for (int j = 0; j < NS; ++j) dlf[j] = 0.0f;
+    if (quads) {
+      for (int64_t qd = d0 + 4 * threadIdx.x; qd < d1; qd += 4 * TH) {
+        float y[4][U];
+        apply4_c<float, NC, NR>(a.S, a.S.c32, r32, (int)qd, y);
+        quad_store<float, NC, NR>(w32, n, qd, y);
+        quad_dot<NC, NR>(r32, n, qd, y, dlf);
+      }
+    } else {
+      for (int64_t dof = d0 + threadIdx.x; dof < d1; dof += TH) {
+        float y[U];
+        apply<float, NC, NR>(a.S, r32, (int)dof, y);
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+          const int64_t i = uidx<NC, NR>(n, dof, u);
+          w32[i] = y[u];
+          dlf[sys_of<NC, NR>(u)] = fmaf(r32[i], y[u], dlf[sys_of<NC, NR>(u)]);
+        }
+      }
+    }
+    if (repm) {
+      for (int64_t dof = d0 + threadIdx.x; dof < d1; dof += TH)
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+          if (!((repm >> sys_of<NC, NR>(u)) & 1)) continue;
+          const int64_t i = uidx<NC, NR>(n, dof, u);
+          x[i] += (double)d32[i];
+          d32[i] = 0.0f;
+        }
+    }
+    double dl[NS];
+#pragma unroll
+    for (int j = 0; j < NS; ++j) dl[j] = (double)dlf[j];
+    block_sum_wide<NS>(dl, s_tot, s_w);
+    double *half = a.part + (size_t)(1 - (pass & 1)) * kPartHalf;  // pass 0 uses half 1
+    if (threadIdx.x < NS) half[(size_t)blockIdx.x * NV + NS + threadIdx.x] = s_tot[threadIdx.x];
+    if (!grid_sync(a.bar, G, tns)) { status = CPM_BARRIER_TIMEOUT; break; }
+    double t[NV];
+    sum_records<NV>(half, G, t, s_tot, s_w);
+    if (threadIdx.x == 0) {
+      int um = 0, rm = 0, am = 0, bad = 0;
+      for (int j = 0; j < NS; ++j) {
+        float al, be;
+        int mode;
+        bad |= ir2_after(st[j], t[j], t[NS + j], t[2 * NS + j], t[3 * NS + j], a.inner_tol, a.maxiter, al, be, mode)
+                   ? 1 : 0;
+        s_al[j] = al;
+        s_be[j] = be;
+        um |= (mode == 1) << j;
+        rm |= (mode == 2) << j;
+        am |= st[j].active << j;
+      }
+      s_mask[0] = um;
+      s_mask[1] = rm;
+      s_mask[2] = am;
+      s_mask[3] = bad ? CPM_NONFINITE : CPM_OK;
+    }
+    __syncthreads();
+    if (s_mask[3] != CPM_OK) { status = s_mask[3]; break; }
+    const int updm = s_mask[0];
+    repm = s_mask[1];
+    activem = s_mask[2];
+    if (!activem) break;
+    float af[NS], bf[NS];
+#pragma unroll
+    for (int j = 0; j < NS; ++j) {
+      af[j] = s_al[j];
+      bf[j] = s_be[j];
+    }
+    // ---- phase A: updates, or the true residual for a replacement pass; partials of the new r
+    float gf[NS], ef[NS], ff[NS];
+    double gr[3 * NS];
+#pragma unroll
+    for (int j = 0; j < NS; ++j) gf[j] = ef[j] = ff[j] = 0.0f;
+#pragma unroll
+    for (int j = 0; j < 3 * NS; ++j) gr[j] = 0.0;
+    if (updm) {
+      if (quads) {
+        for (int64_t qd = d0 + 4 * threadIdx.x; qd < d1; qd += 4 * TH)
+          quad_update2<NC, NR, NS>(n, qd, updm, af, bf, r32, p32, w32, s32, d32, gf, ef, ff);
+      } else {
+        for (int64_t dof = d0 + threadIdx.x; dof < d1; dof += TH)
+#pragma unroll
+          for (int u = 0; u < U; ++u) {
+            const int sy = sys_of<NC, NR>(u);
+            if (!((updm >> sy) & 1)) continue;
+            update2_one(uidx<NC, NR>(n, dof, u), af[sy], bf[sy], r32, p32, w32, s32, d32, gf[sy], ef[sy], ff[sy]);
+          }
+      }
+    }
+    if (repm) {
+      const XPlusD xd{x, d32};
+      for (int64_t dof = d0 + threadIdx.x; dof < d1; dof += TH) {
+        double yt[U];
+        apply_c<double, NC, NR>(a.S, a.S.c64, xd, (int)dof, yt);
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+          const int sy = sys_of<NC, NR>(u);
+          if (!((repm >> sy) & 1)) continue;
+          const int64_t i = uidx<NC, NR>(n, dof, u);
+          const double tv = b[i] - yt[u];
+          r32[i] = (float)tv;
+          gr[sy] = fma(tv, tv, gr[sy]);
+          gr[NS + sy] = fma(tv, (double)s32[i], gr[NS + sy]);
+          gr[2 * NS + sy] = fma(tv, (double)p32[i], gr[2 * NS + sy]);
+        }
+      }
+    }
+    double gef[3 * NS];
+#pragma unroll
+    for (int j = 0; j < NS; ++j) {
+      gef[j] = (double)gf[j] + gr[j];
+      gef[NS + j] = (double)ef[j] + gr[NS + j];
+      gef[2 * NS + j] = (double)ff[j] + gr[2 * NS + j];
+    }
+    block_sum_wide<3 * NS>(gef, s_tot, s_w);
+    double *next = a.part + (size_t)(pass & 1) * kPartHalf;  // the half of the next pass's reduction
+    if (threadIdx.x < 3 * NS) {
+      const int j = threadIdx.x;  // g -> slot j, e -> 2NS + .., f -> 3NS + ..
+      const int slot = j < NS ? j : NS + j;
+      next[(size_t)blockIdx.x * NV + slot] = s_tot[j];
+    }
+    if (!grid_sync(a.bar, G, tns)) { status = CPM_BARRIER_TIMEOUT; break; }
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    int stt = status;
+    int upd = 0;
+    for (int j = 0; j < NS; ++j) {
+      if (stt == CPM_OK && (st[j].unconv || st[j].active)) stt = CPM_NOT_CONVERGED;
+      a.info->iters[j] = st[j].iters;
+      a.info->resid[j] = st[j].resid;
+      upd += st[j].updates;
+    }
+    a.info->outer = upd;
+    set_status(a.info, stt);
+  } else if (status != CPM_OK && threadIdx.x == 0) {
+    set_status(a.info, status);
+  }
+}
+
 // ---------------------------------------------------------------- y = alpha A x (FP64)
 // Same product on quads of 4 DOFs along z (nz % 4 == 0, 16-byte aligned x and y).
 template <int NC, int NR>
@@ -533,13 +773,17 @@ static int launch_stencil_cg(const cpm_stencil *s, const double *b, double *x, c
   a.p32 = w.pa32;
   a.q32 = w.q32;
   a.d32 = w.d32;
+  a.s32 = w.pb32;
   a.part = w.part;
   a.bar = w.bar;
   a.info = info;
   const double tmo = o->barrier_timeout_s > 0 ? o->barrier_timeout_s : 2.0;
   a.timeout_ns = (unsigned long long)(tmo * 1e9);
   const bool fp64 = o->precision == 0;
-  const void *fn = fp64 ? (const void *)cg_stencil_fp64_kernel<NC, NR> : (const void *)cg_stencil_ir_kernel<NC, NR>;
+  // FP32 form: two grid barriers per iteration unless the caller asks for the three-barrier form
+  const bool two = !fp64 && o->form != CPM_CG_FORM_THREE_BARRIER;
+  const void *fn = fp64 ? (const void *)cg_stencil_fp64_kernel<NC, NR>
+                        : two ? (const void *)cg_stencil_ir2_kernel<NC, NR> : (const void *)cg_stencil_ir_kernel<NC, NR>;
   const int threads = fp64 ? kCGThreads : kIRThreads;
   int occ = 0;
   CPM_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fn, threads, 0));
@@ -566,6 +810,10 @@ static int launch_stencil_cg(const cpm_stencil *s, const double *b, double *x, c
   per = (per + 31) / 32 * 32;
   G = (n + per - 1) / per;
   a.dofs_per_cta = per;
+  if (two && G * 4 * n_systems<NC, NR>() > (int64_t)kPartHalf) {
+    set_error("stencil cg: %lld CTAs exceed the partial-sum records of the two-barrier form", (long long)G);
+    return CPM_BAD_ARG;
+  }
   CPM_TRY(cudaMemsetAsync(w.bar, 0, sizeof(GridBarrier), st));
   CPM_TRY(cudaMemsetAsync(info, 0, sizeof(cpm_cg_info), st));
   void *args[] = {&a};

@@ -422,6 +422,67 @@ __device__ __forceinline__ void quad_direction(int64_t n, int64_t d0, int active
   }
 }
 
+// ---------------------------------------------------------------- two-barrier FP32 CG: update phase
+// Phase A of the two-barrier FP32 CG (csrc/stencil.cu, cg_stencil_ir2_kernel) on
+// the quad d0..d0+3, for the systems in `upd`:
+//   p = r + beta p,  s = w + beta s   (s tracks A p, w = A r from the product phase)
+//   d += alpha p,    r -= alpha s
+// and the next reduction's partials of the new r: g += r.r, e += r.s, f += r.p
+// (FP32 per thread).  Every vector is read and written at the thread's own
+// unknowns, so this phase needs no neighbour data.
+template <int NC, int NR, int NS>
+__device__ __forceinline__ void quad_update2(int64_t n, int64_t d0, int upd, const float (&af)[NS],
+                                             const float (&bf)[NS], float *r32, float *p32, const float *w32,
+                                             float *s32, float *d32, float (&g)[NS], float (&e)[NS],
+                                             float (&f)[NS]) {
+  constexpr int H = NC == 3 ? 3 : NR;
+#pragma unroll
+  for (int h = 0; h < H; ++h) {
+    bool any = false;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) any |= (upd >> quad_sys<NC, NR>(h, k)) & 1;
+    if (!any) continue;
+    const int64_t i0 = quad_base<NC, NR>(n, d0, h);
+    float rr[4], pp[4], ww[4], ss[4], dd[4];
+    Vec4<float>::load(r32 + i0, rr);
+    Vec4<float>::load(p32 + i0, pp);
+    Vec4<float>::load(w32 + i0, ww);
+    Vec4<float>::load(s32 + i0, ss);
+    Vec4<float>::load(d32 + i0, dd);
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      const int sy = quad_sys<NC, NR>(h, k);
+      if (!((upd >> sy) & 1)) continue;
+      pp[k] = fmaf(bf[sy], pp[k], rr[k]);
+      ss[k] = fmaf(bf[sy], ss[k], ww[k]);
+      dd[k] = fmaf(af[sy], pp[k], dd[k]);
+      rr[k] = fmaf(-af[sy], ss[k], rr[k]);
+      g[sy] = fmaf(rr[k], rr[k], g[sy]);
+      e[sy] = fmaf(rr[k], ss[k], e[sy]);
+      f[sy] = fmaf(rr[k], pp[k], f[sy]);
+    }
+    Vec4<float>::store(r32 + i0, rr);
+    Vec4<float>::store(p32 + i0, pp);
+    Vec4<float>::store(s32 + i0, ss);
+    Vec4<float>::store(d32 + i0, dd);
+  }
+}
+
+// The same update for one unknown i of system sy (per-DOF path).
+__device__ __forceinline__ void update2_one(int64_t i, float a, float b, float *r32, float *p32, const float *w32,
+                                            float *s32, float *d32, float &g, float &e, float &f) {
+  const float p = fmaf(b, p32[i], r32[i]);
+  const float s = fmaf(b, s32[i], w32[i]);
+  const float r = fmaf(-a, s, r32[i]);
+  d32[i] = fmaf(a, p, d32[i]);
+  p32[i] = p;
+  s32[i] = s;
+  r32[i] = r;
+  g = fmaf(r, r, g);
+  e = fmaf(r, s, e);
+  f = fmaf(r, p, f);
+}
+
 // y at one DOF with the operator's own (launch-parameter) coefficients.
 template <typename T, int NC, int NR>
 __device__ __forceinline__ void apply(const StencilOp &S, const T *__restrict__ x, int dof, T (&y)[NC * NR]) {

@@ -164,12 +164,24 @@ class LLGSolver:
         """Write the run's state (.npz) so that load_state + further steps reproduce an uninterrupted run
         bit for bit (the reference restarts from m alone, magnetization_io.py:80-124)."""
         arrays = {k: v.detach().cpu().numpy() for k, v in self._state_tensors().items()}
-        np.savez(path, nstep=np.int64(self.nstep), n=np.int64(self.n), ME=np.int8(self.ME), **arrays)
+        np.savez(path, nstep=np.int64(self.nstep), n=np.int64(self.n), ME=np.int8(self.ME),
+                 precision=np.str_(self.precision), operators=np.str_(self.operators), **arrays)
 
     def load_state(self, path):
+        """Restore a save_state checkpoint.  The checkpoint must come from a run of the same size,
+        coupling, precision form and operator form (a run's warm-start vectors and iterates depend on
+        all four); a field schedule already set on this solver must have the checkpoint's length."""
         d = np.load(path)
         if int(d["n"]) != self.n or bool(d["ME"]) != self.ME:
             raise ValueError(f"checkpoint of a different run (n={int(d['n'])}, ME={bool(d['ME'])})")
+        for key, mine in (("precision", self.precision), ("operators", self.operators)):
+            if key not in d:
+                raise ValueError(f"checkpoint lacks {key}")
+            if str(d[key]) != str(mine):
+                raise ValueError(f"checkpoint of a run with {key}={str(d[key])!r}, this solver has {mine!r}")
+        if "hsched" in d and self.hsched is not None and tuple(d["hsched"].shape) != tuple(self.hsched.shape):
+            raise ValueError(f"checkpoint field schedule has {d['hsched'].shape[0]} steps, this solver's has "
+                             f"{self.hsched.shape[0]}")
         if "hsched" in d and self.hsched is None:
             self.set_field_schedule(d["hsched"])
         for k, t in self._state_tensors().items():

@@ -41,7 +41,6 @@ from .. import _native as N
 from ..core.assemble_simulation_operators import SimulationOperators
 from ..physics.llg import INNER_TOL, SOLVE_NAMES, LLGSolver
 from ..solvers.linear_solvers import decode_info
-from ..workloads import seeded_m0
 from .blockdiag import BlockDiagPlan, BlockSystem, coef_key, work_bytes
 
 NSLOTS = len(SOLVE_NAMES)
@@ -178,7 +177,7 @@ class ServingEngine:
         self.infos[slot].zero_()
         L = LLGSolver(S, p, precision=self.precision, operators="stencil", info=self.infos[slot])
         L.set_field_schedule(req.fields(p))
-        L.set_magnetization(torch.as_tensor(seeded_m0(S.n_dof, S.DefDOF, req.seed)))
+        L.set_magnetization(torch.as_tensor(req.initial_m(S.n_dof, S.DefDOF)))
         work = torch.empty(work_bytes((p.Nx, p.Ny, p.Nz), 3, 1, self.precision), dtype=torch.uint8,
                            device=self.dev)
         run = Run(req, L, slot, work, est, now)
@@ -370,7 +369,7 @@ def run_sequential(requests, precision="DP", operators="stencil", device=None, k
         S = SimulationOperators(p, device=dev)
         L = LLGSolver(S, p, precision=precision, operators=operators)
         L.set_field_schedule(req.fields(p))
-        L.set_magnetization(torch.as_tensor(seeded_m0(S.n_dof, S.DefDOF, req.seed)))
+        L.set_magnetization(torch.as_tensor(req.initial_m(S.n_dof, S.DefDOF)))
         torch.cuda.synchronize(dev)
         t_setup = time.perf_counter() - t0 - ts
         err = None

@@ -15,7 +15,7 @@ from dataclasses import dataclass
 
 import numpy as np
 
-from ..workloads import hex_params, sweep_field
+from ..workloads import hex_params, seeded_m0, sweep_field
 
 
 @dataclass(frozen=True)
@@ -35,6 +35,11 @@ class Request:
     def fields(self, p=None):
         p = p or self.params()
         return np.array([sweep_field(p, s, self.steps, self.B0) for s in range(self.steps)], dtype=np.float64)
+
+    def initial_m(self, n_dof, defect_dofs):
+        """The run's initial magnetisation (n_dof, 3): normalise((1,0,0) + N(0, 1e-3)) from the request's
+        seed, zero on the defect DOFs."""
+        return seeded_m0(n_dof, defect_dofs, self.seed)
 
     @property
     def n_dof(self):

@@ -44,8 +44,11 @@ class CGSolver:
         return ws
 
     def launch(self, A: DeviceCSR, b: torch.Tensor, x: torch.Tensor, info: torch.Tensor, *, tol, maxiter,
-               use_init=False, use_init_dev: torch.Tensor = None, precision="DP", inner_tol=None):
-        """Asynchronous solve; x is read as x0 when use_init, and overwritten."""
+               use_init=False, use_init_dev: torch.Tensor = None, precision="DP", inner_tol=None, form=0):
+        """Asynchronous solve; x is read as x0 when use_init, and overwritten.
+
+        form (FP32 stencil solves): N.CG_FORM_DEFAULT (two grid barriers per iteration),
+        N.CG_FORM_THREE_BARRIER or N.CG_FORM_TWO_BARRIER."""
         prec = PRECISIONS[precision] if isinstance(precision, str) else int(precision)
         if prec == 1:
             A.ensure_fp32()
@@ -65,6 +68,7 @@ class CGSolver:
         o.precision = prec
         o.inner_tol = self.inner_tol if inner_tol is None else float(inner_tol)
         o.max_outer = self.max_outer
+        o.form = int(form)
         o.barrier_timeout_s = self.barrier_timeout_s
         fn = N.lib().cpm_cg_solve_stencil if stencil else N.lib().cpm_cg_solve
         N.check(fn(A.struct(), b.data_ptr(), x.data_ptr(), nrhs, C.byref(o), ws.data_ptr(), ws.numel(),

@@ -65,9 +65,16 @@ typedef struct {
   int32_t precision;       /* 0 = FP64 CG, 1 = FP32 CG with FP64 reliable updates */
   double inner_tol;        /* reliable update when the FP32 residual fell by this factor (default 0.1) */
   int32_t max_outer;       /* unused (kept for layout) */
-  int32_t pad;
+  int32_t form;            /* FP32 stencil solvers: CPM_CG_FORM_DEFAULT (two grid barriers per
+                              iteration), CPM_CG_FORM_THREE_BARRIER, CPM_CG_FORM_TWO_BARRIER */
   double barrier_timeout_s;/* bound on every grid-barrier wait (seconds) */
 } cpm_cg_opts;
+
+/* Iteration forms of the FP32 stencil CG (cpm_cg_opts.form).  Both run the
+ * same CG to the same FP64 stopping test; the two-barrier form keeps s ~ A p
+ * beside p and forms A r in its one product, so an iteration needs one
+ * reduction of four sums instead of two reductions and a third barrier. */
+enum { CPM_CG_FORM_DEFAULT = 0, CPM_CG_FORM_THREE_BARRIER = 1, CPM_CG_FORM_TWO_BARRIER = 2 };
 
 /* ---- library ---- */
 const char *cpm_version(void);
@@ -111,7 +118,10 @@ int cpm_cg_solve(const cpm_csr *A, const double *b, double *x, int nrhs, const c
  * values of n * nrhs in FP64 (1.65 million in the FP32-refinement form); larger
  * solves are rejected with CPM_BAD_ARG and a message.  The first call on each
  * device looks up the array's device address (cudaGetSymbolAddress) with that
- * device current; make that first call before any stream capture.  All calls
+ * device current and keeps it for the life of the process; make that first
+ * call before any stream capture.  The kept address does not survive a reset
+ * of the device's context (cudaDeviceReset, or a primary context released and
+ * created again): do not call this entry point after one.  All calls
  * share the one array and it keeps the last call's contents (the solver clears
  * what must start at zero), so calls whose kernels overlap on the GPU -- on
  * different streams or different host threads -- race and give wrong results.

@@ -24,9 +24,14 @@ def _axpy(x, a, y):
     return x + a * y
 
 
-def cg(A, b, x0=None, tol=1e-5, maxiter=None, record=None, axpy=None):
-    """axpy(x, a, y) -> x + a * y (element-wise; a threaded one must round the same way)."""
+def cg(A, b, x0=None, tol=1e-5, maxiter=None, record=None, axpy=None, dot=None):
+    """axpy(x, a, y) -> x + a * y (element-wise; a threaded one must round the same way).
+
+    dot(a, b) -> a.b for the two CG inner products (rho and p.q); the default is
+    np.dot.  Tests pass another summation order to measure how far a
+    trajectory moves when only the rounding of one reduction changes."""
     axpy = axpy or _axpy
+    dot = dot or np.dot
     n = A.shape[0]
     if maxiter is None:
         maxiter = n * 10
@@ -44,13 +49,13 @@ def cg(A, b, x0=None, tol=1e-5, maxiter=None, record=None, axpy=None):
     resid = np.inf
     while iters < maxiter:
         rho1 = rho
-        rho = np.dot(r, r)
+        rho = dot(r, r)
         if iters == 0:
             p = r.copy()
         else:
             p = axpy(r, rho / rho1, p)
         q = A @ p
-        alpha = rho / np.dot(p, q)
+        alpha = rho / dot(p, q)
         x = axpy(x, alpha, p)
         r = axpy(r, -alpha, q)
         iters += 1
@@ -65,8 +70,8 @@ def cg(A, b, x0=None, tol=1e-5, maxiter=None, record=None, axpy=None):
     return x, info
 
 
-def solve_cg(A, b, M=None, x0=None, tol=1e-7, maxiter=5000, use_init=False, system=None, record=None):
-    x, info = cg(A, b, x0=(x0 if use_init else None), tol=tol, maxiter=maxiter, record=record)
+def solve_cg(A, b, M=None, x0=None, tol=1e-7, maxiter=5000, use_init=False, system=None, record=None, dot=None):
+    x, info = cg(A, b, x0=(x0 if use_init else None), tol=tol, maxiter=maxiter, record=record, dot=dot)
     if info == 0:
         return x
     rnorm = np.linalg.norm(b - A @ x)

@@ -134,8 +134,10 @@ class LLGState:
         self.iters = []
 
 
-def llg_step(S, ops, Avg, p, Hext, defect, maxiter=None):
-    """Advance S by one GSPM step at applied field Hext (nondimensional)."""
+def llg_step(S, ops, Avg, p, Hext, defect, maxiter=None, dot=None):
+    """Advance S by one GSPM step at applied field Hext (nondimensional).
+
+    dot: the CG inner product (None: np.dot, the restatement's own order)."""
     n = S.m.shape[0]
     tol = p.tol
     maxiter = p.maxiter if maxiter is None else maxiter
@@ -147,7 +149,7 @@ def llg_step(S, ops, Avg, p, Hext, defect, maxiter=None):
     X = S.x
 
     def cg(A, b, key):
-        x = solve_cg(A, b, x0=X.get(key), tol=tol, maxiter=maxiter, use_init=ui, system=key, record=rec)
+        x = solve_cg(A, b, x0=X.get(key), tol=tol, maxiter=maxiter, use_init=ui, system=key, record=rec, dot=dot)
         X[key] = x
         return x
 
@@ -236,7 +238,7 @@ def fixed_sweep_fields(p, steps, B0):
     return out
 
 
-def run_driver(p, ops, Avg, defect, m0, max_steps=100000):
+def run_driver(p, ops, Avg, defect, m0, max_steps=100000, dot=None):
     """The reference's convergence-driven field sweep (Micromagnetics.py:76-347).
 
     Returns the hysteresis rows [Hext1, Hext2, Hext3, <m1>, <m2>, <m3>] (H in
@@ -255,7 +257,7 @@ def run_driver(p, ops, Avg, defect, m0, max_steps=100000):
     while S.avg_m @ stop > p.stop_value and total < max_steps:
         nstep += 1
         total += 1
-        llg_step(S, ops, Avg, p, tuple(Hext), defect)
+        llg_step(S, ops, Avg, p, tuple(Hext), defect, dot=dot)
         conv = S.sumsq < LLG_accuracy and nstep > llg_min_step
         if conv or nstep % p.save_frequency == 0:
             rows.append([float(f"{Hext[0] * p.ms:.1f}"), float(f"{Hext[1] * p.ms:.1f}"),

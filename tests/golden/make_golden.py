@@ -20,7 +20,7 @@ runs the reference's modules unmodified:
 Each case runs in a fresh subprocess because the reference loads its config
 at import time.  Output: ``tests/golden/<case>.npz``.
 
-Usage:  python tests/golden/make_golden.py [--ref /root/reference] [case ...]
+Usage:  python tests/golden/make_golden.py --ref <reference checkout> [case ...]
 """
 import argparse
 import json
@@ -293,7 +293,7 @@ def run_case(name, ref, outdir):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--ref", default="/root/reference")
+    ap.add_argument("--ref", required=True, help="root of the reference checkout (its cupymag/ package)")
     ap.add_argument("--case", default=None, help=argparse.SUPPRESS)
     ap.add_argument("--outdir", default=str(HERE))
     ap.add_argument("cases", nargs="*")

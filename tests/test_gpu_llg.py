@@ -167,3 +167,59 @@ def test_checkpoint_resume_is_bit_exact(tmp_path, case, precision, operators):
     assert C.nstep == 6
     assert torch.equal(A.m, C.m)
     assert torch.equal(A.hist, C.hist)
+    # a checkpoint of another precision form or a schedule of another length is refused
+    D = LLGSolver(S, p, precision="IR" if precision == "DP" else "DP", operators=operators)
+    with pytest.raises(ValueError, match="precision"):
+        D.load_state(tmp_path / "ck.npz")
+    E = LLGSolver(S, p, precision=precision, operators=operators)
+    E.set_field_schedule(fields[:4])
+    with pytest.raises(ValueError, match="schedule"):
+        E.load_state(tmp_path / "ck.npz")
+
+
+def _yaml(d, indent=0):
+    """A config dict as block YAML (the subset the config loader reads)."""
+    out = []
+    pad = "  " * indent
+    for k, v in d.items():
+        if isinstance(v, dict):
+            out.append(f"{pad}{k}:")
+            out.append(_yaml(v, indent + 1))
+        else:
+            out.append(f"{pad}{k}: {_yaml_scalar(v)}")
+    return "\n".join(out)
+
+
+def _yaml_scalar(v):
+    if v is None:
+        return "null"
+    if isinstance(v, bool):
+        return "true" if v else "false"
+    if isinstance(v, (list, tuple)):
+        return "[" + ", ".join(_yaml_scalar(x) for x in v) + "]"
+    if isinstance(v, str):
+        return f'"{v}"'
+    if isinstance(v, float):
+        # PyYAML 1.1 reads a float only with a dot in the mantissa ("2e-05" stays a string)
+        mant, _, exp = repr(v).partition("e")
+        if "." not in mant:
+            mant += ".0"
+        return mant + ("e" + exp if exp else "")
+    return repr(v)
+
+
+def test_cli_runs_a_yaml_config(tmp_path, capsys):
+    """`cupymag config.yaml` on the GPU: the reference's convergence-driven sweep from a YAML file,
+    through the command-line entry point, writes the reference's hysteresis rows."""
+    from cupymag_gb300.cli import main
+    g = G.load(G.DRIVER)
+    cfg = G.config(g)
+    cfg["output"]["directory"] = str(tmp_path / "out")
+    path = tmp_path / "config.yaml"
+    path.write_text(_yaml(cfg) + "\n")
+    assert main([str(path)]) == 0, capsys.readouterr().out
+    rows = np.loadtxt(tmp_path / "out" / "hysteresis.txt", skiprows=1)
+    ref = g["hysteresis"]
+    assert rows.shape == ref.shape
+    np.testing.assert_array_equal(rows[:, :3], ref[:, :3])
+    np.testing.assert_allclose(rows[:-1, 3:], ref[:-1, 3:], rtol=0, atol=1e-10)

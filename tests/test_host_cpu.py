@@ -188,20 +188,6 @@ def test_library_exports_every_header_symbol():
     assert lib.cpm_cg_workspace_bytes(1000, 3, 1) > lib.cpm_cg_workspace_bytes(10, 1, 1)
 
 
-def test_integration_guide_names_exist():
-    """Every C entry point or type INTEGRATION.md names is in the header, and every `N.` binding it uses
-    exists in the ctypes module (the guide follows the API)."""
-    from cupymag_gb300 import _native as N
-    guide = open(os.path.join(ROOT, "INTEGRATION.md")).read()
-    header = open(os.path.join(ROOT, "include", "cupymag_gb300.h")).read()
-    names = set(re.findall(r"\b(cpm_[A-Za-z0-9_]+)", guide))
-    assert names
-    missing = sorted(nm for nm in names if not re.search(r"\b" + nm + r"\b", header))
-    assert not missing, missing
-    attrs = set(re.findall(r"\bN\.([A-Za-z_][A-Za-z0-9_]*)", guide))
-    assert not [a for a in attrs if not hasattr(N, a)], attrs
-
-
 def test_batch_work_bytes_follow_the_grid():
     """cpm_batch_work_bytes sizes a system's work vectors from its grid (host arithmetic, no GPU)."""
     from cupymag_gb300 import _native as N
