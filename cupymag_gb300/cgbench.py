@@ -49,7 +49,7 @@ def main(argv=None):
     ap.add_argument("--inner-tol", type=float, default=0.1,
                     help="reliable-update factor of the FP32 solver (residual drop between FP64 updates)")
     ap.add_argument("--form", type=int, default=0, choices=[0, 1, 2],
-                    help="FP32 stencil solver: 0 default (two barriers), 1 three-barrier, 2 two-barrier")
+                    help="FP32 stencil solver: 0 default (three barriers), 1 three-barrier, 2 two-barrier")
     args = ap.parse_args(argv)
 
     from . import _native as N
@@ -87,7 +87,7 @@ def main(argv=None):
                                        torch.empty(work_bytes((op.nx, op.ny, op.nz), op.ncomp, nrhs,
                                                               args.precision),
                                                    dtype=torch.uint8, device="cuda"), p.tol, args.maxiter))
-        plan = BlockDiagPlan(systems, args.precision, inner_tol=args.inner_tol)
+        plan = BlockDiagPlan(systems, args.precision, inner_tol=args.inner_tol, form=args.form)
         launch = plan.launch
         info_of = lambda: systems[0].info  # noqa: E731
     else:

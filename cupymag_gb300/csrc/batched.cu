@@ -56,7 +56,8 @@ struct BSeg {
   int chunk0, nchunks, cta0, ncta, chunk_dofs;
   int quads;                     // FP32 product on quads of 4 DOFs along z
   double *r, *p, *q;             // precision 0
-  float *r32, *p32, *q32, *d32;  // precision 1
+  float *r32, *p32, *q32, *d32;  // precision 1 (the two-barrier form uses q32 as w = A r)
+  float *s32;                    // two-barrier form: s ~ A p
 };
 
 struct BatchArgs {
@@ -88,9 +89,13 @@ constexpr int kStageDoubles = kStage * 9 * kCGWarps;
 // CTA computes the chunk.  The warp sums of up to kStage chunks wait in
 // `stage` and are added and written together, so a chunk costs shuffles but
 // no block barrier.
-template <int NV, typename Body>
+struct SlotIdentity {
+  __device__ __forceinline__ int operator()(int j) const { return j; }
+};
+
+template <int NV, typename Body, typename Slot = SlotIdentity>
 __device__ __forceinline__ void chunk_partials(const BSeg &S, int l, double *half, double *stage, int nv,
-                                               Body body) {
+                                               Body body, Slot slot = Slot()) {
   static_assert(NV <= 9, "stage holds at most 9 sums per chunk");
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   int held = 0, first = l;
@@ -116,7 +121,7 @@ __device__ __forceinline__ void chunk_partials(const BSeg &S, int l, double *hal
         double s = 0.0;
 #pragma unroll
         for (int k = 0; k < kCGWarps; ++k) s += src[k];
-        half[(size_t)(S.chunk0 + first + cl * S.ncta) * kSlot + j] = s;
+        half[(size_t)(S.chunk0 + first + cl * S.ncta) * kSlot + slot(j)] = s;
       }
       __syncthreads();
       held = 0;
@@ -601,6 +606,280 @@ __global__ void __launch_bounds__(kCGThreads, (NC == 1 && NR == 3) ? 3 : 4) cg_b
   }
 }
 
+
+// ---------------------------------------------------------------- FP32, two grid barriers per iteration
+// Opt-in (CPM_CG_FORM_TWO_BARRIER; the single-system form measured slower and,
+// at 128^3, stalling on the elastic and demag solves).  The two-barrier
+// iteration of csrc/stencil.cu (cg_stencil_ir2_kernel, state transitions in
+// IR2State) per segment: phase B forms w = A32 r and the chunk
+// partials of r.w (a system in its replacement pass also folds x += d, d = 0),
+// then the reduction barrier; phase A updates p, s, d, r (or computes the true
+// residual t = b - A64 (x + d) for a replacement pass) and stores the chunk
+// partials r.r, r.s, r.p of the new r in the next reduction's records, then the
+// barrier before the next product.  A chunk's record holds its 4 NS sums
+// (slots: g, r.w, e, f per system), written by the two phases in turn; a
+// system's totals add its own chunks in a fixed order, so its iterates do not
+// depend on the rest of the batch.
+template <int NC, int NR>
+__global__ void __launch_bounds__(kCGThreads, (NC == 1 && NR == 3) ? 3 : 4) cg_batched_ir2_kernel(const __grid_constant__ BatchArgs a) {
+  constexpr int U = NC * NR;
+  constexpr int NS = b_systems<NC, NR>();
+  constexpr int NV = 4 * NS;
+  __shared__ double s_tot[NV];
+  __shared__ double s_w[8][kCGThreads];
+  __shared__ double s_stage[kStageDoubles];
+  __shared__ IR2State st[NS];
+  __shared__ float s_al[NS], s_be[NS];
+  __shared__ int s_mask[4];  // update, replacement, active, status
+  __shared__ BSeg s_seg;
+  if (threadIdx.x == 0) s_seg = a.segs[a.cta_seg[blockIdx.x]];
+  __syncthreads();
+  const BSeg &S = s_seg;
+  const int l = blockIdx.x - S.cta0;
+  const bool lead = l == 0;
+  const Geo g{S.nx, S.ny, S.nz, S.n, S.flags};
+  const int64_t n = g.n;
+  const double *__restrict__ b = S.b;
+  double *x = S.x;
+  float *r32 = S.r32, *p32 = S.p32, *w32 = S.q32, *s32 = S.s32, *d32 = S.d32;
+  const bool use_init = S.use_init_dev && __ldcg(S.use_init_dev) != 0;
+  const bool quads = S.quads != 0;
+  int par = 0;
+
+  // ---- prologue: r = b - A64 x, r32 = r, p = s = d = 0; ||b||^2, ||r||^2 (half 0),
+  // and the g slots of the first product's reduction (half 1: g = r.r; e = f = 0)
+  double *h0 = a.part, *h1 = a.part + (size_t)a.half;
+  chunk_partials<2 * NS>(S, l, h0, s_stage, 2 * NS, [&](int d0, int d1, double (&w)[2 * NS]) {
+    for (int dof = d0 + threadIdx.x; dof < d1; dof += kCGThreads) {
+      double y[U];
+      if (use_init) apply_c<double, NC, NR>(g, a.c64, x, dof, y);
+#pragma unroll
+      for (int u = 0; u < U; ++u) {
+        const int64_t i = uidx<NC, NR>(n, dof, u);
+        const double bi = b[i];
+        const double ri = use_init ? bi - y[u] : bi;
+        if (!use_init) x[i] = 0.0;
+        r32[i] = (float)ri;
+        p32[i] = 0.0f;
+        s32[i] = 0.0f;
+        d32[i] = 0.0f;
+        const int sy = b_sys<NC, NR>(u);
+        w[sy] = fma(bi, bi, w[sy]);
+        w[NS + sy] = fma(ri, ri, w[NS + sy]);
+      }
+    }
+  });
+  // the g slots of half 1 repeat the r.r partials (slots NS..2NS of half 0); e and f start at zero
+  __syncthreads();
+  for (int c = l; c < S.nchunks; c += S.ncta)
+    for (int j = threadIdx.x; j < NV; j += kCGThreads) {
+      const size_t rec = (size_t)(S.chunk0 + c) * kSlot;
+      h1[rec + j] = j < NS ? h0[rec + NS + j] : 0.0;
+    }
+  bool ok = grid_sync(a.bar, gridDim.x, a.timeout_ns);
+  double v[2 * NS];
+  if (ok) {
+#pragma unroll
+    for (int j = 0; j < 2 * NS; ++j) v[j] = 0.0;
+    for (int c = threadIdx.x; c < S.nchunks; c += kCGThreads) {
+      const double *src = h0 + (size_t)(S.chunk0 + c) * kSlot;
+#pragma unroll
+      for (int j = 0; j < 2 * NS; ++j) v[j] += __ldcg(src + j);
+    }
+    block_sum_wide<2 * NS>(v, s_tot, s_w);
+  }
+  if (threadIdx.x == 0) {
+    int am = 0;
+    for (int j = 0; j < NS; ++j) {
+      const double bn = ok ? sqrt(v[j]) : 0.0;
+      ir2_init(st[j], bn, ok ? v[NS + j] : 0.0, S.tol);
+      am |= st[j].active << j;
+      if (lead) S.info->bnorm[j] = bn;
+    }
+    if (lead) {
+      for (int j = NS; j < 3; ++j) S.info->bnorm[j] = 0.0;
+      if (am) atomicAdd(a.live, 1);
+    }
+    s_mask[2] = am;
+  }
+  __syncthreads();
+  int activem = s_mask[2], repm = 0;
+  int status = ok ? CPM_OK : CPM_BARRIER_TIMEOUT;
+  if (ok && use_init) {
+    for (int cc = l; cc < S.nchunks; cc += S.ncta) {
+      const int d1 = min(g.n, (cc + 1) * S.chunk_dofs);
+      for (int dof = cc * S.chunk_dofs + threadIdx.x; dof < d1; dof += kCGThreads)
+#pragma unroll
+        for (int u = 0; u < U; ++u)
+          if (!((activem >> b_sys<NC, NR>(u)) & 1)) x[uidx<NC, NR>(n, dof, u)] = b[uidx<NC, NR>(n, dof, u)];
+    }
+  }
+  par = 1;  // the first product's reduction uses half 1
+  const int max_pass = 2 * S.maxiter + 8;
+  for (int pass = 0; ok; ++pass) {
+    // ---- phase B: w = A32 r, r.w; replacement passes fold x += d, d = 0
+    double *half = a.part + (size_t)par * (size_t)a.half;
+    const bool busy = activem != 0;
+    if (busy) {
+      chunk_partials<NS>(S, l, half, s_stage, NS, [&](int d0, int d1, double (&w)[NS]) {
+        float dlf[NS];
+#pragma unroll
+        for (int j = 0; j < NS; ++j) dlf[j] = 0.0f;
+        if (quads) {
+          for (int qd = d0 + 4 * threadIdx.x; qd < d1; qd += 4 * kCGThreads) {
+            float y[4][U];
+            apply4_c<float, NC, NR>(g, a.c32, r32, qd, y);
+            quad_store<float, NC, NR>(w32, n, qd, y);
+            quad_dot<NC, NR>(r32, n, qd, y, dlf);
+          }
+        } else {
+          for (int dof = d0 + threadIdx.x; dof < d1; dof += kCGThreads) {
+            float y[U];
+            apply_c<float, NC, NR>(g, a.c32, r32, dof, y);
+#pragma unroll
+            for (int u = 0; u < U; ++u) {
+              const int64_t i = uidx<NC, NR>(n, dof, u);
+              w32[i] = y[u];
+              dlf[b_sys<NC, NR>(u)] = fmaf(r32[i], y[u], dlf[b_sys<NC, NR>(u)]);
+            }
+          }
+        }
+        if (repm) {
+          for (int dof = d0 + threadIdx.x; dof < d1; dof += kCGThreads)
+#pragma unroll
+            for (int u = 0; u < U; ++u) {
+              if (!((repm >> b_sys<NC, NR>(u)) & 1)) continue;
+              const int64_t i = uidx<NC, NR>(n, dof, u);
+              x[i] += (double)d32[i];
+              d32[i] = 0.0f;
+            }
+        }
+#pragma unroll
+        for (int j = 0; j < NS; ++j) w[j] = (double)dlf[j];
+      }, [](int j) { return NS + j; });
+    }
+    if (!grid_sync(a.bar, gridDim.x, a.timeout_ns)) { status = CPM_BARRIER_TIMEOUT; break; }
+    int updm = 0;
+    if (busy) {
+      double t[NV];
+#pragma unroll
+      for (int j = 0; j < NV; ++j) t[j] = 0.0;
+      for (int c = threadIdx.x; c < S.nchunks; c += kCGThreads) {
+        const double *src = half + (size_t)(S.chunk0 + c) * kSlot;
+#pragma unroll
+        for (int j = 0; j < NV; ++j) t[j] += __ldcg(src + j);
+      }
+      block_sum_wide<NV>(t, s_tot, s_w);
+      if (threadIdx.x == 0) {
+        int um = 0, rm = 0, am = 0, bad = 0;
+        for (int j = 0; j < NS; ++j) {
+          float al, be;
+          int mode;
+          bad |= ir2_after(st[j], t[j], t[NS + j], t[2 * NS + j], t[3 * NS + j], a.inner_tol, S.maxiter, al, be,
+                           mode) ? 1 : 0;
+          if (!bad && pass + 1 >= max_pass && st[j].active) {
+            st[j].active = 0;
+            st[j].unconv = 1;
+            mode = 0;
+          }
+          s_al[j] = al;
+          s_be[j] = be;
+          um |= (mode == 1) << j;
+          rm |= (mode == 2) << j;
+          am |= st[j].active << j;
+        }
+        if (bad) {
+          for (int j = 0; j < NS; ++j) st[j].active = 0;
+          um = rm = am = 0;
+        }
+        if (lead && am == 0) atomicSub(a.live, 1);
+        s_mask[0] = um;
+        s_mask[1] = rm;
+        s_mask[2] = am;
+        s_mask[3] = bad ? CPM_NONFINITE : CPM_OK;
+      }
+      __syncthreads();
+      if (s_mask[3] != CPM_OK) status = s_mask[3];
+      updm = s_mask[0];
+      repm = s_mask[1];
+      activem = s_mask[2];
+    }
+    par ^= 1;
+    // ---- phase A: updates, or the true residual for a replacement pass; partials of the new r
+    if (activem) {
+      float af[NS], bf[NS];
+#pragma unroll
+      for (int j = 0; j < NS; ++j) {
+        af[j] = s_al[j];
+        bf[j] = s_be[j];
+      }
+      double *next = a.part + (size_t)par * (size_t)a.half;
+      chunk_partials<3 * NS>(S, l, next, s_stage, 3 * NS, [&](int d0, int d1, double (&w)[3 * NS]) {
+        float gf[NS], ef[NS], ff[NS];
+#pragma unroll
+        for (int j = 0; j < NS; ++j) gf[j] = ef[j] = ff[j] = 0.0f;
+        if (updm) {
+          if (quads) {
+            for (int qd = d0 + 4 * threadIdx.x; qd < d1; qd += 4 * kCGThreads)
+              quad_update2<NC, NR, NS>(n, qd, updm, af, bf, r32, p32, w32, s32, d32, gf, ef, ff);
+          } else {
+            for (int dof = d0 + threadIdx.x; dof < d1; dof += kCGThreads)
+#pragma unroll
+              for (int u = 0; u < U; ++u) {
+                const int sy = b_sys<NC, NR>(u);
+                if (!((updm >> sy) & 1)) continue;
+                update2_one(uidx<NC, NR>(n, dof, u), af[sy], bf[sy], r32, p32, w32, s32, d32, gf[sy], ef[sy],
+                            ff[sy]);
+              }
+          }
+        }
+#pragma unroll
+        for (int j = 0; j < NS; ++j) {
+          w[j] = (double)gf[j];
+          w[NS + j] = (double)ef[j];
+          w[2 * NS + j] = (double)ff[j];
+        }
+        if (repm) {
+          const XPlusD xd{x, d32};
+          for (int dof = d0 + threadIdx.x; dof < d1; dof += kCGThreads) {
+            double yt[U];
+            apply_c<double, NC, NR>(g, a.c64, xd, dof, yt);
+#pragma unroll
+            for (int u = 0; u < U; ++u) {
+              const int sy = b_sys<NC, NR>(u);
+              if (!((repm >> sy) & 1)) continue;
+              const int64_t i = uidx<NC, NR>(n, dof, u);
+              const double tv = b[i] - yt[u];
+              r32[i] = (float)tv;
+              w[sy] = fma(tv, tv, w[sy]);
+              w[NS + sy] = fma(tv, (double)s32[i], w[NS + sy]);
+              w[2 * NS + sy] = fma(tv, (double)p32[i], w[2 * NS + sy]);
+            }
+          }
+        }
+      }, [](int j) { return j < NS ? j : NS + j; });
+    }
+    if (!grid_sync(a.bar, gridDim.x, a.timeout_ns)) { status = CPM_BARRIER_TIMEOUT; break; }
+    // every change of the counter happened before this barrier and none happens
+    // before the next one: all CTAs read the same value
+    if (__ldcg(a.live) == 0) break;
+  }
+  if (lead && threadIdx.x == 0) {
+    int sta = status;
+    if (*(volatile const int *)&a.bar->error && sta == CPM_OK) sta = CPM_BARRIER_TIMEOUT;
+    int upd = 0;
+    for (int j = 0; j < 3; ++j) {
+      if (j < NS && sta == CPM_OK && (st[j].unconv || st[j].active)) sta = CPM_NOT_CONVERGED;
+      S.info->iters[j] = j < NS ? st[j].iters : 0;
+      S.info->resid[j] = j < NS ? st[j].resid : 0.0;
+      if (j < NS) upd += st[j].updates;
+    }
+    S.info->outer = upd;
+    S.info->pad = 0;
+    S.info->status = sta;
+  }
+}
+
 // ---------------------------------------------------------------- host side
 // DOFs per chunk of one system: a base size per operator kind, doubled until
 // the system has at most kMaxChunks chunks.  It depends on the system alone,
@@ -612,14 +891,22 @@ static int chunk_dofs_for(int ncomp, int nrhs, int64_t n) {
   return (int)cd;
 }
 
-static const void *batched_kernel(int ncomp, int nrhs, int precision) {
+// form: CPM_CG_FORM_* of the FP32 solver (the three-barrier form unless the two-barrier one is asked for)
+static const void *batched_kernel(int ncomp, int nrhs, int precision, int form) {
   if (precision == 0) {
     if (ncomp == 3) return (const void *)cg_batched_fp64_kernel<3, 1>;
     return nrhs == 3 ? (const void *)cg_batched_fp64_kernel<1, 3> : (const void *)cg_batched_fp64_kernel<1, 1>;
   }
-  if (ncomp == 3) return (const void *)cg_batched_ir_kernel<3, 1>;
-  return nrhs == 3 ? (const void *)cg_batched_ir_kernel<1, 3> : (const void *)cg_batched_ir_kernel<1, 1>;
+  if (form != CPM_CG_FORM_TWO_BARRIER) {
+    if (ncomp == 3) return (const void *)cg_batched_ir_kernel<3, 1>;
+    return nrhs == 3 ? (const void *)cg_batched_ir_kernel<1, 3> : (const void *)cg_batched_ir_kernel<1, 1>;
+  }
+  if (ncomp == 3) return (const void *)cg_batched_ir2_kernel<3, 1>;
+  return nrhs == 3 ? (const void *)cg_batched_ir2_kernel<1, 3> : (const void *)cg_batched_ir2_kernel<1, 1>;
 }
+
+// FP64 work vectors r, p, q; FP32 r, p, q (w), d and s (the two-barrier form's A p)
+constexpr int kWorkVecs64 = 3, kWorkVecs32 = 5;
 
 static size_t vec_bytes(int64_t n, int ncomp, int nrhs, int precision) {
   return align256((size_t)n * ncomp * nrhs * (precision ? 4 : 8));
@@ -667,9 +954,16 @@ static int assign(const cpm_batch_system *sys, int nsys, int ncomp, int nrhs, in
     A.nchunks[s] = (int)((n + cd - 1) / cd);
     A.total_chunks += A.nchunks[s];
   }
+  // the plan's grid must be resident for every kernel form that may launch it
   int occ = 0;
-  CPM_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, batched_kernel(ncomp, nrhs, precision), kCGThreads,
+  CPM_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, batched_kernel(ncomp, nrhs, precision, 0), kCGThreads,
                                                         0));
+  if (precision) {
+    int occ2 = 0;
+    CPM_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+        &occ2, batched_kernel(ncomp, nrhs, precision, CPM_CG_FORM_TWO_BARRIER), kCGThreads, 0));
+    occ = std::min(occ, occ2);
+  }
   if (occ < 1) {
     set_error("%s: kernel cannot be resident on an SM", who);
     return CPM_CUDA_ERROR;
@@ -706,7 +1000,7 @@ extern "C" int64_t cpm_batch_work_bytes(int32_t nx, int32_t ny, int32_t nz, int3
   using namespace cpm;
   if (nx < 1 || ny < 1 || nz < 1 || (ncomp != 1 && ncomp != 3) || (nrhs != 1 && nrhs != 3)) return 0;
   const int64_t n = (int64_t)nx * ny * nz;
-  return (int64_t)((precision ? 4 : 3) * vec_bytes(n, ncomp, nrhs, precision));
+  return (int64_t)((precision ? kWorkVecs32 : kWorkVecs64) * vec_bytes(n, ncomp, nrhs, precision));
 }
 
 extern "C" int cpm_batch_plan_bytes(const cpm_batch_system *sys, int32_t nsys, int32_t ncomp, int32_t nrhs,
@@ -771,6 +1065,7 @@ extern "C" int cpm_batch_plan_build(const cpm_batch_system *sys, int32_t nsys, i
       S.p32 = (float *)(w + vb);
       S.q32 = (float *)(w + 2 * vb);
       S.d32 = (float *)(w + 3 * vb);
+      S.s32 = (float *)(w + 4 * vb);
     }
     for (int t = 0; t < S.ncta; ++t) cmap[cta0 + t] = s;
     chunk0 += S.nchunks;
@@ -819,7 +1114,8 @@ extern "C" int cpm_cg_solve_blockdiag(const cpm_batch_plan *plan, const cpm_cg_o
   cudaStream_t st = (cudaStream_t)stream;
   CPM_TRY(cudaMemsetAsync(base + L.bar, 0, 32, st));
   void *args[] = {&a};
-  CPM_TRY(cudaLaunchCooperativeKernel(batched_kernel(plan->ncomp, plan->nrhs, plan->precision), dim3(plan->grid),
+  CPM_TRY(cudaLaunchCooperativeKernel(batched_kernel(plan->ncomp, plan->nrhs, plan->precision, opts->form),
+                                      dim3(plan->grid),
                                       dim3(kCGThreads), args, 0, st));
   return CPM_OK;
 }

@@ -152,7 +152,13 @@ __device__ __forceinline__ bool grid_sync(GridBarrier *bar, unsigned int nblocks
       unsigned int spins = 0;
       while (*vgen == g) {
         if (*verr) { fail = 1; break; }
-        if ((++spins & 63u) == 0 && global_ns() - t0 > timeout_ns) {
+        // the clock is read on polls 1, 2, 4, ..., 32 and then every 64th (each poll is an L2 round trip)
+        ++spins;
+        if ((spins & 63u) == 0 || (spins < 64u && (spins & (spins - 1u)) == 0)) {
+          if (global_ns() - t0 <= timeout_ns) {
+            __nanosleep(20);
+            continue;
+          }
           atomicExch(&bar->error, 1);
           fail = 1;
           break;

@@ -450,6 +450,11 @@ __global__ void __launch_bounds__(kIRThreads, 4) cg_stencil_ir_kernel(const __gr
 // written in A).  A replacement pass costs one extra pass of both phases with
 // an FP64 product; the stopping test is decided on t only, as in the
 // three-barrier form.
+// Opt-in (CPM_CG_FORM_TWO_BARRIER).  Measured on GB300 it is not faster: cold
+// elastic solves took 42.4 us per iteration at 64^3 (three-barrier 35.4) and
+// 100.6 us at 128^3 (77.6), where the five FP32 vectors no longer fit the L2;
+// and at 128^3 the elastic and demag solves stalled (20000 iterations), as the
+// FP32 recurrences for s ~ A p and p.s drift over thousands of iterations.
 template <int NC, int NR>
 __global__ void __launch_bounds__(kIRThreads, 4) cg_stencil_ir2_kernel(const __grid_constant__ StencilCG a) {
   constexpr int U = NC * NR;
@@ -780,8 +785,8 @@ static int launch_stencil_cg(const cpm_stencil *s, const double *b, double *x, c
   const double tmo = o->barrier_timeout_s > 0 ? o->barrier_timeout_s : 2.0;
   a.timeout_ns = (unsigned long long)(tmo * 1e9);
   const bool fp64 = o->precision == 0;
-  // FP32 form: two grid barriers per iteration unless the caller asks for the three-barrier form
-  const bool two = !fp64 && o->form != CPM_CG_FORM_THREE_BARRIER;
+  // FP32 form: three grid barriers per iteration unless the caller asks for the two-barrier form
+  const bool two = !fp64 && o->form == CPM_CG_FORM_TWO_BARRIER;
   const void *fn = fp64 ? (const void *)cg_stencil_fp64_kernel<NC, NR>
                         : two ? (const void *)cg_stencil_ir2_kernel<NC, NR> : (const void *)cg_stencil_ir_kernel<NC, NR>;
   const int threads = fp64 ? kCGThreads : kIRThreads;

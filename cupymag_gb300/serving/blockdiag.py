@@ -50,7 +50,7 @@ def coef_key(op) -> bytes:
 
 
 class BlockDiagPlan:
-    def __init__(self, systems, precision="IR", device=None, inner_tol=0.1, barrier_timeout_s=2.0):
+    def __init__(self, systems, precision="IR", device=None, inner_tol=0.1, barrier_timeout_s=2.0, form=0):
         if not systems:
             raise ValueError("a block-diagonal plan needs at least one system")
         self.precision = PRECISIONS[precision] if isinstance(precision, str) else int(precision)
@@ -90,6 +90,7 @@ class BlockDiagPlan:
         self.opts = N.CGOpts()
         self.opts.inner_tol = float(inner_tol)
         self.opts.barrier_timeout_s = float(barrier_timeout_s)
+        self.opts.form = int(form)   # FP32: N.CG_FORM_DEFAULT (three barriers) or N.CG_FORM_TWO_BARRIER
         self.systems = list(systems)   # keeps every buffer the plan points to alive
         self.ncomp, self.nrhs = ncomp, nrhs
 

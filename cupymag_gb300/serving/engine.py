@@ -53,12 +53,13 @@ def estimate_bytes(p, precision="IR") -> int:
     the volume-average weights, five flag arrays and the defect mask, the
     three derivative matrices (27 non-zeros per row, shared indices), the
     elastic right-hand-side matrix (3 rows x 162 non-zeros) with coupling, and
-    the block-diagonal CG vectors of the largest solve (3n unknowns)."""
+    the block-diagonal CG vectors of the largest solve (3n unknowns: five FP32
+    or three FP64 vectors)."""
     n = int(p.Nx) * int(p.Ny) * int(p.Nz)
     per = (51 if p.ME else 33) * 8 + 8 + 6 + (4 + 27 * 4 + 3 * 27 * 8)
     if p.ME:
         per += 3 * 4 + 3 * 162 * 12
-    per += 3 * (16 if precision != "DP" else 24)
+    per += 3 * (20 if precision != "DP" else 24)
     return int(per * n * 1.05) + (8 << 20)
 
 

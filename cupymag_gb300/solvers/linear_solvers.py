@@ -47,8 +47,8 @@ class CGSolver:
                use_init=False, use_init_dev: torch.Tensor = None, precision="DP", inner_tol=None, form=0):
         """Asynchronous solve; x is read as x0 when use_init, and overwritten.
 
-        form (FP32 stencil solves): N.CG_FORM_DEFAULT (two grid barriers per iteration),
-        N.CG_FORM_THREE_BARRIER or N.CG_FORM_TWO_BARRIER."""
+        form (FP32 stencil solves): N.CG_FORM_DEFAULT (three grid barriers per iteration),
+        N.CG_FORM_THREE_BARRIER or N.CG_FORM_TWO_BARRIER (opt-in)."""
         prec = PRECISIONS[precision] if isinstance(precision, str) else int(precision)
         if prec == 1:
             A.ensure_fp32()

@@ -65,15 +65,17 @@ typedef struct {
   int32_t precision;       /* 0 = FP64 CG, 1 = FP32 CG with FP64 reliable updates */
   double inner_tol;        /* reliable update when the FP32 residual fell by this factor (default 0.1) */
   int32_t max_outer;       /* unused (kept for layout) */
-  int32_t form;            /* FP32 stencil solvers: CPM_CG_FORM_DEFAULT (two grid barriers per
+  int32_t form;            /* FP32 stencil solvers: CPM_CG_FORM_DEFAULT (= three grid barriers per
                               iteration), CPM_CG_FORM_THREE_BARRIER, CPM_CG_FORM_TWO_BARRIER */
   double barrier_timeout_s;/* bound on every grid-barrier wait (seconds) */
 } cpm_cg_opts;
 
-/* Iteration forms of the FP32 stencil CG (cpm_cg_opts.form).  Both run the
- * same CG to the same FP64 stopping test; the two-barrier form keeps s ~ A p
- * beside p and forms A r in its one product, so an iteration needs one
- * reduction of four sums instead of two reductions and a third barrier. */
+/* Iteration forms of the FP32 stencil CG (cpm_cg_opts.form).  Both run CG to
+ * the same FP64 stopping test; the two-barrier form keeps s ~ A p beside p and
+ * forms A r in its one product, so an iteration needs one reduction of four
+ * sums instead of two reductions and a third barrier.  The two-barrier form is
+ * opt-in: on GB300 it measured slower per iteration, and its FP32 recurrences
+ * drift enough to stall the 128^3 elastic and demag solves. */
 enum { CPM_CG_FORM_DEFAULT = 0, CPM_CG_FORM_THREE_BARRIER = 1, CPM_CG_FORM_TWO_BARRIER = 2 };
 
 /* ---- library ---- */

@@ -123,3 +123,29 @@ def test_blockdiag_rejects_mixed_kinds():
     b = _systems(("A1", 1), [8], "DP")[0][0]
     with pytest.raises(ValueError):
         BlockDiagPlan([a, b], "DP")
+
+
+@pytest.mark.parametrize("kind", KINDS, ids=[k[0] + str(k[1]) for k in KINDS])
+def test_blockdiag_two_barrier_form_alone_equals_in_mix(kind):
+    """The opt-in two-barrier FP32 form of the block-diagonal kernel: each system's iterates are the same
+    alone and in a mix (bit for bit), and every system meets the FP64 stopping test."""
+    from cupymag_gb300 import _native as N
+    from cupymag_gb300.serving.blockdiag import BlockDiagPlan
+    from cupymag_gb300.solvers.linear_solvers import decode_info
+
+    def solve(systems):
+        for s in systems:
+            s.x.zero_()
+        BlockDiagPlan(systems, "IR", form=N.CG_FORM_TWO_BARRIER).launch()
+        torch.cuda.synchronize()
+        return [(s.x.cpu().numpy(), decode_info(s.info.cpu().numpy())) for s in systems]
+
+    sys_ = _systems(kind, [7, 12, 9, 16], "IR", seed=4)
+    mix = solve([s for s, _, _ in sys_])
+    for i, (s, A, b) in enumerate(sys_):
+        alone = solve([s])[0]
+        assert np.array_equal(alone[0], mix[i][0]), (kind, i)
+        assert alone[1] == mix[i][1]
+        assert mix[i][1]["status"] == 0, mix[i][1]
+        r = b - A @ mix[i][0]
+        assert np.all(np.linalg.norm(r, axis=0) <= 1e-10 * np.linalg.norm(b, axis=0) * 1.001), (kind, i)

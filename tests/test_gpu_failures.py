@@ -52,7 +52,8 @@ def _solve(solver, A, b, prec):
 def test_barrier_timeout_is_reported_and_the_context_stays_usable(form, prec):
     from cupymag_gb300 import _native as N
     from cupymag_gb300.solvers.linear_solvers import CGSolver
-    A, b = _demag(form=form)
+    # 48^3: over a hundred CTAs and iterations, so some barrier wait lasts past the first clock reads
+    A, b = _demag(edge=48, form=form)
     ref, inf_ref = _solve(CGSolver(), A, b, prec)
     assert inf_ref["status"] == N.CPM_OK
     s = CGSolver()

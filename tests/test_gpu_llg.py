@@ -130,9 +130,10 @@ def test_driver_sweep_matches_reference_main(tmp_path):
     ref = g["hysteresis"]
     assert rows.shape == ref.shape
     np.testing.assert_array_equal(rows[:, :3], ref[:, :3])
-    # stable branches track to rounding; the last row follows the switching event
-    np.testing.assert_allclose(rows[:-1, 3:], ref[:-1, 3:], rtol=0, atol=1e-10)
-    np.testing.assert_allclose(rows[-1, 3:], ref[-1, 3:], rtol=0, atol=1e-6)
+    # every row to 1e-10, the last one (after the switching event) included: measured on GB300 4.9e-14
+    # (CSR) and 8.4e-15 (stencil) there; the oracle with its CG dot products summed in another order
+    # moves that row by 2.6e-14
+    np.testing.assert_allclose(rows[:, 3:], ref[:, 3:], rtol=0, atol=1e-10)
 
 
 @pytest.mark.parametrize("case,precision,operators", [("hex_me_rot", "DP", "csr"), ("hex_me_norot", "IR", "stencil"),
@@ -222,4 +223,4 @@ def test_cli_runs_a_yaml_config(tmp_path, capsys):
     ref = g["hysteresis"]
     assert rows.shape == ref.shape
     np.testing.assert_array_equal(rows[:, :3], ref[:, :3])
-    np.testing.assert_allclose(rows[:-1, 3:], ref[:-1, 3:], rtol=0, atol=1e-10)
+    np.testing.assert_allclose(rows[:, 3:], ref[:, 3:], rtol=0, atol=1e-10)

@@ -196,9 +196,9 @@ def test_batch_work_bytes_follow_the_grid():
     build()
     N.load()
     al = lambda b: (b + 255) // 256 * 256  # noqa: E731
-    assert work_bytes((10, 11, 12), 3, 1, "IR") == 4 * al(10 * 11 * 12 * 3 * 4)   # r, p, q, d in FP32
+    assert work_bytes((10, 11, 12), 3, 1, "IR") == 5 * al(10 * 11 * 12 * 3 * 4)   # r, p, q (w), d, s in FP32
     assert work_bytes((10, 11, 12), 1, 3, "DP") == 3 * al(10 * 11 * 12 * 3 * 8)   # r, p, q in FP64
-    assert work_bytes((9, 9, 9), 1, 1, "IR") == 4 * al(729 * 4)
+    assert work_bytes((9, 9, 9), 1, 1, "IR") == 5 * al(729 * 4)
     for dims, ncomp, nrhs in (((0, 4, 4), 1, 1), ((4, 4, 4), 2, 1), ((4, 4, 4), 1, 2)):
         with pytest.raises(ValueError):
             work_bytes(dims, ncomp, nrhs, "IR")
