@@ -10,8 +10,8 @@ with all operators and state resident in HBM.
                   [--precision DP|IR] [--operators csr|stencil] [--impl ours|reference]
 
 value:  steps/s over K steps timed with CUDA events (device-resident inputs;
-        about 12.9 GB resident at 128^3, far above the L2, so no flush is
-        needed); max over ranks.
+        about 1.1 GB resident at 128^3 with every operator matrix-free, far
+        above the L2, so no flush is needed); max over ranks.
 e2e:    the same steps through the public API with the magnetisation copied in
         from pinned host memory and the new m and <m> read back every step.
 fp64:   the same steps from the same m0 in plain FP64 on the same GPU, with
@@ -41,15 +41,6 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 METRIC = "LLG steps/s & SpMV HBM GB/s vs plain FP64 at |m| err<=1e-6; serving p50/p99"
-
-# CG iterations per solve of a warm-started 128^3 ME step (elasticity, demag,
-# g1n, g2n, g3n, g1*, g2*, m1**, m2**, m3**), measured on the GPU; used only to
-# extrapolate the CPU sample of --impl reference, which cannot afford the
-# full solves (a full CPU step takes tens of minutes).
-REFERENCE_ITERS = {"hex128_me": [1930, 375, 22, 30, 30, 22, 29, 30, 44, 44],
-                   "hex64_me": [960, 190, 22, 30, 30, 22, 29, 30, 44, 44],
-                   "hex32_plain": [95, 22, 30, 30, 22, 29, 30, 44, 44]}
-
 
 def elastic_launch_traffic(n_dof, elastic, steps):
     """DRAM bytes per elasticity-solve launch (ncu bytes per unknown-iteration x this run's iterations)
@@ -194,6 +185,36 @@ def cg_launch_bytes(A, nvec, iters, warm):
     per_it = spmv_bytes(A, nvec) + 6 * n * 8 * nvec
     head = (spmv_bytes(A, nvec) + 3 * n * 8 * nvec) if warm else 2 * n * 8 * nvec
     return head + iters * per_it
+
+
+def workload_config(args, w, S, p, world, ops_kind):
+    """The `config` object both arms print: the workload and its sizes (no run-specific values)."""
+    return {"workload": args.workload,
+            "mesh": (f"hex {w['n']}^3 periodic, defect {w['defect']}^3" if S.structured else
+                     f"{w['n']}^3 cube of Kuhn tets ({S.n_elements} tets, interior nodes jittered "
+                     f"+-{w['jitter']} h), {w['defect']} defect, seeded rotation"),
+            "n_dof": S.n_dof, "magnetoelastic": w["ME"], "rot111": w["rot111"],
+            "precision": args.precision, "operators": ops_kind, "tol": p.tol,
+            "sweep": f"+{w['B0']} T -> -{w['B0']} T over {w['steps']} steps",
+            "l2": ("inputs larger than L2 (the step's vectors alone are far above its 126 MB)"
+                   if S.n_dof * 33 * 8 > 4 * 126e6 else
+                   "inputs smaller than L2, not flushed (a latency-bound side workload, not the headline)"),
+            "parallelism": f"replicas x{world}"}
+
+
+def threaded_oracle_cg(axpy):
+    """oracle.cg.solve_cg with the CG's element-wise updates as row blocks on every host thread (the
+    products are threaded by the operators themselves); the same arithmetic as the single-threaded
+    oracle, so the same iterates."""
+    from oracle.cg import cg
+
+    def solve(A, b, M=None, x0=None, tol=1e-7, maxiter=5000, use_init=False, system=None, record=None, dot=None):
+        x, info = cg(A, b, x0=(x0 if use_init else None), tol=tol, maxiter=maxiter, record=record, axpy=axpy,
+                     dot=dot)
+        if info != 0:
+            raise RuntimeError(f"Error! CG for {system} did not converge. info={info}.")
+        return x
+    return solve
 
 
 # ------------------------------------------------------------------ CPU oracle sample
@@ -348,6 +369,7 @@ def run_ours(args):
     for s in range(args.warmup):
         L.step(fields[s])
         L.check()
+    resident_bytes = torch.cuda.memory_allocated()   # operators, state and CG workspaces
     stream = torch.cuda.current_stream()
     # per-CG-launch events and solver infos for the roofline of the CG kernel
     cg_events = []
@@ -461,8 +483,9 @@ def run_ours(args):
         del R
         torch.cuda.empty_cache()
 
+    resident_gb = resident_bytes / 1e9
     op_gb = sum(x.nbytes() for x in [L.A_demag, L.A1, L.A2, L.F1, L.Fx, L.F_el] + ([L.A_el] if L.ME else [])
-                if hasattr(x, "nbytes")) / 1e9
+                if x is not None and hasattr(x, "nbytes")) / 1e9
     serving = None
     if args.serve_requests > 0 and S.structured:
         # every rank serves its share of the request stream (no data-path collective)
@@ -490,16 +513,10 @@ def run_ours(args):
             "warmup": args.warmup, "ms_per_step": round(ms_max / args.steps, 3), "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64" if args.precision == "DP" else "f32+f64",
             "data": "synthetic (seeded m0 = normalise((1,0,0)+N(0,1e-3)), fixed field sweep)",
-            "config": {"workload": args.workload,
-                       "mesh": (f"hex {w['n']}^3 periodic, defect {w['defect']}^3" if S.structured else
-                                f"{w['n']}^3 cube of Kuhn tets ({S.n_elements} tets, interior nodes jittered "
-                                f"+-{w['jitter']} h), {w['defect']} defect, seeded rotation"),
-                       "n_dof": S.n_dof, "magnetoelastic": w["ME"], "rot111": w["rot111"],
-                       "precision": args.precision, "operators": ops_kind, "tol": p.tol, "sweep": f"+{w['B0']} T -> -{w['B0']} T over "
-                       f"{w['steps']} steps", "timed_steps": f"{args.warmup}..{args.warmup + args.steps - 1}",
-                       "l2": "inputs larger than L2 (operators %.1f GB resident)" % op_gb,
-                       "parallelism": f"replicas x{world}", "setup_s": round(t_setup, 1),
-                       "cg_iterations_per_step": [round(x, 1) for x in its_mean]},
+            "config": workload_config(args, w, S, p, world, ops_kind),
+            "run": {"timed_steps": f"{args.warmup}..{args.warmup + args.steps - 1}",
+                    "resident_gb": round(resident_gb, 2), "csr_operator_gb": round(op_gb, 2),
+                    "setup_s": round(t_setup, 1), "cg_iterations_per_step": [round(x, 1) for x in its_mean]},
             "e2e": {"value": round(e2e_value, 4), "unit": "steps/s",
                     "h2d_bytes_per_step": S.n_dof * 3 * 8, "d2h_bytes_per_step": S.n_dof * 3 * 8 + 24},
             "gpu_launches": launches,
@@ -518,43 +535,65 @@ def run_ours(args):
 
 # ------------------------------------------------------------------ reference arm
 def run_reference(args):
+    """The reference's CPU path for the step, measured: the oracle (the reference's step restated in
+    NumPy/SciPy; the reference itself needs CuPy and a CUDA GPU) with operators assembled on the host,
+    sparse products and CG updates on every host thread, every CG uncapped.  One cold step, then the
+    timed warm-started steps.  Workloads of a million DOFs or more time one step after one cold step
+    (a full 128^3 step takes minutes on the host cores), whatever --steps and --warmup ask."""
     rank, world, local = dist_env()
     if rank != 0:
         return None
     import numpy as np
-    import torch
+    import oracle.llg as OL
+    from oracle.threaded import ThreadedAxpy, threaded_operators
+    from oracle.volume_average import VolumeAverage as OVA
     from cupymag_gb300.core.assemble_simulation_operators import SimulationOperators
-    from cupymag_gb300.workloads import workload
+    from cupymag_gb300.workloads import seeded_m0, sweep_field, workload
 
     p, w = workload(args.workload)
-    dev = "cuda" if torch.cuda.is_available() else "cpu"
-    # setup only (not timed): the structured assembly builds the same CSR matrices
-    S = SimulationOperators(p, device=dev, mesh=w.get("mesh"))
-    its = REFERENCE_ITERS.get(args.workload)
-    if its is None:
-        print(json.dumps({"impl": "reference", "metric": METRIC, "unavailable":
-                          f"no measured FP64 iteration counts for workload {args.workload} to extrapolate the "
-                          f"sampled CPU step (known: {sorted(REFERENCE_ITERS)})"}))
-        return None
-    times = []
-    threads = 1
-    for s in range(args.warmup + args.steps):
-        cs = cpu_sample(p, S, its)
-        threads = cs["cores"]
-        if s >= args.warmup:
-            times.append(cs["t_step_est_s"])
+    t0 = time.perf_counter()
+    S = SimulationOperators(p, device="cpu", mesh=w.get("mesh"))
+    # row blocks on every host thread pay off for large grids only (thread hand-offs cost more than
+    # a 32^3 product)
+    ops, pool, threads = threaded_operators(S.host_operators(), None if S.n_dof >= 200_000 else 1)
+    Avg = OVA(S.node_coords_np, S.elements_np, S.global_id_np)
+    t_setup = time.perf_counter() - t0
+    big = S.n_dof >= 1_000_000
+    warmup, steps = (1, 1) if big else (args.warmup, args.steps)
+    nsw = w["steps"]
+    st = OL.LLGState(seeded_m0(S.n_dof, S.DefDOF, seed=1234), Avg.average)
+    orig = OL.solve_cg
+    OL.solve_cg = threaded_oracle_cg(ThreadedAxpy(pool, threads))
+    times, iters = [], []
+    try:
+        for s in range(warmup + steps):
+            st.iters = []
+            ts = time.perf_counter()
+            OL.llg_step(st, ops, Avg.average, p, sweep_field(p, s % nsw, nsw, w["B0"]), S.DefDOF)
+            if s >= warmup:
+                times.append(time.perf_counter() - ts)
+                iters.append(list(st.iters))
+    finally:
+        OL.solve_cg = orig
+        pool.shutdown()
     t = float(np.mean(times))
     value = 1.0 / t
+    ops_kind = args.operators or ("csr" if args.precision == "DP" or not S.structured else "stencil")
     line = {"impl": "reference", "metric": METRIC, "value": round(value, 6), "unit": "steps/s", "n_gpus": world,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(t * 1e3, 1), "higher_is_better": True,
+            "steps": steps, "warmup": warmup, "ms_per_step": round(t * 1e3, 1), "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": args.workload, "mesh": f"hex {w['n']}^3", "n_dof": S.n_dof},
+            "config": workload_config(args, w, S, p, world, ops_kind),
+            "run": {"steps_note": (f"{warmup} cold step then {steps} timed warm-started step(s)"
+                                   + (f" (--steps {args.steps} --warmup {args.warmup} cut: a full {w['n']}^3 "
+                                      f"oracle step takes minutes on the host cores)" if big else "")),
+                    "setup_s": round(t_setup, 1), "cg_iterations_per_step": iters,
+                    "measured": "every CG uncapped, wall time of the whole step; nothing extrapolated"},
             "cpu_baseline": {"value": round(value, 6), "unit": "steps/s", "cores": threads, "kind": "port",
-                             "sample": (f"CPU oracle (NumPy/SciPy restatement of the reference step; the reference "
-                                        f"itself needs CuPy and a CUDA GPU): each step = one {w['n']}^3 step with "
-                                        f"every CG capped at 3 iterations, timed per solve and extrapolated with "
-                                        f"the GPU-measured warm-start iteration counts {its}; sparse products and CG "
-                                        f"updates as row blocks on {threads} host threads")},
+                             "sample": (f"CPU oracle (NumPy/SciPy restatement of the reference step, whose own "
+                                        f"arithmetic is CuPy on a GPU): {steps} full warm-started {w['n']}^3 "
+                                        f"step(s) after {warmup} cold one, operators assembled on the host, "
+                                        f"sparse products and CG updates as row blocks on {threads} host threads, "
+                                        f"dot products single-threaded NumPy")},
             "e2e": {"value": round(value, 6), "unit": "steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
     return line

@@ -61,6 +61,15 @@ class BatchPlan(C.Structure):
                 ("precision", i32), ("total_chunks", i32), ("coef", dbl * 243)]
 
 
+class DerivStencilC(C.Structure):
+    _fields_ = [("nx", i32), ("ny", i32), ("nz", i32), ("pad", i32), ("fx", dbl * 27), ("fy", dbl * 27),
+                ("fz", dbl * 27)]
+
+
+class FelStencilC(C.Structure):
+    _fields_ = [("nx", i32), ("ny", i32), ("nz", i32), ("anchor", i32), ("coef", dbl * 486)]
+
+
 CG_INFO_BYTES = C.sizeof(CGInfo)
 
 _PROTOS = {
@@ -91,6 +100,9 @@ _PROTOS = {
     "cpm_build_E0": (C.c_int, [i64, vp, dbl, dbl, vp, vp, vp, vp]),
     "cpm_strain_from_u": (C.c_int, [C.POINTER(CSR), vp, vp, vp, vp, vp, vp]),
     "cpm_strain_finalize": (C.c_int, [i64, vp, vp, vp, dbl, dbl, vp, vp, vp, C.c_int, vp]),
+    "cpm_stencil_deriv": (C.c_int, [C.POINTER(DerivStencilC), vp, vp, dbl, C.c_int, vp, i64, vp]),
+    "cpm_stencil_strain": (C.c_int, [C.POINTER(DerivStencilC), vp, vp, vp, vp]),
+    "cpm_stencil_fel": (C.c_int, [C.POINTER(FelStencilC), vp, vp, vp]),
 }
 
 EXPORTED = tuple(_PROTOS)

@@ -178,6 +178,26 @@ class SimulationOperators:
             return A_el, self.elastic_rhs_operator()
         return self._coo_op("A_el"), self._coo_op("F_el")
 
+    def stencil_derivatives(self):
+        """Matrix-free Fx, Fy, Fz (StencilDerivatives: Hd, demag right-hand side, strain) for structured hex grids."""
+        from ..utils.stencil_derivatives import StencilDerivatives
+        if not self.structured:
+            raise ValueError("stencil derivatives need a structured hex grid (at least 3 cells per axis)")
+        g, e = self.fem_grid, self._cell()
+        fx, fy, fz = (SH.stencil_from_element(f).reshape(-1) for f in e["F"])
+        return StencilDerivatives(g.Nx, g.Ny, g.Nz, fx, fy, fz, self.device)
+
+    def stencil_coupling(self):
+        """Matrix-free F_el (StencilCoupling, anchor rows of DOF 0 empty); None without ME."""
+        from ..utils.stencil_derivatives import StencilCoupling
+        if not self.p.ME:
+            return None
+        if not self.structured:
+            raise ValueError("the stencil coupling needs a structured hex grid (at least 3 cells per axis)")
+        g, e = self.fem_grid, self._cell()
+        SF = SH.stencil_from_element(e["Fel"], 3, 6).reshape(3, 6, 27)
+        return StencilCoupling(g.Nx, g.Ny, g.Nz, SF.reshape(-1), anchor=True, device=self.device)
+
     def stencil_operators(self):
         """Matrix-free forms of A_demag, A1, A2, F1 (and A_el with ME) for structured hex grids."""
         from ..utils.stencil_operator import COL_EXCLUDED, ROW_IDENTITY, ROW_ZERO, StencilOperator
@@ -196,6 +216,15 @@ class SimulationOperators:
         if self.p.ME:
             out["A_el"] = mk(SH.stencil_from_element(e["Kel"], 3, 3).reshape(-1), pin)
         return out
+
+    def stencil_step_operators(self):
+        """Every operator of an LLG step in matrix-free form, as the tuple LLGSolver(ops=...) takes:
+        (A_demag, Fx, Fy, Fz, Deriv, A1, A2, F1, A_el, F_el, Avg) with Fx = Fy = Fz = None (the
+        derivatives act through Deriv).  The objects are read-only during a step, so runs of identical
+        grids and materials can share one tuple."""
+        so = self.stencil_operators()
+        return (so["A_demag"], None, None, None, self.stencil_derivatives(), so["A1"], so["A2"], so["F1"],
+                so.get("A_el"), self.stencil_coupling(), self.volume_average())
 
     def volume_average(self):
         return VolumeAverage(self.node_coords_np, self.elements_np, self.global_id_np, device=self.device)

@@ -29,6 +29,7 @@ from __future__ import annotations
 
 import ctypes as C
 import math
+import os
 
 import numpy as np
 import torch
@@ -49,6 +50,20 @@ SOLVE_NAMES = ["elasticity", "demag", "Gauss-Seidel g1n/g2n/g3n", "Gauss-Seidel 
 # iterations with any factor, so fewer FP64 products win (1e-4); demag is best near 1e-3.
 INNER_TOL = [0.1, 1e-3, 1e-4, 1e-4, 1e-4, 1e-4]
 
+# NVTX ranges around the stages of a step (magnetoelastic, demag, Gauss-Seidel projection) when
+# CPM_NVTX=1, so a profiler's timeline shows where a step's time goes; off by default (no calls).
+NVTX = os.environ.get("CPM_NVTX") == "1"
+
+
+def _range_push(name):
+    if NVTX:
+        torch.cuda.nvtx.range_push(name)
+
+
+def _range_pop():
+    if NVTX:
+        torch.cuda.nvtx.range_pop()
+
 
 class LLGSolver:
     """Device-resident state and operators of one LLG run."""
@@ -61,17 +76,13 @@ class LLGSolver:
         self.n = n = sim_ops.n_dof
         self.operators = operators
         if operators == "stencil":
-            # matrix-free forms of the solved operators and of F1 (structured hex
-            # grids); only the derivative matrices and F_el stay CSR
-            so = sim_ops.stencil_operators()
-            A_demag, A1, A2, F1 = so["A_demag"], so["A1"], so["A2"], so["F1"]
-            A_el = so.get("A_el")
+            # matrix-free forms of every operator of the step (structured hex grids): the solved
+            # operators, F1, the derivative matrices Fx, Fy, Fz and F_el; no CSR matrix is resident
             if ops is None:
-                Fx, Fy, Fz, Deriv = sim_ops.derivative_operators()
-                F_el = sim_ops.elastic_rhs_operator()
-                Avg = sim_ops.volume_average()
-            else:
-                _, Fx, Fy, Fz, Deriv, _, _, _, _, F_el, Avg = ops
+                ops = sim_ops.stencil_step_operators()
+            A_demag, Fx, Fy, Fz, Deriv, A1, A2, F1, A_el, F_el, Avg = ops
+            if not hasattr(A_demag, "ncomp"):
+                raise ValueError("operators='stencil' needs matrix-free operators in ops")
             if F_el is None and params.ME:
                 raise ValueError("magnetoelastic run without F_el")
         elif ops is None:
@@ -312,9 +323,15 @@ class LLGSolver:
         executor can collect the requests of several runs and solve them in
         one launch."""
         if self.ME:
+            _range_push("cpm magnetoelastic")
             yield from self._me_gen()
+            _range_pop()
+        _range_push("cpm demag")
         yield from self._demag_gen()
+        _range_pop()
+        _range_push("cpm gauss-seidel projection")
         yield from self._gs_gen(Hext)
+        _range_pop()
         self.nstep += 1
 
     # ------------------------------------------------------------------ results

@@ -47,18 +47,13 @@ NSLOTS = len(SOLVE_NAMES)
 
 
 def estimate_bytes(p, precision="IR") -> int:
-    """Device bytes one run holds (stencil operators, FP64 state, CSR derivative matrices).
-
-    Per DOF: 33 FP64 vectors of the step (51 with magnetoelastic coupling),
-    the volume-average weights, five flag arrays and the defect mask, the
-    three derivative matrices (27 non-zeros per row, shared indices), the
-    elastic right-hand-side matrix (3 rows x 162 non-zeros) with coupling, and
-    the block-diagonal CG vectors of the largest solve (3n unknowns: five FP32
-    or three FP64 vectors)."""
+    """Device bytes one run holds.  Every operator of a served run is matrix-free (stencils of the
+    solved operators, F1, Fx, Fy, Fz and F_el), so per DOF it is: 33 FP64 vectors of the step (51 with
+    magnetoelastic coupling), the volume-average weights, five flag arrays and the defect mask, and
+    the block-diagonal CG vectors of the largest solve (3n unknowns: five FP32 or three FP64
+    vectors)."""
     n = int(p.Nx) * int(p.Ny) * int(p.Nz)
-    per = (51 if p.ME else 33) * 8 + 8 + 6 + (4 + 27 * 4 + 3 * 27 * 8)
-    if p.ME:
-        per += 3 * 4 + 3 * 162 * 12
+    per = (51 if p.ME else 33) * 8 + 8 + 6
     per += 3 * (20 if precision != "DP" else 24)
     return int(per * n * 1.05) + (8 << 20)
 
@@ -116,6 +111,43 @@ class ServeStats:
         return self.steps / self.makespan_s if self.makespan_s > 0 else 0.0
 
 
+class OperatorCache:
+    """The matrix-free operators of a run, shared by runs of the same grid, defect and material.
+
+    Admission builds a run's mesh, DOF map, defect DOFs and stencil operators
+    (cupymag/core/assemble_simulation_operators.py:42-107) once per key
+    (edge, defect size and centre, coupling, rotation, the solved operators'
+    material and time-step constants) and hands every later run with that key
+    the same read-only objects.  Least recently used keys leave when the cache
+    holds `capacity` of them."""
+
+    def __init__(self, device, capacity=64):
+        self.dev = device
+        self.capacity = int(capacity)
+        self._d = {}
+        self.hits = self.misses = 0
+
+    @staticmethod
+    def key(p):
+        return (int(p.Nx), int(p.Ny), int(p.Nz), int(p.Ndx), int(p.Ndy), int(p.Ndz),
+                None if p.defect_center is None else tuple(float(v) for v in p.defect_center), bool(p.ME),
+                bool(p.rot111), float(p.alpha1), float(p.alpha2), float(p.c11), float(p.c12), float(p.c44))
+
+    def get(self, p):
+        k = self.key(p)
+        hit = self._d.pop(k, None)
+        if hit is None:
+            self.misses += 1
+            S = SimulationOperators(p, device=self.dev)
+            hit = (S, S.stencil_step_operators())
+            if len(self._d) >= self.capacity:
+                self._d.pop(next(iter(self._d)))
+        else:
+            self.hits += 1
+        self._d[k] = hit
+        return hit
+
+
 class _Group:
     """Runs of one size class: stepped together, with their own plans and CUDA graph."""
 
@@ -158,6 +190,7 @@ class ServingEngine:
         self.groups = {}
         self.used = 0
         self.stats = ServeStats()
+        self.cache = OperatorCache(self.dev)
 
     @property
     def active(self):
@@ -173,10 +206,10 @@ class ServingEngine:
     def admit(self, req, now):
         p = req.params()
         est = estimate_bytes(p, self.precision)
-        S = SimulationOperators(p, device=self.dev)
+        S, ops = self.cache.get(p)
         slot = self.free.pop()
         self.infos[slot].zero_()
-        L = LLGSolver(S, p, precision=self.precision, operators="stencil", info=self.infos[slot])
+        L = LLGSolver(S, p, precision=self.precision, operators="stencil", ops=ops, info=self.infos[slot])
         L.set_field_schedule(req.fields(p))
         L.set_magnetization(torch.as_tensor(req.initial_m(S.n_dof, S.DefDOF)))
         work = torch.empty(work_bytes((p.Nx, p.Ny, p.Nz), 3, 1, self.precision), dtype=torch.uint8,

@@ -284,6 +284,45 @@ size_t cpm_volavg_scratch_doubles(int ncomp);
 int cpm_volavg(int64_t n, int ncomp, const double *f, const double *w, double volume, const double *R9,
                double *out, double *scratch, void *stream);
 
+/* ---- matrix-free derivative and coupling operators (structured hex grids) ----
+ * On a grid of identical unit cells the derivative matrices F_i (F_i[p,q] =
+ * integral of N_p dN_q/dx_i, cupymag/physics/assemble_demag.py:95-184) and the
+ * magnetoelastic coupling F_el = B^T C S (assemble_elasticity.py:268-459) are
+ * 27-point periodic stencils, d = (dx+1)*9 + (dy+1)*3 + (dz+1) as for
+ * cpm_stencil.  These entry points apply them without the CSR matrices (FP64;
+ * results equal the CSR products to rounding).  Host structs; coefficients
+ * travel as launch parameters. */
+typedef struct {
+  int32_t nx, ny, nz;      /* cells per axis (>= 3) */
+  int32_t pad;
+  double fx[27], fy[27], fz[27];  /* stencils of Fx, Fy, Fz */
+} cpm_deriv_stencil;
+
+/* Matrix-free form of cpm_spmv_csr_multi: mode 0 (compute_Hd_from_U,
+ * cupymag/utils/compute_derivatives.py:36-58): y[i,k] = alpha (F_k x)_i, x (n,),
+ * y (n,3); mode 1 (demag right-hand side, cupymag/core/Micromagnetics.py:166-168):
+ * y[i] = alpha sum_k (F_k (x[:,k] - shift[k]))_i, y[pin] = 0 if pin >= 0,
+ * x (n,3), shift device double[3] or NULL. */
+int cpm_stencil_deriv(const cpm_deriv_stencil *D, const double *x, double *y, double alpha, int mode,
+                      const double *shift, int64_t pin, void *stream);
+
+/* Matrix-free form of cpm_strain_from_u (compute_derivatives.py:60-125): E
+ * (n,6) Voigt strain from u = [ux|uy|uz]; R9 (row-major 3x3, device) or NULL.
+ * E 16-byte aligned. */
+int cpm_stencil_strain(const cpm_deriv_stencil *D, const double *u, const double *R9, double *E, void *stream);
+
+typedef struct {
+  int32_t nx, ny, nz;      /* cells per axis (>= 3) */
+  int32_t anchor;          /* 1: rows of DOF 0 (b_el[0], b_el[n], b_el[2n]) are empty, as the reference's
+                              F_el anchors them (assemble_elasticity.py:461-527) */
+  double coef[486];        /* coef[(a*6 + v)*27 + d]: displacement component a, Voigt column v */
+} cpm_fel_stencil;
+
+/* b_el (3n, [x|y|z]) = F_el E0 with E0 (6n, node-interleaved Voigt, 16-byte
+ * aligned): the right-hand side of the elastic solve (Micromagnetics.py:123)
+ * without the 162-non-zero-per-row CSR matrix. */
+int cpm_stencil_fel(const cpm_fel_stencil *F, const double *E0, double *b_el, void *stream);
+
 /* Magnetostrictive eigenstrain E0 (6n, node-interleaved Voigt with doubled
  * shears), cupymag/utils/final_assembly.py:208-266.  With R9/M36 (both or
  * neither) it is built from m100 = m R and rotated per node by M^T

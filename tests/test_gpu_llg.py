@@ -224,3 +224,21 @@ def test_cli_runs_a_yaml_config(tmp_path, capsys):
     assert rows.shape == ref.shape
     np.testing.assert_array_equal(rows[:, :3], ref[:, :3])
     np.testing.assert_allclose(rows[:, 3:], ref[:, 3:], rtol=0, atol=1e-10)
+
+
+def test_nvtx_ranges_mark_the_stages_of_a_step(monkeypatch):
+    """With CPM_NVTX=1 a step opens and closes one NVTX range per stage, in the step's order."""
+    import cupymag_gb300.physics.llg as LL
+    g = G.load("hex_me_rot")
+    p = G.params(g)
+    L = LL.LLGSolver(_ops(g, p), p)
+    L.set_magnetization(torch.as_tensor(g["m0"]))
+    seen = []
+    monkeypatch.setattr(LL, "NVTX", True)
+    monkeypatch.setattr(torch.cuda.nvtx, "range_push", lambda name: seen.append(("push", name)))
+    monkeypatch.setattr(torch.cuda.nvtx, "range_pop", lambda: seen.append(("pop", None)))
+    L.step(p.Hext)
+    L.check()
+    names = [nm for op, nm in seen if op == "push"]
+    assert names == ["cpm magnetoelastic", "cpm demag", "cpm gauss-seidel projection"]
+    assert [op for op, _ in seen] == ["push", "pop"] * 3

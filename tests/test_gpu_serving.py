@@ -97,3 +97,18 @@ def test_realtime_arrivals_overlap():
     assert st.failed == 0 and st.max_batch >= 2
     assert all(res[r.rid].steps == r.steps for r in reqs)
     assert st.latency_p99_s >= st.latency_p50_s > 0
+
+
+def test_operator_cache_shares_operators_of_identical_grids():
+    """Runs with the same grid, defect and material share one set of matrix-free operators; their results
+    are the ones each has when served by an engine of its own."""
+    from cupymag_gb300.serving import Request, ServingEngine
+    reqs = [Request(0, 10, 2, True, 0.1, 3, 21), Request(1, 10, 2, True, 0.15, 3, 22),
+            Request(2, 10, 2, False, 0.1, 3, 23), Request(3, 10, 2, True, 0.05, 3, 24)]
+    eng = ServingEngine("IR", keep_m=True)
+    res, st = eng.serve(reqs, realtime=False)
+    assert st.failed == 0
+    assert eng.cache.misses == 2 and eng.cache.hits == 2
+    for r in reqs:
+        alone, _ = ServingEngine("IR", keep_m=True).serve([r], realtime=False)
+        assert np.array_equal(alone[r.rid].m, res[r.rid].m), r.rid

@@ -175,3 +175,39 @@ def test_two_barrier_fp32_cg_reaches_the_fp64_stopping_test(edge):
         print(name, nrhs, "three-barrier", its[0], "two-barrier", its[2])
         for a, c in zip(its[0], its[2]):
             assert c <= 1.5 * a + 3, (name, nrhs, its)
+
+
+@pytest.mark.parametrize("dims", [(6, 6, 6), (7, 5, 9), (4, 4, 4), (12, 10, 8)])
+@pytest.mark.parametrize("rot", [False, True])
+def test_matrix_free_derivatives_and_coupling_match_csr(dims, rot):
+    """Hd = -F U, the demag right-hand side (shifted by <m>, pinned at DOF 0), the strain from u (with and
+    without the [111] rotation) and b_el = F_el E0 (anchor rows empty), matrix-free against the CSR
+    matrices of the same grid, to 1e-13 of the largest value."""
+    from oracle.llg import R_matrix, strain_from_u
+    S, p = _sim(Nx=dims[0], Ny=dims[1], Nz=dims[2], Ndx=2, Ndy=2, Ndz=1, ME=True, rot111=rot)
+    D = S.stencil_derivatives()
+    F = S.stencil_coupling()
+    h = S.host_operators()
+    n = S.n_dof
+    rng = np.random.default_rng(sum(dims) + rot)
+    dev = lambda a: torch.as_tensor(np.ascontiguousarray(a), device="cuda")  # noqa: E731
+
+    def close(got, ref, what):
+        np.testing.assert_allclose(got, ref, rtol=0, atol=1e-13 * np.abs(ref).max(), err_msg=what)
+
+    U = rng.normal(size=n)
+    Hd = D.hd_into(dev(U), torch.empty((n, 3), dtype=torch.float64, device="cuda")).cpu().numpy()
+    close(Hd, -np.stack([h["Fx"] @ U, h["Fy"] @ U, h["Fz"] @ U], axis=1), "Hd")
+    m = rng.normal(size=(n, 3))
+    avg = rng.normal(size=3)
+    b = D.demag_rhs_into(dev(m), dev(avg), torch.empty(n, dtype=torch.float64, device="cuda"), pin=0).cpu().numpy()
+    mt = m - avg
+    ref = -(h["Fx"] @ mt[:, 0] + h["Fy"] @ mt[:, 1] + h["Fz"] @ mt[:, 2])
+    ref[0] = 0.0
+    close(b, ref, "demag rhs")
+    u = rng.normal(size=3 * n)
+    R = R_matrix() if rot else None
+    E = D.compute_E_from_u(n, dev(u), None if R is None else dev(R)).cpu().numpy()
+    close(E, strain_from_u(h, n, u, R), "strain")
+    E0 = rng.normal(size=6 * n)
+    close(F.spmv(dev(E0)).cpu().numpy(), h["F_el"] @ E0, "F_el E0")

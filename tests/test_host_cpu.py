@@ -262,4 +262,5 @@ def test_memory_estimate_grows_with_size_and_coupling():
     b = estimate_bytes(hex_params(32, 4, True, True))
     c = estimate_bytes(hex_params(64, 4, True, True))
     assert a < b < c
-    assert 5e9 < estimate_bytes(hex_params(96, 12, True, True)) < 8e9
+    # matrix-free operators: about 500 bytes per DOF at 96^3 with coupling
+    assert 0.3e9 < estimate_bytes(hex_params(96, 12, True, True)) < 0.8e9
