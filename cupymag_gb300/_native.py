@@ -70,6 +70,11 @@ class FelStencilC(C.Structure):
     _fields_ = [("nx", i32), ("ny", i32), ("nz", i32), ("anchor", i32), ("coef", dbl * 486)]
 
 
+class FftPrecondC(C.Structure):
+    _fields_ = [("nx", i32), ("ny", i32), ("nz", i32), ("ncomp", i32), ("dev", vp), ("bytes", i64),
+                ("npass", i32 * 3), ("radix", (i32 * 16) * 3)]
+
+
 CG_INFO_BYTES = C.sizeof(CGInfo)
 
 _PROTOS = {
@@ -103,6 +108,12 @@ _PROTOS = {
     "cpm_stencil_deriv": (C.c_int, [C.POINTER(DerivStencilC), vp, vp, dbl, C.c_int, vp, i64, vp]),
     "cpm_stencil_strain": (C.c_int, [C.POINTER(DerivStencilC), vp, vp, vp, vp]),
     "cpm_stencil_fel": (C.c_int, [C.POINTER(FelStencilC), vp, vp, vp]),
+    "cpm_fft_precond_bytes": (i64, [i32, i32, i32, i32]),
+    "cpm_fft_precond_build": (C.c_int, [C.POINTER(Stencil), vp, i64, C.POINTER(FftPrecondC), vp]),
+    "cpm_fft_precond_apply": (C.c_int, [C.POINTER(FftPrecondC), vp, vp, vp, i64, vp]),
+    "cpm_cg_fft_workspace_bytes": (C.c_size_t, [i32, i32, i32, i32]),
+    "cpm_cg_solve_stencil_fft": (C.c_int, [C.POINTER(Stencil), C.POINTER(FftPrecondC), vp, vp, C.POINTER(CGOpts),
+                                           vp, C.c_size_t, vp, vp]),
 }
 
 EXPORTED = tuple(_PROTOS)

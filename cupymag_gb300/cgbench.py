@@ -3,7 +3,7 @@
     python -m cupymag_gb300.cgbench [--edge 128] [--op A_el|A_demag|A1|A2] [--nrhs 1|3]
                                     [--precision IR|DP] [--operators stencil|csr]
                                     [--solves 3] [--maxiter 20000] [--batch 1] [--batched]
-                                    [--form 0|1|2]
+                                    [--form 0|1|2] [--precond fft]
 
 Builds only the requested operator (the magnetoelastic 128^3 material), a
 seeded right-hand side with the reference's pins (b[0] = 0 for A_demag,
@@ -50,6 +50,8 @@ def main(argv=None):
                     help="reliable-update factor of the FP32 solver (residual drop between FP64 updates)")
     ap.add_argument("--form", type=int, default=0, choices=[0, 1, 2],
                     help="FP32 stencil solver: 0 default (three barriers), 1 three-barrier, 2 two-barrier")
+    ap.add_argument("--precond", default=None, choices=["fft"],
+                    help="FP32 stencil solve preconditioned by the circulant inverse (FFT) inside FP64 refinement")
     args = ap.parse_args(argv)
 
     from . import _native as N
@@ -98,7 +100,8 @@ def main(argv=None):
 
         def launch():
             solver.launch(op, bd, x, info[0], tol=p.tol, maxiter=args.maxiter, precision=args.precision,
-                          form=args.form)
+                          form=args.form, precond=args.precond,
+                          inner_tol=1e-4 if args.precond else args.inner_tol)
         info_of = lambda: info[0]  # noqa: E731
     for _ in range(args.solves):
         e0 = torch.cuda.Event(enable_timing=True)
@@ -115,7 +118,7 @@ def main(argv=None):
     ms = float(np.median(times))
     nb = _bytes(op, nrhs, its, d["outer"], args.precision == "IR", csr) * args.batch
     print(json.dumps({"op": args.op, "edge": args.edge, "n": n, "nrhs": nrhs, "precision": args.precision,
-                      "inner_tol": args.inner_tol, "form": args.form,
+                      "inner_tol": args.inner_tol, "form": args.form, "precond": args.precond,
                       "operators": args.operators, "batch": args.batch,
                       "kernel": "blockdiag" if args.batch > 1 or args.batched else "single",
                       "status": N.STATUS_NAMES[d["status"]],

@@ -50,6 +50,13 @@ SOLVE_NAMES = ["elasticity", "demag", "Gauss-Seidel g1n/g2n/g3n", "Gauss-Seidel 
 # iterations with any factor, so fewer FP64 products win (1e-4); demag is best near 1e-3.
 INNER_TOL = [0.1, 1e-3, 1e-4, 1e-4, 1e-4, 1e-4]
 
+# Solves that the precision form runs as FFT-preconditioned CG on stencil operators: elasticity and demag,
+# whose operators are circulant apart from the anchor at DOF 0 (the Gauss-Seidel operators A1/A2 carry
+# the defect rows and columns, and plain FP32 CG already needs only 20-55 iterations there).  Each inner
+# preconditioned solve lowers the residual 1e4-fold before the next FP64 residual.
+FFT_SLOTS = (0, 1)
+FFT_INNER_TOL = 1e-4
+
 # NVTX ranges around the stages of a step (magnetoelastic, demag, Gauss-Seidel projection) when
 # CPM_NVTX=1, so a profiler's timeline shows where a step's time goes; off by default (no calls).
 NVTX = os.environ.get("CPM_NVTX") == "1"
@@ -68,9 +75,18 @@ def _range_pop():
 class LLGSolver:
     """Device-resident state and operators of one LLG run."""
 
-    def __init__(self, sim_ops, params, precision="DP", device=None, ops=None, operators="csr", info=None):
+    def __init__(self, sim_ops, params, precision="DP", device=None, ops=None, operators="csr", info=None,
+                 precond="auto"):
+        """precond: "fft" runs the elastic and demag solves of the precision form as FFT-preconditioned CG
+        (stencil operators only), None runs every solve as plain CG; "auto" is "fft" for the precision
+        form on stencil operators."""
         self.p = params
         self.precision = "DP" if precision == "DP" else "IR"
+        if precond == "auto":
+            precond = "fft" if (self.precision == "IR" and operators == "stencil") else None
+        if precond not in (None, "fft"):
+            raise ValueError(f"unknown preconditioner {precond!r}")
+        self.precond = precond
         self.dev = device or sim_ops.device
         dev = self.dev
         self.n = n = sim_ops.n_dof
@@ -218,8 +234,10 @@ class LLGSolver:
 
     def _cg(self, A, b, x, k):
         self.launches += 1
+        fft = self.precond == "fft" and k in FFT_SLOTS
         self.solver.launch(A, b, x, self.info[k], tol=self.p.tol, maxiter=self.p.maxiter,
-                           use_init_dev=self.use_init, precision=self.precision, inner_tol=INNER_TOL[k])
+                           use_init_dev=self.use_init, precision=self.precision,
+                           inner_tol=FFT_INNER_TOL if fft else INNER_TOL[k], precond="fft" if fft else None)
 
     def cg_request(self, A, b, x, k):
         """A solve of this step, for an executor that batches solves of several runs."""

@@ -44,12 +44,19 @@ class CGSolver:
         return ws
 
     def launch(self, A: DeviceCSR, b: torch.Tensor, x: torch.Tensor, info: torch.Tensor, *, tol, maxiter,
-               use_init=False, use_init_dev: torch.Tensor = None, precision="DP", inner_tol=None, form=0):
+               use_init=False, use_init_dev: torch.Tensor = None, precision="DP", inner_tol=None, form=0,
+               precond=None):
         """Asynchronous solve; x is read as x0 when use_init, and overwritten.
 
         form (FP32 stencil solves): N.CG_FORM_DEFAULT (three grid barriers per iteration),
-        N.CG_FORM_THREE_BARRIER or N.CG_FORM_TWO_BARRIER (opt-in)."""
+        N.CG_FORM_THREE_BARRIER or N.CG_FORM_TWO_BARRIER (opt-in).
+        precond="fft" (FP32 form on a stencil operator with one right-hand side): CG preconditioned by
+        the operator's circulant inverse inside FP64 refinement (inner_tol: the residual drop of each
+        inner solve); the plain FP32 form is used where the grid has no FFT plan."""
         prec = PRECISIONS[precision] if isinstance(precision, str) else int(precision)
+        if precond == "fft" and prec == 1 and hasattr(A, "fft_plan") and b.dim() == 1 and A.fft_plan() is not None:
+            return self._launch_fft(A, b, x, info, tol=tol, maxiter=maxiter, use_init=use_init,
+                                    use_init_dev=use_init_dev, inner_tol=inner_tol)
         if prec == 1:
             A.ensure_fp32()
         n = A.shape[0]
@@ -73,6 +80,29 @@ class CGSolver:
         fn = N.lib().cpm_cg_solve_stencil if stencil else N.lib().cpm_cg_solve
         N.check(fn(A.struct(), b.data_ptr(), x.data_ptr(), nrhs, C.byref(o), ws.data_ptr(), ws.numel(),
                    info.data_ptr(), N.stream_ptr()), "cpm_cg_solve")
+
+
+    def _launch_fft(self, A, b, x, info, *, tol, maxiter, use_init, use_init_dev, inner_tol):
+        if b.shape[0] != A.shape[0] or x.shape != b.shape or b.dtype != torch.float64 or x.dtype != torch.float64 \
+                or not (b.is_contiguous() and x.is_contiguous()):
+            raise ValueError("b and x must be contiguous float64 device vectors of the operator's size")
+        key = ("fft", A.nx, A.ny, A.nz, A.ncomp)
+        ws = self._ws.get(key)
+        if ws is None:
+            nbytes = N.lib().cpm_cg_fft_workspace_bytes(A.nx, A.ny, A.nz, A.ncomp)
+            ws = torch.zeros(nbytes, dtype=torch.uint8, device=self.device)
+            self._ws[key] = ws
+        o = N.CGOpts()
+        o.tol = float(tol)
+        o.maxiter = int(maxiter)
+        o.use_init_host = 1 if use_init else 0
+        o.use_init_dev = use_init_dev.data_ptr() if use_init_dev is not None else None
+        o.precision = 1
+        o.inner_tol = 1e-4 if inner_tol is None else float(inner_tol)
+        o.barrier_timeout_s = self.barrier_timeout_s
+        N.check(N.lib().cpm_cg_solve_stencil_fft(A.struct(), A.fft_plan(), b.data_ptr(), x.data_ptr(), C.byref(o),
+                                                 ws.data_ptr(), ws.numel(), info.data_ptr(), N.stream_ptr()),
+                "cpm_cg_solve_stencil_fft")
 
 
 def new_info(count=1, device=None) -> torch.Tensor:

@@ -84,6 +84,36 @@ class StencilOperator:
     def __matmul__(self, x):
         return self.spmv(x)
 
+    def fft_plan(self):
+        """The circulant-inverse preconditioner of this operator (built once; None when the grid's
+        dimensions are not supported)."""
+        if getattr(self, "_fft", None) is None:
+            nb = int(N.lib().cpm_fft_precond_bytes(self.nx, self.ny, self.nz, self.ncomp))
+            if nb <= 0:
+                return None
+            mem = torch.empty(nb, dtype=torch.uint8, device=self.device)
+            if mem.data_ptr() % 256:
+                raise RuntimeError("plan memory is not 256-byte aligned")
+            plan = N.FftPrecondC()
+            N.check(N.lib().cpm_fft_precond_build(self.struct(), mem.data_ptr(), nb, plan, N.stream_ptr()),
+                    "cpm_fft_precond_build")
+            self._fft = (plan, mem)
+        return self._fft[0]
+
+    def precondition32(self, r: torch.Tensor, out: torch.Tensor = None) -> torch.Tensor:
+        """z = M r with M the circulant-inverse preconditioner (FP32), as the preconditioned solve applies it."""
+        plan = self.fft_plan()
+        if plan is None:
+            raise ValueError(f"no FFT preconditioner for a {self.nx} x {self.ny} x {self.nz} grid")
+        r = r.contiguous()
+        if r.dtype != torch.float32 or r.numel() != self.shape[0]:
+            raise ValueError("r must be a float32 vector of the operator's size")
+        out = torch.empty_like(r) if out is None else out
+        work = torch.empty(8 * r.numel(), dtype=torch.uint8, device=r.device)
+        N.check(N.lib().cpm_fft_precond_apply(plan, r.data_ptr(), out.data_ptr(), work.data_ptr(), work.numel(),
+                                              N.stream_ptr()), "cpm_fft_precond_apply")
+        return out
+
     # the same operator with unit (and excluded) rows at the given DOFs
     @staticmethod
     def flags_for(n, dofs, bits):
