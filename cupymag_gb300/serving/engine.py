@@ -39,22 +39,30 @@ import torch
 
 from .. import _native as N
 from ..core.assemble_simulation_operators import SimulationOperators
-from ..physics.llg import INNER_TOL, SOLVE_NAMES, LLGSolver
+from ..physics.llg import FFT_SLOTS, INNER_TOL, SOLVE_NAMES, LLGSolver
 from ..solvers.linear_solvers import decode_info
 from .blockdiag import BlockDiagPlan, BlockSystem, coef_key, work_bytes
 
 NSLOTS = len(SOLVE_NAMES)
+# Runs of at least this many DOFs solve elasticity and demag with the FFT-preconditioned solver, one launch
+# per run; smaller runs keep them in the block-diagonal launches (latency-bound either way).
+FFT_MIN_DOFS = 32 ** 3
 
 
 def estimate_bytes(p, precision="IR") -> int:
     """Device bytes one run holds.  Every operator of a served run is matrix-free (stencils of the
     solved operators, F1, Fx, Fy, Fz and F_el), so per DOF it is: 33 FP64 vectors of the step (51 with
-    magnetoelastic coupling), the volume-average weights, five flag arrays and the defect mask, and
-    the block-diagonal CG vectors of the largest solve (3n unknowns: five FP32 or three FP64
-    vectors)."""
+    magnetoelastic coupling), the volume-average weights, five flag arrays and the defect mask, the
+    block-diagonal CG vectors of the largest solve (3n unknowns: five FP32 or three FP64 vectors), and
+    for runs that solve elasticity and demag with the FFT-preconditioned solver its workspace and
+    plans."""
     n = int(p.Nx) * int(p.Ny) * int(p.Nz)
     per = (51 if p.ME else 33) * 8 + 8 + 6
     per += 3 * (20 if precision != "DP" else 24)
+    if precision != "DP" and n >= FFT_MIN_DOFS:
+        # FFT-preconditioned solves: workspace (five FP32 vectors and a complex field of 3n unknowns) and
+        # the plans' inverse symbols (6 floats per DOF elastic, 1 demag)
+        per += 3 * (20 + 8) + 4 * (6 + 1)
     return int(per * n * 1.05) + (8 << 20)
 
 
@@ -104,6 +112,7 @@ class ServeStats:
     peak_budget_gb: float = 0.0
     graph_error: str = None
     blockdiag_launches: int = 0
+    fft_launches: int = 0
     extra: dict = field(default_factory=dict)
 
     @property
@@ -229,11 +238,22 @@ class ServingEngine:
         return run
 
     # ------------------------------------------------------------------ one batched step of a group
+    def _fft_solve(self, L, k, A):
+        """Whether slot k of run L is solved alone with the FFT-preconditioned solver (precision form,
+        elasticity or demag, a grid of at least FFT_MIN_DOFS DOFs with an FFT plan) instead of in the
+        block-diagonal launch.  It depends on the run alone, so a run's result is the same in any mix."""
+        return (self.precision == "IR" and L.precond == "fft" and k in FFT_SLOTS and L.n >= FFT_MIN_DOFS
+                and A.fft_plan() is not None)
+
     def _build_plans(self, g):
         sys_by_key = {}
+        fft = {k: [] for k in range(NSLOTS)}
         for run in g.runs:
             L = run.solver
             for k, A, b, x in L.solve_slots():
+                if self._fft_solve(L, k, A):
+                    fft[k].append((run, A, b, x))
+                    continue
                 key = (k, A.ncomp, 1 if b.dim() == 1 else int(b.shape[1]), coef_key(A))
                 sys_by_key.setdefault(key, []).append(
                     BlockSystem(A, b, x, L.info[k], run.work, L.p.tol, L.p.maxiter, L.use_init))
@@ -241,6 +261,7 @@ class ServingEngine:
         for key, systems in sys_by_key.items():
             plans[key[0]].append(BlockDiagPlan(systems, self.precision, device=self.dev, inner_tol=INNER_TOL[key[0]]))
         g.plans = plans
+        g.fft = fft
 
     def _step_runs(self, g):
         """Launch one step of every run of the group: element-wise kernels per run, one CG launch per slot."""
@@ -260,6 +281,9 @@ class ServingEngine:
                 else:
                     plan.launch()
                 self.stats.blockdiag_launches += 1
+            for run, A, b, x in g.fft[k]:
+                run.solver._cg(A, b, x, k)
+                self.stats.fft_launches += 1
             for i in idx:
                 cur[i] = next(gens[i], None)
         if any(q is not None for q in cur):

@@ -78,7 +78,8 @@ def test_budget_admission_serialises_runs():
 def test_estimate_covers_allocation():
     from cupymag_gb300.serving import ServingEngine, estimate_bytes
     from cupymag_gb300.serving.workload import Request
-    for r in (Request(0, 24, 4, True, 0.1, 1, 1), Request(1, 24, 4, False, 0.1, 1, 2)):
+    for r in (Request(0, 24, 4, True, 0.1, 1, 1), Request(1, 24, 4, False, 0.1, 1, 2),
+              Request(2, 32, 4, True, 0.1, 1, 3), Request(3, 34, 0, False, 0.1, 1, 4)):
         eng = ServingEngine("IR")
         torch.cuda.synchronize()
         before = torch.cuda.memory_allocated()
@@ -112,3 +113,21 @@ def test_operator_cache_shares_operators_of_identical_grids():
     for r in reqs:
         alone, _ = ServingEngine("IR", keep_m=True).serve([r], realtime=False)
         assert np.array_equal(alone[r.rid].m, res[r.rid].m), r.rid
+
+
+def test_fft_solved_runs_are_the_same_alone_and_in_the_mix():
+    """Runs of 32^3 and up solve elasticity and demag with the FFT-preconditioned solver, one launch per
+    run, beside block-diagonal launches for the small runs: every result is the same alone and in the mix
+    (bit for bit) and within 1e-6 of the same run in plain FP64."""
+    from cupymag_gb300.serving import Request, ServingEngine, run_sequential
+    reqs = [Request(0, 32, 4, True, 0.12, 4, 31), Request(1, 10, 2, False, 0.07, 4, 32),
+            Request(2, 34, 0, False, 0.1, 3, 33), Request(3, 8, 2, True, 0.2, 5, 34)]
+    eng = ServingEngine("IR", keep_m=True)
+    mix, st = eng.serve(reqs, realtime=False)
+    assert st.failed == 0 and st.fft_launches > 0 and st.graph_steps > 0
+    seq, _ = run_sequential(reqs, precision="DP", keep_m=True)
+    for r in reqs:
+        alone, _ = ServingEngine("IR", keep_m=True).serve([r], realtime=False)
+        assert np.array_equal(alone[r.rid].m, mix[r.rid].m), r.rid
+        assert np.array_equal(alone[r.rid].hist, mix[r.rid].hist), r.rid
+        assert np.abs(mix[r.rid].m - seq[r.rid].m).max() <= 1e-6, r.rid
