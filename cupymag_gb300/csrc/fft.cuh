@@ -79,7 +79,7 @@ __device__ __forceinline__ void butterfly<3>(float2 (&v)[3], bool inverse) {
 // One Stockham pass of radix R (2, 3 or 4): every work item is one butterfly j of a
 // line, with the pre-twiddles W^(r (j % Ns) n / (Ns R)) (exponents below n, no wrap).
 template <int R>
-__device__ __forceinline__ void stockham_pass(const float2 *src, float2 *dst, int n, int lines, int Ns,
+__device__ __forceinline__ void stockham_pass(const float2 *src, float2 *dst, int n, int ld, int lines, int Ns,
                                               const float2 *tw, bool inverse) {
   const int m = n / R;
   const int span = n / (Ns * R);
@@ -89,7 +89,7 @@ __device__ __forceinline__ void stockham_pass(const float2 *src, float2 *dst, in
     const int j = b - line * m;
     const int jd = j / Ns;
     const int k = j - jd * Ns;
-    const float2 *in = src + line * n + j;
+    const float2 *in = src + line * ld + j;
     float2 v[R];
 #pragma unroll
     for (int r = 0; r < R; ++r) v[r] = in[r * m];
@@ -102,15 +102,15 @@ __device__ __forceinline__ void stockham_pass(const float2 *src, float2 *dst, in
       }
     }
     butterfly<R>(v, inverse);
-    float2 *out = dst + line * n + jd * Ns * R + k;
+    float2 *out = dst + line * ld + jd * Ns * R + k;
 #pragma unroll
     for (int r = 0; r < R; ++r) out[r * Ns] = v[r];
   }
 }
 
 // Any radix R: every work item is one output (j, q), R complex multiply-adds.
-__device__ __forceinline__ void stockham_pass_any(const float2 *src, float2 *dst, int n, int lines, int Ns, int R,
-                                                  const float2 *tw, bool inverse) {
+__device__ __forceinline__ void stockham_pass_any(const float2 *src, float2 *dst, int n, int ld, int lines, int Ns,
+                                                  int R, const float2 *tw, bool inverse) {
   const int m = n / R;
   const int span = n / (Ns * R);
   const int total = lines * n;
@@ -121,7 +121,7 @@ __device__ __forceinline__ void stockham_pass_any(const float2 *src, float2 *dst
     const int j = o - q * m;
     const int k = j % Ns;
     const int bt = k * span + q * m;  // twiddle exponent of input r is r * bt (mod n); bt < n
-    const float2 *in = src + line * n + j;
+    const float2 *in = src + line * ld + j;
     float2 acc = make_float2(0.0f, 0.0f);
     int t = 0;
     for (int r = 0; r < R; ++r) {
@@ -133,25 +133,30 @@ __device__ __forceinline__ void stockham_pass_any(const float2 *src, float2 *dst
       t += bt;
       if (t >= n) t -= n;
     }
-    dst[line * n + (j / Ns) * Ns * R + k + q * Ns] = acc;
+    dst[line * ld + (j / Ns) * Ns * R + k + q * Ns] = acc;
   }
 }
 
-// 1D DFTs of `lines` lines of length ax.n stored at buf[line * ax.n + i] (shared
-// memory), with scratch of the same size; returns the buffer holding the
-// result.  inverse: conjugate twiddles, no scaling.  All threads of the block
-// take part; ends with a block barrier.
+// Shared-memory stride of a line of length n: odd, so that threads walking
+// across lines (the tile loads of the y and x passes) hit different banks.
+__host__ __device__ __forceinline__ int line_stride(int n) { return n | 1; }
+
+// 1D DFTs of `lines` lines of length ax.n stored at buf[line * line_stride(n) + i]
+// (shared memory), with scratch of the same size; returns the buffer holding
+// the result.  inverse: conjugate twiddles, no scaling.  All threads of the
+// block take part; ends with a block barrier.
 __device__ __forceinline__ float2 *dft_lines(float2 *buf, float2 *scratch, const FftAxis &ax, int lines,
                                              bool inverse) {
   const int n = ax.n;
+  const int ld = line_stride(n);
   float2 *src = buf, *dst = scratch;
   int Ns = 1;
   for (int s = 0; s < ax.npass; ++s) {
     const int R = ax.radix[s];
-    if (R == 4) stockham_pass<4>(src, dst, n, lines, Ns, ax.tw, inverse);
-    else if (R == 2) stockham_pass<2>(src, dst, n, lines, Ns, ax.tw, inverse);
-    else if (R == 3) stockham_pass<3>(src, dst, n, lines, Ns, ax.tw, inverse);
-    else stockham_pass_any(src, dst, n, lines, Ns, R, ax.tw, inverse);
+    if (R == 4) stockham_pass<4>(src, dst, n, ld, lines, Ns, ax.tw, inverse);
+    else if (R == 2) stockham_pass<2>(src, dst, n, ld, lines, Ns, ax.tw, inverse);
+    else if (R == 3) stockham_pass<3>(src, dst, n, ld, lines, Ns, ax.tw, inverse);
+    else stockham_pass_any(src, dst, n, ld, lines, Ns, R, ax.tw, inverse);
     __syncthreads();
     float2 *tmp = src;
     src = dst;

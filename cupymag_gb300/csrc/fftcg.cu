@@ -52,11 +52,18 @@ __device__ void pass_z_fwd(const FftGrid &g, const float *r, float2 *s0, float2 
     const int c = tile / per, l0 = (tile - c * per) * g.lz;
     const int L = min(g.lz, nlines - l0);
     const float *src = r + (int64_t)c * g.n + (int64_t)l0 * g.nz;
-    for (int e = threadIdx.x; e < L * g.nz; e += blockDim.x) s0[e] = make_float2(src[e], 0.0f);
+    const int ld = line_stride(g.nz);
+    for (int e = threadIdx.x; e < L * g.nz; e += blockDim.x) {
+      const int l = e / g.nz, k = e - l * g.nz;
+      s0[l * ld + k] = make_float2(src[e], 0.0f);
+    }
     __syncthreads();
     const float2 *out = dft_lines(s0, s1, g.az, L, false);
     float2 *dst = g.C + (int64_t)c * g.n + (int64_t)l0 * g.nz;
-    for (int e = threadIdx.x; e < L * g.nz; e += blockDim.x) dst[e] = out[e];
+    for (int e = threadIdx.x; e < L * g.nz; e += blockDim.x) {
+      const int l = e / g.nz, k = e - l * g.nz;
+      dst[e] = out[l * ld + k];
+    }
     __syncthreads();
   }
 }
@@ -71,15 +78,16 @@ __device__ void pass_y(const FftGrid &g, bool inverse, float2 *s0, float2 *s1) {
     const int i = rem / kb, k0 = (rem - i * kb) * g.kty;
     const int kv = min(g.kty, g.nz - k0);
     float2 *base = g.C + (int64_t)c * g.n + (int64_t)i * g.ny * g.nz + k0;
+    const int ld = line_stride(g.ny);
     for (int e = threadIdx.x; e < kv * g.ny; e += blockDim.x) {
       const int j = e / kv, kk = e - j * kv;
-      s0[kk * g.ny + j] = base[(int64_t)j * g.nz + kk];
+      s0[kk * ld + j] = base[(int64_t)j * g.nz + kk];
     }
     __syncthreads();
     const float2 *out = dft_lines(s0, s1, g.ay, kv, inverse);
     for (int e = threadIdx.x; e < kv * g.ny; e += blockDim.x) {
       const int j = e / kv, kk = e - j * kv;
-      base[(int64_t)j * g.nz + kk] = out[kk * g.ny + j];
+      base[(int64_t)j * g.nz + kk] = out[kk * ld + j];
     }
     __syncthreads();
   }
@@ -95,10 +103,11 @@ __device__ void pass_x_solve(const FftGrid &g, float2 *s0, float2 *s1) {
     const int j = tile / kb, k0 = (tile - j * kb) * g.ktx;
     const int kv = min(g.ktx, g.nz - k0);
     const int lines = nc * kv;
+    const int ld = line_stride(g.nx);
     for (int e = threadIdx.x; e < lines * g.nx; e += blockDim.x) {
       const int i = e / lines, lr = e - i * lines;  // lr = c * kv + kk
       const int c = lr / kv, kk = lr - c * kv;
-      s0[lr * g.nx + i] = g.C[(int64_t)c * g.n + ((int64_t)i * g.ny + j) * g.nz + k0 + kk];
+      s0[lr * ld + i] = g.C[(int64_t)c * g.n + ((int64_t)i * g.ny + j) * g.nz + k0 + kk];
     }
     __syncthreads();
     float2 *spec = dft_lines(s0, s1, g.ax, lines, false);
@@ -107,16 +116,16 @@ __device__ void pass_x_solve(const FftGrid &g, float2 *s0, float2 *s1) {
       const int64_t kidx = ((int64_t)i * g.ny + j) * g.nz + k0 + kk;
       if (nc == 1) {
         const float w = __ldg(g.sym + kidx);
-        float2 &v = spec[kk * g.nx + i];
+        float2 &v = spec[kk * ld + i];
         v.x *= w;
         v.y *= w;
       } else {
         const float *m = g.sym + 6 * kidx;
         const float mxx = __ldg(m), myy = __ldg(m + 1), mzz = __ldg(m + 2);
         const float mxy = __ldg(m + 3), myz = __ldg(m + 4), mxz = __ldg(m + 5);
-        float2 &a = spec[(0 * kv + kk) * g.nx + i];
-        float2 &b = spec[(1 * kv + kk) * g.nx + i];
-        float2 &d = spec[(2 * kv + kk) * g.nx + i];
+        float2 &a = spec[(0 * kv + kk) * ld + i];
+        float2 &b = spec[(1 * kv + kk) * ld + i];
+        float2 &d = spec[(2 * kv + kk) * ld + i];
         const float2 va = a, vb = b, vd = d;
         a = make_float2(mxx * va.x + mxy * vb.x + mxz * vd.x, mxx * va.y + mxy * vb.y + mxz * vd.y);
         b = make_float2(mxy * va.x + myy * vb.x + myz * vd.x, mxy * va.y + myy * vb.y + myz * vd.y);
@@ -129,7 +138,7 @@ __device__ void pass_x_solve(const FftGrid &g, float2 *s0, float2 *s1) {
     for (int e = threadIdx.x; e < lines * g.nx; e += blockDim.x) {
       const int i = e / lines, lr = e - i * lines;
       const int c = lr / kv, kk = lr - c * kv;
-      g.C[(int64_t)c * g.n + ((int64_t)i * g.ny + j) * g.nz + k0 + kk] = out[lr * g.nx + i];
+      g.C[(int64_t)c * g.n + ((int64_t)i * g.ny + j) * g.nz + k0 + kk] = out[lr * ld + i];
     }
     __syncthreads();
   }
@@ -147,12 +156,17 @@ __device__ float pass_z_inv(const FftGrid &g, float *zout, const float *r, float
     const int c = tile / per, l0 = (tile - c * per) * g.lz;
     const int L = min(g.lz, nlines - l0);
     const float2 *src = g.C + (int64_t)c * g.n + (int64_t)l0 * g.nz;
-    for (int e = threadIdx.x; e < L * g.nz; e += blockDim.x) s0[e] = src[e];
+    const int ld = line_stride(g.nz);
+    for (int e = threadIdx.x; e < L * g.nz; e += blockDim.x) {
+      const int l = e / g.nz, k = e - l * g.nz;
+      s0[l * ld + k] = src[e];
+    }
     __syncthreads();
     const float2 *out = dft_lines(s0, s1, g.az, L, true);
     const int64_t off = (int64_t)c * g.n + (int64_t)l0 * g.nz;
     for (int e = threadIdx.x; e < L * g.nz; e += blockDim.x) {
-      const float v = out[e].x * scale;
+      const int l = e / g.nz, k = e - l * g.nz;
+      const float v = out[l * ld + k].x * scale;
       zout[off + e] = v;
       if (r) acc = fmaf(r[off + e], v, acc);
     }
@@ -273,16 +287,17 @@ static FftGrid grid_of(const cpm_fft_precond *P, float2 *C) {
   const PrecondLayout L = precond_layout(P->nx, P->ny, P->nz, P->ncomp);
   g.sym = (const float *)((const char *)P->dev + L.sym);
   g.C = C;
-  g.lz = std::max(1, kFftTile / g.nz);
-  g.kty = std::max(1, std::min(g.nz, kFftTile / g.ny));
-  g.ktx = std::max(1, std::min(g.nz, kFftTile / (g.nc * g.nx)));
+  g.lz = std::max(1, kFftTile / line_stride(g.nz));
+  g.kty = std::max(1, std::min(g.nz, kFftTile / line_stride(g.ny)));
+  g.ktx = std::max(1, std::min(g.nz, kFftTile / (g.nc * line_stride(g.nx))));
   return g;
 }
 
 static bool precond_dims_ok(int nx, int ny, int nz, int nc) {
   int r[kFftMaxPass];
-  return nx >= 3 && ny >= 3 && nz >= 3 && (nc == 1 || nc == 3) && nx * nc <= kFftTile && ny <= kFftTile &&
-         nz <= kFftTile && (int64_t)nx * ny * nz * nc < ((int64_t)1 << 31) && radices(nx, r) >= 0 &&
+  return nx >= 3 && ny >= 3 && nz >= 3 && (nc == 1 || nc == 3) && line_stride(nx) * nc <= kFftTile &&
+         line_stride(ny) <= kFftTile && line_stride(nz) <= kFftTile &&
+         (int64_t)nx * ny * nz * nc < ((int64_t)1 << 31) && radices(nx, r) >= 0 &&
          radices(ny, r) >= 0 && radices(nz, r) >= 0;
 }
 
