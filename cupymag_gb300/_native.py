@@ -16,7 +16,9 @@ _lib = None
 
 CPM_OK, CPM_NOT_CONVERGED, CPM_BARRIER_TIMEOUT, CPM_NONFINITE, CPM_BAD_ARG, CPM_CUDA_ERROR = range(6)
 # iteration forms of the FP32 stencil CG (cpm_cg_opts.form)
-CG_FORM_DEFAULT, CG_FORM_THREE_BARRIER, CG_FORM_TWO_BARRIER = 0, 1, 2
+CG_FORM_DEFAULT, CG_FORM_THREE_BARRIER, CG_FORM_TWO_BARRIER, CG_FORM_FFT_PCG = 0, 1, 2, 3
+# spectrum layouts of the FFT preconditioner (cpm_fft_precond.layout)
+FFT_LAYOUT_AUTO, FFT_LAYOUT_SLAB, FFT_LAYOUT_PASSES = 0, 1, 2
 STATUS_NAMES = {0: "ok", 1: "not converged", 2: "grid barrier timeout", 3: "non-finite value", 4: "bad argument",
                 5: "CUDA error"}
 
@@ -72,7 +74,7 @@ class FelStencilC(C.Structure):
 
 class FftPrecondC(C.Structure):
     _fields_ = [("nx", i32), ("ny", i32), ("nz", i32), ("ncomp", i32), ("dev", vp), ("bytes", i64),
-                ("npass", i32 * 3), ("radix", (i32 * 16) * 3)]
+                ("npass", i32 * 3), ("radix", (i32 * 16) * 3), ("layout", i32), ("anchor", i32)]
 
 
 CG_INFO_BYTES = C.sizeof(CGInfo)

@@ -3,7 +3,7 @@
     python -m cupymag_gb300.cgbench [--edge 128] [--op A_el|A_demag|A1|A2] [--nrhs 1|3]
                                     [--precision IR|DP] [--operators stencil|csr]
                                     [--solves 3] [--maxiter 20000] [--batch 1] [--batched]
-                                    [--form 0|1|2] [--precond fft]
+                                    [--form 0|1|2|3] [--precond fft]
 
 Builds only the requested operator (the magnetoelastic 128^3 material), a
 seeded right-hand side with the reference's pins (b[0] = 0 for A_demag,
@@ -48,8 +48,11 @@ def main(argv=None):
                     help="solve through the block-diagonal (serving) kernel even for --batch 1")
     ap.add_argument("--inner-tol", type=float, default=0.1,
                     help="reliable-update factor of the FP32 solver (residual drop between FP64 updates)")
-    ap.add_argument("--form", type=int, default=0, choices=[0, 1, 2],
-                    help="FP32 stencil solver: 0 default (three barriers), 1 three-barrier, 2 two-barrier")
+    ap.add_argument("--form", type=int, default=0, choices=[0, 1, 2, 3],
+                    help="FP32 stencil solver: 0 default (three barriers), 1 three-barrier, 2 two-barrier; "
+                         "FFT solves: 0 direct refinement (anchored operators), 3 preconditioned CG")
+    ap.add_argument("--fft-layout", default="auto", choices=["auto", "slab", "passes"],
+                    help="spectrum layout of the FFT preconditioner")
     ap.add_argument("--precond", default=None, choices=["fft"],
                     help="FP32 stencil solve preconditioned by the circulant inverse (FFT) inside FP64 refinement")
     args = ap.parse_args(argv)
@@ -79,6 +82,7 @@ def main(argv=None):
     bd = torch.as_tensor(b, device="cuda").contiguous()
     stream = torch.cuda.current_stream()
     times, infos = [], []
+    inner_tol = args.inner_tol
     if args.batch > 1 or args.batched:
         if csr:
             raise SystemExit("--batch needs stencil operators")
@@ -93,15 +97,20 @@ def main(argv=None):
         launch = plan.launch
         info_of = lambda: systems[0].info  # noqa: E731
     else:
+        # the FFT-preconditioned inner solve drops its residual by 1e-4 (a circulant inverse leaves few
+        # directions to resolve); plain FP32 CG restarts after the --inner-tol drop
+        inner_tol = 1e-4 if args.precond else args.inner_tol
         solver = CGSolver()
         solver.inner_tol = args.inner_tol
+        solver.fft_layout = {"auto": N.FFT_LAYOUT_AUTO, "slab": N.FFT_LAYOUT_SLAB,
+                             "passes": N.FFT_LAYOUT_PASSES}[args.fft_layout]
         x = torch.zeros_like(bd)
         info = new_info(1)
 
         def launch():
             solver.launch(op, bd, x, info[0], tol=p.tol, maxiter=args.maxiter, precision=args.precision,
                           form=args.form, precond=args.precond,
-                          inner_tol=1e-4 if args.precond else args.inner_tol)
+                          inner_tol=inner_tol)
         info_of = lambda: info[0]  # noqa: E731
     for _ in range(args.solves):
         e0 = torch.cuda.Event(enable_timing=True)
@@ -118,7 +127,8 @@ def main(argv=None):
     ms = float(np.median(times))
     nb = _bytes(op, nrhs, its, d["outer"], args.precision == "IR", csr) * args.batch
     print(json.dumps({"op": args.op, "edge": args.edge, "n": n, "nrhs": nrhs, "precision": args.precision,
-                      "inner_tol": args.inner_tol, "form": args.form, "precond": args.precond,
+                      "inner_tol": inner_tol, "form": args.form, "precond": args.precond,
+                      "fft_layout": args.fft_layout if args.precond else None,
                       "operators": args.operators, "batch": args.batch,
                       "kernel": "blockdiag" if args.batch > 1 or args.batched else "single",
                       "status": N.STATUS_NAMES[d["status"]],

@@ -17,11 +17,19 @@ constexpr size_t kPartHalf = (size_t)9 * kMaxGrid;  // doubles per half of the p
 // FP64 instructions: they skip values not in use, and one warp adds a
 // block's values (13 FP64 warp instructions per value, where shuffles in
 // every warp and a per-thread sum of the warp sums took 48).
-template <int NV, int NW>
+// The staging array of block_sum: one per block size, shared by every instantiation.
+template <int NT>
+__device__ __forceinline__ double *block_sum_scratch() {
+  __shared__ double s_all[NT];
+  return s_all;
+}
+
+// NT: the block's thread count.
+template <int NV, int NW, int NT = kCGThreads>
 __device__ __forceinline__ void block_sum(double (&v)[NV], double (*s)[NW], int nv = NV) {
-  // per value: every thread stores its value, one warp adds 8 per lane (threads
-  // 8l..8l+7, in order) and then the 32 lane sums with a fixed shuffle tree
-  __shared__ double s_all[kCGThreads];
+  // per value: every thread stores its value, one warp adds NT/32 per lane (threads
+  // l NT/32 .. (l+1) NT/32 - 1, in order) and then the 32 lane sums with a fixed shuffle tree
+  double *s_all = block_sum_scratch<NT>();
   const int lane = threadIdx.x & 31;
 #pragma unroll
   for (int j = 0; j < NV; ++j) {
@@ -31,7 +39,7 @@ __device__ __forceinline__ void block_sum(double (&v)[NV], double (*s)[NW], int 
     if (threadIdx.x < kWarp) {
       double t = 0.0;
 #pragma unroll
-      for (int k = 0; k < kCGThreads / kWarp; ++k) t += s_all[lane * (kCGThreads / kWarp) + k];
+      for (int k = 0; k < NT / kWarp; ++k) t += s_all[lane * (NT / kWarp) + k];
       t = warp_sum(t);
       if (lane == 0) s[j][0] = t;
     }
@@ -50,10 +58,10 @@ __device__ __forceinline__ void block_sum(double (&v)[NV], double (*s)[NW], int 
 // CTA may start writing the next reduction's partials while slower CTAs still
 // read this one's, and the barrier of the next reduction orders the reuse of
 // a half.
-template <int NV, int NW>
+template <int NV, int NW, int NT = kCGThreads>
 __device__ __forceinline__ bool grid_sum(double (&v)[NV], double *part, int &parity, GridBarrier *bar,
                                          unsigned long long tns, double (*s)[NW], int nv = NV) {
-  block_sum<NV>(v, s, nv);
+  block_sum<NV, NW, NT>(v, s, nv);
   const int G = gridDim.x;
   part += (size_t)parity * kPartHalf;
   parity ^= 1;
@@ -69,7 +77,7 @@ __device__ __forceinline__ bool grid_sum(double (&v)[NV], double *part, int &par
     for (int j = 0; j < NV; ++j)
       if (j < nv) acc[j] += __ldcg(&part[(size_t)g * NV + j]);
   }
-  block_sum<NV>(acc, s, nv);
+  block_sum<NV, NW, NT>(acc, s, nv);
 #pragma unroll
   for (int j = 0; j < NV; ++j) v[j] = j < nv ? acc[j] : 0.0;
   return true;

@@ -17,11 +17,24 @@
 // ||t|| <= tol ||b||, else runs FP32 preconditioned CG on A e = t from e = 0 until
 // its residual has dropped by inner_tol (default 1e-4) and adds e to x.  The
 // whole solve is one persistent cooperative launch; every grid barrier is
-// bounded (GridBarrier).  Per inner iteration:
-//   z = M r: DFT along z, y, then along x with the symbol solve and the
-//            inverse DFT along x in the same shared-memory tile, inverse along
-//            y and z (five passes over the complex field, with r.z);
-//   p = z + beta p; q = A32 p with p.q; d += alpha p, r -= alpha q with r.r.
+// bounded (GridBarrier).  Per inner iteration: z = M r with r.z;
+// p = z + beta p; q = A32 p with p.q; d += alpha p, r -= alpha q with r.r.
+//
+// z = M r has two layouts of the spectrum:
+//  * slab (the default where it fits in shared memory): r is real, so along z
+//    only the nz/2 + 1 non-negative frequencies are kept (the others are the
+//    conjugates).  Pass 1 takes one x-plane of one component per CTA step:
+//    the real z lines two at a time as one complex DFT (lines 2p + i 2p+1),
+//    split into the two half spectra, then the DFT along y of every kz column,
+//    all in shared memory, one read of r and one write of the half spectrum.
+//    Pass 2 takes tiles of (kz, y) columns of all components: DFT along x,
+//    the 3x3 (1x1) symbol solve, inverse DFT along x.  Pass 3 undoes pass 1
+//    (inverse y, the two half spectra joined into one complex line, inverse
+//    z) and writes z with the partial of r.z.  Three passes, two grid
+//    barriers plus the r.z sum, half the complex traffic.
+//  * five passes over the full complex field (grids whose x-plane does not fit
+//    in shared memory): DFT along z, y, x with the symbol solve and the
+//    inverse along x in one tile, inverse along y, inverse along z.
 #include <algorithm>
 #include <cmath>
 #include <vector>
@@ -31,37 +44,219 @@
 
 namespace cpm {
 
-constexpr int kFftThreads = 256;
-constexpr int kFftTile = 4096;  // complex values per shared-memory tile buffer (two buffers per CTA)
+constexpr int kFftTile = 4096;  // five-pass layout: complex values per tile buffer (two buffers per CTA)
+// slab layout: the largest dynamic shared memory of a CTA (two regions and the twiddle tables),
+// under the 227 KB of an SM with the kernel's static reductions beside it
+constexpr size_t kSlabSmemMax = 220 * 1024;
+
+// Threads per CTA and resident CTAs per SM of the solve kernel, per layout.
+template <int LAYOUT>
+struct FftShape;
+template <>
+struct FftShape<CPM_FFT_LAYOUT_SLAB> {
+  static constexpr int threads = 512, blocks = 1;
+};
+template <>
+struct FftShape<CPM_FFT_LAYOUT_PASSES> {
+  static constexpr int threads = 256, blocks = 2;
+};
 
 struct FftGrid {
   int nx, ny, nz, n, nc;
+  int layout;
   FftAxis ax, ay, az;
-  const float *sym;  // inverse symbol per wave vector: nc == 1: 1 float; nc == 3: xx yy zz xy yz xz
-  float2 *C;         // complex field, nc * n
-  int lz, kty, ktx;  // lines per tile of the z, y and x passes
+  // inverse symbol per wave vector: nc == 1: 1 float; nc == 3: xx yy zz xy yz xz.
+  // five passes: wave vector (i, j, k) at ((i ny + j) nz + k), the 6 values together;
+  // slab: (i, kz, j) at (i h + kz) ny + j, one plane of nx h ny values per entry.
+  const float *sym;
+  float2 *C;         // complex field: nc * n (five passes) or nc * nx * h * ny (slab, [c][i][kz][j])
+  int lz, kty, ktx;  // five passes: lines per tile of the z, y and x passes
+  int h, pc, reg;    // slab: nz / 2 + 1, (kz, y) columns per x tile, complex values per shared region
 };
 
-// ---------------------------------------------------------------- the five passes
+// Complex values of one shared-memory region.
+__host__ __device__ __forceinline__ int fft_region(const FftGrid &g) {
+  return g.layout == CPM_FFT_LAYOUT_SLAB ? g.reg : kFftTile;
+}
+
+// Dynamic shared memory of a pass or solve CTA: two regions and the twiddle tables of the three axes.
+static size_t fft_smem_bytes(const FftGrid &g) {
+  return sizeof(float2) * (2 * (size_t)fft_region(g) + g.nx + g.ny + g.nz);
+}
+
+// Copy the three twiddle tables into shared memory (behind the two regions); ends with a block barrier.
+__device__ __forceinline__ void load_twiddles(const FftGrid &g, float2 *fsm, const float2 *&twx,
+                                              const float2 *&twy, const float2 *&twz) {
+  float2 *t = fsm + 2 * fft_region(g);
+  for (int e = threadIdx.x; e < g.nx; e += blockDim.x) t[e] = g.ax.tw[e];
+  for (int e = threadIdx.x; e < g.ny; e += blockDim.x) t[g.nx + e] = g.ay.tw[e];
+  for (int e = threadIdx.x; e < g.nz; e += blockDim.x) t[g.nx + g.ny + e] = g.az.tw[e];
+  twx = t;
+  twy = t + g.nx;
+  twz = t + g.nx + g.ny;
+  __syncthreads();
+}
+
+// Symbol solve of one wave vector: the nc values v[c] (shared memory, stride cs) times the
+// inverse symbol at index kidx (plane stride ps between the 6 entries; 1 for the interleaved form
+// with kidx already scaled by 6).
+__device__ __forceinline__ void symbol_solve(const float *sym, int64_t kidx, int64_t ps, int nc, float2 *v,
+                                             int cs) {
+  if (nc == 1) {
+    const float w = __ldg(sym + kidx);
+    v->x *= w;
+    v->y *= w;
+    return;
+  }
+  const float mxx = __ldg(sym + kidx), myy = __ldg(sym + kidx + ps), mzz = __ldg(sym + kidx + 2 * ps);
+  const float mxy = __ldg(sym + kidx + 3 * ps), myz = __ldg(sym + kidx + 4 * ps), mxz = __ldg(sym + kidx + 5 * ps);
+  float2 &a = v[0];
+  float2 &b = v[cs];
+  float2 &d = v[2 * cs];
+  const float2 va = a, vb = b, vd = d;
+  a = make_float2(mxx * va.x + mxy * vb.x + mxz * vd.x, mxx * va.y + mxy * vb.y + mxz * vd.y);
+  b = make_float2(mxy * va.x + myy * vb.x + myz * vd.x, mxy * va.y + myy * vb.y + myz * vd.y);
+  d = make_float2(mxz * va.x + myz * vb.x + mzz * vd.x, mxz * va.y + myz * vb.y + mzz * vd.y);
+}
+
+// ---------------------------------------------------------------- slab layout
+// Pass 1, per (component c, x-plane i): real z lines -> half spectra along z -> DFT along y -> C.
+__device__ void slab_fwd(const FftGrid &g, const float *__restrict__ r, float2 *R0, float2 *R1,
+                         const float2 *twy, const float2 *twz) {
+  const int ny = g.ny, nz = g.nz, h = g.h, P = (ny + 1) >> 1;
+  const int ldz = line_stride(nz), ldy = line_stride(ny), Hc = h * ny;
+  const float inv_nz = __frcp_rn((float)nz), inv_h = __frcp_rn((float)h), inv_ny = __frcp_rn((float)ny);
+  const float inv_nx = __frcp_rn((float)g.nx);
+  for (int s = blockIdx.x; s < g.nc * g.nx; s += gridDim.x) {
+    const int c = qdiv(s, inv_nx), i = s - c * g.nx;
+    const float *src = r + (int64_t)c * g.n + (int64_t)i * ny * nz;
+    // lines 2p and 2p+1 (zero past the last line) as the real and imaginary parts of line p
+    for (Walk2 w(nz, inv_nz); w.row < P; w.next()) {
+      const int p = w.row, k = w.col;
+      const int j = 2 * p;
+      const float re = src[j * nz + k];
+      const float im = j + 1 < ny ? src[(j + 1) * nz + k] : 0.0f;
+      R0[p * ldz + k] = make_float2(re, im);
+    }
+    __syncthreads();
+    float2 *Z = dft_lines<false>(R0, R1, g.az, twz, P);
+    float2 *B = Z == R0 ? R1 : R0;
+    // Z = A + i B' with A, B' the spectra of the two real lines: A[k] = (Z[k] + conj Z[-k]) / 2,
+    // B'[k] = (Z[k] - conj Z[-k]) / 2i; kept for k < h, stored as columns B[kz][j]
+    for (Walk2 w(h, inv_h); w.row < P; w.next()) {
+      const int p = w.row, k = w.col;
+      const float2 a = Z[p * ldz + k];
+      const float2 m = Z[p * ldz + (k == 0 ? 0 : nz - k)];
+      B[k * ldy + 2 * p] = make_float2(0.5f * (a.x + m.x), 0.5f * (a.y - m.y));
+      if (2 * p + 1 < ny) B[k * ldy + 2 * p + 1] = make_float2(0.5f * (a.y + m.y), 0.5f * (m.x - a.x));
+    }
+    __syncthreads();
+    const float2 *Y = dft_lines<false>(B, Z, g.ay, twy, h);
+    float2 *dst = g.C + (int64_t)s * Hc;
+    for (Walk2 w(ny, inv_ny); w.row < h; w.next()) dst[w.row * ny + w.col] = Y[w.row * ldy + w.col];
+    __syncthreads();
+  }
+}
+
+// Pass 2, per tile of pc consecutive (kz, y) columns: DFT along x of every component, the symbol
+// solve per wave vector, inverse DFT along x, in place in C.
+__device__ void slab_x_solve(const FftGrid &g, float2 *R0, float2 *R1, const float2 *twx) {
+  const int nx = g.nx, nc = g.nc, Hc = g.h * g.ny, pc = g.pc;
+  const int ldx = line_stride(nx);
+  const int ntiles = (Hc + pc - 1) / pc;
+  const int64_t plane = (int64_t)nx * Hc;
+  const float inv_nx = __frcp_rn((float)nx);
+  for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
+    const int c0 = t * pc, pv = min(pc, Hc - c0);
+    const float inv_pv = __frcp_rn((float)pv);
+    const int lines = nc * pv;  // line c pv + l: component c, column c0 + l
+    for (Walk2 w(pv, inv_pv); w.row < nc * nx; w.next()) {
+      const int ci = w.row, l = w.col;  // ci = c nx + i
+      const int c = qdiv(ci, inv_nx), i = ci - c * nx;
+      R0[(c * pv + l) * ldx + i] = g.C[(int64_t)ci * Hc + c0 + l];
+    }
+    __syncthreads();
+    float2 *spec = dft_lines<false>(R0, R1, g.ax, twx, lines);
+    for (Walk2 w(pv, inv_pv); w.row < nx; w.next())
+      symbol_solve(g.sym, (int64_t)w.row * Hc + c0 + w.col, plane, nc, spec + w.col * ldx + w.row, pv * ldx);
+    __syncthreads();
+    float2 *other = spec == R0 ? R1 : R0;
+    const float2 *out = dft_lines<true>(spec, other, g.ax, twx, lines);
+    for (Walk2 w(pv, inv_pv); w.row < nc * nx; w.next()) {
+      const int ci = w.row, l = w.col;
+      const int c = qdiv(ci, inv_nx), i = ci - c * nx;
+      g.C[(int64_t)ci * Hc + c0 + l] = out[(c * pv + l) * ldx + i];
+    }
+    __syncthreads();
+  }
+}
+
+// Pass 3, per (c, i): inverse DFT along y, the half spectra of lines 2p and 2p+1 joined as
+// Z = A + i B' (A[-k] = conj A[k]), inverse DFT along z, zout = (Re, Im) / n.  Returns this
+// thread's FP32 partial of r . zout (r may be NULL: no partial).
+__device__ float slab_inv(const FftGrid &g, float *__restrict__ zout, const float *__restrict__ r, float2 *R0,
+                          float2 *R1, const float2 *twy, const float2 *twz) {
+  const int ny = g.ny, nz = g.nz, h = g.h, P = (ny + 1) >> 1;
+  const int ldz = line_stride(nz), ldy = line_stride(ny), Hc = h * ny;
+  const float inv_nz = __frcp_rn((float)nz), inv_ny = __frcp_rn((float)ny), inv_nx = __frcp_rn((float)g.nx);
+  const float scale = 1.0f / (float)g.n;
+  float acc = 0.0f;
+  for (int s = blockIdx.x; s < g.nc * g.nx; s += gridDim.x) {
+    const int c = qdiv(s, inv_nx), i = s - c * g.nx;
+    const float2 *src = g.C + (int64_t)s * Hc;
+    for (Walk2 w(ny, inv_ny); w.row < h; w.next()) R0[w.row * ldy + w.col] = src[w.row * ny + w.col];
+    __syncthreads();
+    float2 *Y = dft_lines<true>(R0, R1, g.ay, twy, h);
+    float2 *Z = Y == R0 ? R1 : R0;
+    for (Walk2 w(nz, inv_nz); w.row < P; w.next()) {
+      const int p = w.row, k = w.col;
+      const bool lo = k < h;
+      const int kk = lo ? k : nz - k;
+      const int j = 2 * p;
+      float2 a = Y[kk * ldy + j];
+      float2 b = j + 1 < ny ? Y[kk * ldy + j + 1] : make_float2(0.0f, 0.0f);
+      if (!lo) {
+        a.y = -a.y;
+        b.y = -b.y;
+      }
+      Z[p * ldz + k] = make_float2(a.x - b.y, a.y + b.x);
+    }
+    __syncthreads();
+    const float2 *out = dft_lines<true>(Z, Y, g.az, twz, P);
+    const int64_t off = (int64_t)c * g.n + (int64_t)i * ny * nz;
+    for (Walk2 w(nz, inv_nz); w.row < ny; w.next()) {
+      const int j = w.row, e = j * nz + w.col;
+      const float2 u = out[(j >> 1) * ldz + w.col];
+      const float v = ((j & 1) ? u.y : u.x) * scale;
+      zout[off + e] = v;
+      if (r) acc = fmaf(r[off + e], v, acc);
+    }
+    __syncthreads();
+  }
+  return acc;
+}
+
+// ---------------------------------------------------------------- five-pass layout
 // z lines of the real input (per component): forward DFT along z into C.
-__device__ void pass_z_fwd(const FftGrid &g, const float *r, float2 *s0, float2 *s1) {
+__device__ void pass_z_fwd(const FftGrid &g, const float *r, float2 *s0, float2 *s1, const float2 *twz) {
   const int nlines = g.nx * g.ny;
   const int per = (nlines + g.lz - 1) / g.lz;
   const int ntiles = g.nc * per;
+  const int ld = line_stride(g.nz);
+  const float inv_nz = __frcp_rn((float)g.nz);
   for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
     const int c = tile / per, l0 = (tile - c * per) * g.lz;
     const int L = min(g.lz, nlines - l0);
     const float *src = r + (int64_t)c * g.n + (int64_t)l0 * g.nz;
-    const int ld = line_stride(g.nz);
     for (int e = threadIdx.x; e < L * g.nz; e += blockDim.x) {
-      const int l = e / g.nz, k = e - l * g.nz;
+      const int l = qdiv(e, inv_nz), k = e - l * g.nz;
       s0[l * ld + k] = make_float2(src[e], 0.0f);
     }
     __syncthreads();
-    const float2 *out = dft_lines(s0, s1, g.az, L, false);
+    const float2 *out = dft_lines<false>(s0, s1, g.az, twz, L);
     float2 *dst = g.C + (int64_t)c * g.n + (int64_t)l0 * g.nz;
     for (int e = threadIdx.x; e < L * g.nz; e += blockDim.x) {
-      const int l = e / g.nz, k = e - l * g.nz;
+      const int l = qdiv(e, inv_nz), k = e - l * g.nz;
       dst[e] = out[l * ld + k];
     }
     __syncthreads();
@@ -69,24 +264,25 @@ __device__ void pass_z_fwd(const FftGrid &g, const float *r, float2 *s0, float2 
 }
 
 // y lines (tiles of kty consecutive z at fixed x), forward or inverse, in place in C.
-__device__ void pass_y(const FftGrid &g, bool inverse, float2 *s0, float2 *s1) {
+__device__ void pass_y(const FftGrid &g, bool inverse, float2 *s0, float2 *s1, const float2 *twy) {
   const int kb = (g.nz + g.kty - 1) / g.kty;
   const int ntiles = g.nc * g.nx * kb;
+  const int ld = line_stride(g.ny);
   for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
     const int c = tile / (g.nx * kb);
     const int rem = tile - c * g.nx * kb;
     const int i = rem / kb, k0 = (rem - i * kb) * g.kty;
     const int kv = min(g.kty, g.nz - k0);
     float2 *base = g.C + (int64_t)c * g.n + (int64_t)i * g.ny * g.nz + k0;
-    const int ld = line_stride(g.ny);
+    const float inv_kv = __frcp_rn((float)kv);
     for (int e = threadIdx.x; e < kv * g.ny; e += blockDim.x) {
-      const int j = e / kv, kk = e - j * kv;
+      const int j = qdiv(e, inv_kv), kk = e - j * kv;
       s0[kk * ld + j] = base[(int64_t)j * g.nz + kk];
     }
     __syncthreads();
-    const float2 *out = dft_lines(s0, s1, g.ay, kv, inverse);
+    const float2 *out = inverse ? dft_lines<true>(s0, s1, g.ay, twy, kv) : dft_lines<false>(s0, s1, g.ay, twy, kv);
     for (int e = threadIdx.x; e < kv * g.ny; e += blockDim.x) {
-      const int j = e / kv, kk = e - j * kv;
+      const int j = qdiv(e, inv_kv), kk = e - j * kv;
       base[(int64_t)j * g.nz + kk] = out[kk * ld + j];
     }
     __syncthreads();
@@ -95,49 +291,34 @@ __device__ void pass_y(const FftGrid &g, bool inverse, float2 *s0, float2 *s1) {
 
 // x lines of every component (tiles of ktx consecutive z at fixed y): forward DFT,
 // u^(k) = S^-1(k) r^(k), inverse DFT, all in the tile.
-__device__ void pass_x_solve(const FftGrid &g, float2 *s0, float2 *s1) {
+__device__ void pass_x_solve(const FftGrid &g, float2 *s0, float2 *s1, const float2 *twx) {
   const int kb = (g.nz + g.ktx - 1) / g.ktx;
   const int ntiles = g.ny * kb;
   const int nc = g.nc;
+  const int ld = line_stride(g.nx);
   for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
     const int j = tile / kb, k0 = (tile - j * kb) * g.ktx;
     const int kv = min(g.ktx, g.nz - k0);
     const int lines = nc * kv;
-    const int ld = line_stride(g.nx);
+    const float inv_lines = __frcp_rn((float)lines), inv_kv = __frcp_rn((float)kv);
     for (int e = threadIdx.x; e < lines * g.nx; e += blockDim.x) {
-      const int i = e / lines, lr = e - i * lines;  // lr = c * kv + kk
-      const int c = lr / kv, kk = lr - c * kv;
+      const int i = qdiv(e, inv_lines), lr = e - i * lines;  // lr = c * kv + kk
+      const int c = qdiv(lr, inv_kv), kk = lr - c * kv;
       s0[lr * ld + i] = g.C[(int64_t)c * g.n + ((int64_t)i * g.ny + j) * g.nz + k0 + kk];
     }
     __syncthreads();
-    float2 *spec = dft_lines(s0, s1, g.ax, lines, false);
+    float2 *spec = dft_lines<false>(s0, s1, g.ax, twx, lines);
     for (int e = threadIdx.x; e < kv * g.nx; e += blockDim.x) {
-      const int i = e / kv, kk = e - i * kv;
+      const int i = qdiv(e, inv_kv), kk = e - i * kv;
       const int64_t kidx = ((int64_t)i * g.ny + j) * g.nz + k0 + kk;
-      if (nc == 1) {
-        const float w = __ldg(g.sym + kidx);
-        float2 &v = spec[kk * ld + i];
-        v.x *= w;
-        v.y *= w;
-      } else {
-        const float *m = g.sym + 6 * kidx;
-        const float mxx = __ldg(m), myy = __ldg(m + 1), mzz = __ldg(m + 2);
-        const float mxy = __ldg(m + 3), myz = __ldg(m + 4), mxz = __ldg(m + 5);
-        float2 &a = spec[(0 * kv + kk) * ld + i];
-        float2 &b = spec[(1 * kv + kk) * ld + i];
-        float2 &d = spec[(2 * kv + kk) * ld + i];
-        const float2 va = a, vb = b, vd = d;
-        a = make_float2(mxx * va.x + mxy * vb.x + mxz * vd.x, mxx * va.y + mxy * vb.y + mxz * vd.y);
-        b = make_float2(mxy * va.x + myy * vb.x + myz * vd.x, mxy * va.y + myy * vb.y + myz * vd.y);
-        d = make_float2(mxz * va.x + myz * vb.x + mzz * vd.x, mxz * va.y + myz * vb.y + mzz * vd.y);
-      }
+      symbol_solve(g.sym, nc == 1 ? kidx : 6 * kidx, 1, nc, spec + kk * ld + i, kv * ld);
     }
     __syncthreads();
     float2 *other = spec == s0 ? s1 : s0;
-    const float2 *out = dft_lines(spec, other, g.ax, lines, true);
+    const float2 *out = dft_lines<true>(spec, other, g.ax, twx, lines);
     for (int e = threadIdx.x; e < lines * g.nx; e += blockDim.x) {
-      const int i = e / lines, lr = e - i * lines;
-      const int c = lr / kv, kk = lr - c * kv;
+      const int i = qdiv(e, inv_lines), lr = e - i * lines;
+      const int c = qdiv(lr, inv_kv), kk = lr - c * kv;
       g.C[(int64_t)c * g.n + ((int64_t)i * g.ny + j) * g.nz + k0 + kk] = out[lr * ld + i];
     }
     __syncthreads();
@@ -146,26 +327,28 @@ __device__ void pass_x_solve(const FftGrid &g, float2 *s0, float2 *s1) {
 
 // Inverse DFT along z, z_out = Re / n; returns this thread's FP32 partial of r . z_out
 // (r may be NULL: no partial).
-__device__ float pass_z_inv(const FftGrid &g, float *zout, const float *r, float2 *s0, float2 *s1) {
+__device__ float pass_z_inv(const FftGrid &g, float *zout, const float *r, float2 *s0, float2 *s1,
+                            const float2 *twz) {
   const int nlines = g.nx * g.ny;
   const int per = (nlines + g.lz - 1) / g.lz;
   const int ntiles = g.nc * per;
   const float scale = 1.0f / (float)g.n;
+  const int ld = line_stride(g.nz);
+  const float inv_nz = __frcp_rn((float)g.nz);
   float acc = 0.0f;
   for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
     const int c = tile / per, l0 = (tile - c * per) * g.lz;
     const int L = min(g.lz, nlines - l0);
     const float2 *src = g.C + (int64_t)c * g.n + (int64_t)l0 * g.nz;
-    const int ld = line_stride(g.nz);
     for (int e = threadIdx.x; e < L * g.nz; e += blockDim.x) {
-      const int l = e / g.nz, k = e - l * g.nz;
+      const int l = qdiv(e, inv_nz), k = e - l * g.nz;
       s0[l * ld + k] = src[e];
     }
     __syncthreads();
-    const float2 *out = dft_lines(s0, s1, g.az, L, true);
+    const float2 *out = dft_lines<true>(s0, s1, g.az, twz, L);
     const int64_t off = (int64_t)c * g.n + (int64_t)l0 * g.nz;
     for (int e = threadIdx.x; e < L * g.nz; e += blockDim.x) {
-      const int l = e / g.nz, k = e - l * g.nz;
+      const int l = qdiv(e, inv_nz), k = e - l * g.nz;
       const float v = out[l * ld + k].x * scale;
       zout[off + e] = v;
       if (r) acc = fmaf(r[off + e], v, acc);
@@ -175,9 +358,36 @@ __device__ float pass_z_inv(const FftGrid &g, float *zout, const float *r, float
   return acc;
 }
 
+// z = M r of either layout with the grid barriers between its passes; returns this thread's
+// partial of r . z (the caller's grid sum is the last barrier).  false: a barrier timed out.
+template <int LAYOUT>
+__device__ __forceinline__ bool precondition(const FftGrid &g, const float *r, float *z, float2 *s0, float2 *s1,
+                                             const float2 *twx, const float2 *twy, const float2 *twz,
+                                             GridBarrier *bar, unsigned long long tns, float &rz) {
+  if (LAYOUT == CPM_FFT_LAYOUT_SLAB) {
+    slab_fwd(g, r, s0, s1, twy, twz);
+    if (!grid_sync(bar, gridDim.x, tns)) return false;
+    slab_x_solve(g, s0, s1, twx);
+    if (!grid_sync(bar, gridDim.x, tns)) return false;
+    rz = slab_inv(g, z, r, s0, s1, twy, twz);
+  } else {
+    pass_z_fwd(g, r, s0, s1, twz);
+    if (!grid_sync(bar, gridDim.x, tns)) return false;
+    pass_y(g, false, s0, s1, twy);
+    if (!grid_sync(bar, gridDim.x, tns)) return false;
+    pass_x_solve(g, s0, s1, twx);
+    if (!grid_sync(bar, gridDim.x, tns)) return false;
+    pass_y(g, true, s0, s1, twy);
+    if (!grid_sync(bar, gridDim.x, tns)) return false;
+    rz = pass_z_inv(g, z, r, s0, s1, twz);
+  }
+  return true;
+}
+
 // ---------------------------------------------------------------- the inverse symbol (setup)
 struct SymArgs {
   int nx, ny, nz, nc;
+  int slab, h;  // slab layout: wave vectors (i, kz < h, j), one plane per symbol entry
   double c[243];
   double sigma;
   const double *cx, *sx, *cy, *sy, *cz, *sz;  // cos / sin of 2 pi i / n per axis (device tables)
@@ -185,12 +395,21 @@ struct SymArgs {
 };
 
 __global__ void __launch_bounds__(256) fft_symbol_kernel(const __grid_constant__ SymArgs a) {
-  const int64_t n = (int64_t)a.nx * a.ny * a.nz;
+  const int64_t n = a.slab ? (int64_t)a.nx * a.h * a.ny : (int64_t)a.nx * a.ny * a.nz;
   for (int64_t kidx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; kidx < n;
        kidx += (int64_t)gridDim.x * blockDim.x) {
-    const int ix = (int)(kidx / ((int64_t)a.ny * a.nz));
-    const int rem = (int)(kidx - (int64_t)ix * a.ny * a.nz);
-    const int iy = rem / a.nz, iz = rem - iy * a.nz;
+    int ix, iy, iz;
+    if (a.slab) {
+      ix = (int)(kidx / ((int64_t)a.h * a.ny));
+      const int rem = (int)(kidx - (int64_t)ix * a.h * a.ny);
+      iz = rem / a.ny;
+      iy = rem - iz * a.ny;
+    } else {
+      ix = (int)(kidx / ((int64_t)a.ny * a.nz));
+      const int rem = (int)(kidx - (int64_t)ix * a.ny * a.nz);
+      iy = rem / a.nz;
+      iz = rem - iy * a.nz;
+    }
     // e^{i theta_a d} for d = -1, 0, 1 per axis
     double ex[3][2], ey[3][2], ez[3][2];
     ex[0][0] = a.cx[ix]; ex[0][1] = -a.sx[ix]; ex[1][0] = 1.0; ex[1][1] = 0.0; ex[2][0] = a.cx[ix]; ex[2][1] = a.sx[ix];
@@ -222,20 +441,27 @@ __global__ void __launch_bounds__(256) fft_symbol_kernel(const __grid_constant__
       const double cxy = xz * yz - xy * zz, cyz = xy * xz - xx * yz, cxz = xy * yz - xz * yy;
       const double det = xx * cxx + xy * cxy + xz * cxz;
       const double id = 1.0 / det;
-      float *o = a.sym + 6 * kidx;
-      o[0] = (float)(cxx * id);
-      o[1] = (float)(cyy * id);
-      o[2] = (float)(czz * id);
-      o[3] = (float)(cxy * id);
-      o[4] = (float)(cyz * id);
-      o[5] = (float)(cxz * id);
+      const int64_t base = a.slab ? kidx : 6 * kidx, st = a.slab ? n : 1;
+      const double v[6] = {cxx * id, cyy * id, czz * id, cxy * id, cyz * id, cxz * id};
+      for (int m = 0; m < 6; ++m) a.sym[base + m * st] = (float)v[m];
     }
   }
 }
 
+// Counts the nodes whose row/column flags (bits 1, 2, 4) differ from a single pinned node `anchor`
+// (flags 1|4 there, none elsewhere; bit 8 marks rows that take the checked path and is ignored).
+__global__ void __launch_bounds__(256) anchor_check_kernel(const uint8_t *flags, int64_t n, int anchor, int *bad) {
+  int cnt = 0;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const int f = flags[i] & 7;
+    cnt += (i == anchor) ? (f != 5) : (f != 0);
+  }
+  if (cnt) atomicAdd(bad, cnt);
+}
+
 // ---------------------------------------------------------------- plan layout
 struct PrecondLayout {
-  size_t tw[3], trig[3], sym, total;
+  size_t tw[3], trig[3], sym, check, total;
 };
 
 static PrecondLayout precond_layout(int nx, int ny, int nz, int nc) {
@@ -248,20 +474,47 @@ static PrecondLayout precond_layout(int nx, int ny, int nz, int nc) {
     L.trig[a] = off;
     off += align256(sizeof(double) * 2 * dims[a]);
   }
+  // sized for the full spectrum (the slab layout's half spectrum takes less)
   L.sym = off;
   off += align256(sizeof(float) * (size_t)nx * ny * nz * (nc == 3 ? 6 : 1));
+  L.check = off;  // one int: the anchor check of the build
+  off += 256;
   L.total = off;
   return L;
 }
 
-// Radices of n: 4s, a 2, then 3, 5, 7 and larger primes.
+// Radices of n: 8s, a 4 and a 2, then 3, 5, 7 and larger primes.
 static int radices(int n, int *out) {
   int k = 0, m = n;
+  while (m % 8 == 0 && k < kFftMaxPass) { out[k++] = 8; m /= 8; }
   while (m % 4 == 0 && k < kFftMaxPass) { out[k++] = 4; m /= 4; }
   while (m % 2 == 0 && k < kFftMaxPass) { out[k++] = 2; m /= 2; }
   for (int p = 3; m > 1 && k < kFftMaxPass; p += 2)
     while (m % p == 0 && k < kFftMaxPass) { out[k++] = p; m /= p; }
   return m == 1 ? k : -1;
+}
+
+// Complex values per shared region of the slab layout: the paired z lines, the kz columns along
+// y, and at least one x line of every component.
+static int slab_region(int nx, int ny, int nz, int nc) {
+  const int P = (ny + 1) / 2, h = nz / 2 + 1;
+  return std::max({P * line_stride(nz), h * line_stride(ny), nc * line_stride(nx)});
+}
+
+static bool slab_fits(int nx, int ny, int nz, int nc) {
+  return sizeof(float2) * (2 * (size_t)slab_region(nx, ny, nz, nc) + nx + ny + nz) <= kSlabSmemMax;
+}
+
+static int auto_layout(int nx, int ny, int nz, int nc) {
+  return slab_fits(nx, ny, nz, nc) ? CPM_FFT_LAYOUT_SLAB : CPM_FFT_LAYOUT_PASSES;
+}
+
+static bool precond_dims_ok(int nx, int ny, int nz, int nc) {
+  int r[kFftMaxPass];
+  return nx >= 3 && ny >= 3 && nz >= 3 && (nc == 1 || nc == 3) && line_stride(nx) * nc <= kFftTile &&
+         line_stride(ny) <= kFftTile && line_stride(nz) <= kFftTile &&
+         (int64_t)nx * ny * nz * nc < ((int64_t)1 << 31) && radices(nx, r) >= 0 &&
+         radices(ny, r) >= 0 && radices(nz, r) >= 0;
 }
 
 static FftAxis axis_of(const cpm_fft_precond *P, int a) {
@@ -274,31 +527,43 @@ static FftAxis axis_of(const cpm_fft_precond *P, int a) {
   return ax;
 }
 
-static FftGrid grid_of(const cpm_fft_precond *P, float2 *C) {
+// Lines per tile: as many as a tile buffer holds, but no more than spreads the pass over all G CTAs.
+static int tile_lines(int cap, int64_t units, int64_t G) {
+  const int64_t even = (units + G - 1) / G;
+  return (int)std::max<int64_t>(1, std::min<int64_t>(cap, even));
+}
+
+static FftGrid grid_of(const cpm_fft_precond *P, float2 *C, int64_t G) {
   FftGrid g{};
   g.nx = P->nx;
   g.ny = P->ny;
   g.nz = P->nz;
   g.n = P->nx * P->ny * P->nz;
   g.nc = P->ncomp;
+  g.layout = P->layout;
   g.ax = axis_of(P, 0);
   g.ay = axis_of(P, 1);
   g.az = axis_of(P, 2);
   const PrecondLayout L = precond_layout(P->nx, P->ny, P->nz, P->ncomp);
   g.sym = (const float *)((const char *)P->dev + L.sym);
   g.C = C;
-  g.lz = std::max(1, kFftTile / line_stride(g.nz));
-  g.kty = std::max(1, std::min(g.nz, kFftTile / line_stride(g.ny)));
-  g.ktx = std::max(1, std::min(g.nz, kFftTile / (g.nc * line_stride(g.nx))));
+  if (g.layout == CPM_FFT_LAYOUT_SLAB) {
+    g.h = g.nz / 2 + 1;
+    g.reg = slab_region(g.nx, g.ny, g.nz, g.nc);
+    // x tiles: as many columns as a region holds, spread evenly over the waves of G CTAs, a
+    // multiple of 4 columns (32-byte segments of the complex rows) where that still fits
+    const int64_t Hc = (int64_t)g.h * g.ny;
+    const int cap = std::max(1, g.reg / (g.nc * line_stride(g.nx)));
+    const int64_t waves = std::max<int64_t>(1, ((Hc + cap - 1) / cap + G - 1) / G);
+    int pc = (int)std::min<int64_t>(cap, (Hc + waves * G - 1) / (waves * G));
+    if ((pc + 3) / 4 * 4 <= cap) pc = (pc + 3) / 4 * 4;
+    g.pc = std::max(1, pc);
+  } else {
+    g.lz = tile_lines(std::max(1, kFftTile / line_stride(g.nz)), (int64_t)g.nc * g.nx * g.ny, G);
+    g.kty = tile_lines(std::max(1, std::min(g.nz, kFftTile / line_stride(g.ny))), (int64_t)g.nc * g.nx * g.nz, G);
+    g.ktx = tile_lines(std::max(1, std::min(g.nz, kFftTile / (g.nc * line_stride(g.nx)))), (int64_t)g.ny * g.nz, G);
+  }
   return g;
-}
-
-static bool precond_dims_ok(int nx, int ny, int nz, int nc) {
-  int r[kFftMaxPass];
-  return nx >= 3 && ny >= 3 && nz >= 3 && (nc == 1 || nc == 3) && line_stride(nx) * nc <= kFftTile &&
-         line_stride(ny) <= kFftTile && line_stride(nz) <= kFftTile &&
-         (int64_t)nx * ny * nz * nc < ((int64_t)1 << 31) && radices(nx, r) >= 0 &&
-         radices(ny, r) >= 0 && radices(nz, r) >= 0;
 }
 
 // ---------------------------------------------------------------- the preconditioned solve
@@ -319,15 +584,102 @@ struct FftCGArgs {
   unsigned long long timeout_ns;
   int64_t dofs_per_cta;
   int quads;
+  int anchor;  // >= 0: direct refinement with this pinned node; -1: preconditioned CG
 };
 
 constexpr int kInnerMax = 200;  // iterations of one inner preconditioned solve (a safety bound)
 
+// q = A32 p on this CTA's DOFs [d0, d1); returns the thread's FP32 partial of p . q.
+template <int NC, int NT>
+__device__ __forceinline__ float product32(const FftCGArgs &a, int64_t d0, int64_t d1) {
+  const int64_t n = a.S.n;
+  const float *p = a.p;
+  float *q = a.q;
+  float pqf[1] = {0.0f};
+  if (a.quads) {
+    for (int64_t qd = d0 + 4 * threadIdx.x; qd < d1; qd += 4 * NT) {
+      float y[4][NC];
+      apply4_c<float, NC, 1>(a.S, a.S.c32, p, (int)qd, y);
+      quad_store<float, NC, 1>(q, n, qd, y);
+      quad_dot<NC, 1>(p, n, qd, y, pqf);
+    }
+  } else {
+    for (int64_t dof = d0 + threadIdx.x; dof < d1; dof += NT) {
+      float y[NC];
+      apply<float, NC, 1>(a.S, p, (int)dof, y);
+#pragma unroll
+      for (int u = 0; u < NC; ++u) {
+        const int64_t i = uidx<NC, 1>(n, dof, u);
+        q[i] = y[u];
+        pqf[0] = fmaf(p[i], y[u], pqf[0]);
+      }
+    }
+  }
+  return pqf[0];
+}
+
+// t = b - A64 x on this CTA's DOFs: r = t (FP32), d = 0; v[0] = the thread's FP64 partial of t . t
+// and, with SUMS, v[1 + c] = its partial of the sum of component c of t.
+template <int NC, int NT, bool SUMS, int NV>
+__device__ __forceinline__ void true_residual64(const FftCGArgs &a, int64_t d0, int64_t d1, double (&v)[NV]) {
+  const int64_t n = a.S.n;
+#pragma unroll
+  for (int j = 0; j < NV; ++j) v[j] = 0.0;
+  for (int64_t dof = d0 + threadIdx.x; dof < d1; dof += NT) {
+    double y[NC];
+    apply<double, NC, 1>(a.S, a.x, (int)dof, y);
+#pragma unroll
+    for (int u = 0; u < NC; ++u) {
+      const int64_t i = uidx<NC, 1>(n, dof, u);
+      const double t = a.b[i] - y[u];
+      a.r[i] = (float)t;
+      if (!SUMS) a.d[i] = 0.0f;
+      v[0] = fma(t, t, v[0]);
+      if (SUMS) v[1 + u] += t;
+    }
+  }
+}
+
+// The right-hand side t~ of the direct step (CTA 0, after the residual's grid sum): the free
+// nodes r next to the anchor a take (C_ra t_a)_r = sum_q c_pq(a - r) t_a,q, and the anchor takes
+// minus the sum over the free nodes, so that every component of t~ sums to zero.  ta: t at the
+// anchor (FP64); v[1 + c]: the sum of component c of t over all nodes.
 template <int NC>
-__global__ void __launch_bounds__(kFftThreads, 2) cg_stencil_fft_kernel(const __grid_constant__ FftCGArgs a) {
+__device__ __forceinline__ void anchor_rhs(const FftCGArgs &a, const double (&ta)[NC], const double *v, float *r) {
+  const int an = a.anchor, nx = a.S.nx, ny = a.S.ny, nz = a.S.nz;
+  const int64_t n = a.S.n;
+  const int ia = an / (ny * nz), ja = (an / nz) % ny, ka = an % nz;
+  const int t = threadIdx.x;
+  if (t < 27 * NC && t % 27 != 13) {
+    const int d = t % 27, p = t / 27;
+    const int dx = d / 9 - 1, dy = (d / 3) % 3 - 1, dz = d % 3 - 1;
+    // the row r with r + d = a (periodic): its column a carries c(d)
+    const int node = (((ia - dx + nx) % nx) * ny + (ja - dy + ny) % ny) * nz + (ka - dz + nz) % nz;
+    double corr = 0.0;
+#pragma unroll
+    for (int q = 0; q < NC; ++q) corr = fma(a.S.c64[(p * NC + q) * 27 + d], ta[q], corr);
+    r[(int64_t)p * n + node] += (float)corr;
+  }
+  if (t < NC) {
+    double s = v[1 + t] - ta[t];
+    for (int d = 0; d < 27; ++d) {
+      if (d == 13) continue;
+#pragma unroll
+      for (int q = 0; q < NC; ++q) s = fma(a.S.c64[(t * NC + q) * 27 + d], ta[q], s);
+    }
+    r[(int64_t)t * n + an] = (float)(-s);
+  }
+}
+
+template <int NC, int LAYOUT>
+__global__ void __launch_bounds__(FftShape<LAYOUT>::threads, FftShape<LAYOUT>::blocks)
+    cg_stencil_fft_kernel(const __grid_constant__ FftCGArgs a) {
+  constexpr int NT = FftShape<LAYOUT>::threads, NW = NT / kWarp;
   extern __shared__ float2 fsm[];
-  float2 *s0 = fsm, *s1 = fsm + kFftTile;
-  __shared__ double s_red[3][kCGWarps];
+  float2 *s0 = fsm, *s1 = fsm + fft_region(a.F);
+  const float2 *twx, *twy, *twz;
+  load_twiddles(a.F, fsm, twx, twy, twz);
+  __shared__ double s_red[3][NW];
   const int64_t n = a.S.n;
   const int64_t d0 = min(n, (int64_t)blockIdx.x * a.dofs_per_cta);
   const int64_t d1 = min(n, d0 + a.dofs_per_cta);
@@ -340,7 +692,7 @@ __global__ void __launch_bounds__(kFftThreads, 2) cg_stencil_fft_kernel(const __
 
   // ---- ||b||; x = 0 for a cold start
   double v[1] = {0.0};
-  for (int64_t dof = d0 + threadIdx.x; dof < d1; dof += kFftThreads)
+  for (int64_t dof = d0 + threadIdx.x; dof < d1; dof += NT)
 #pragma unroll
     for (int u = 0; u < NC; ++u) {
       const int64_t i = uidx<NC, 1>(n, dof, u);
@@ -348,7 +700,7 @@ __global__ void __launch_bounds__(kFftThreads, 2) cg_stencil_fft_kernel(const __
       v[0] = fma(bi, bi, v[0]);
       if (!use_init) x[i] = 0.0;
     }
-  if (!grid_sum<1>(v, a.part, par, a.bar, tns, s_red)) {
+  if (!grid_sum<1, NW, NT>(v, a.part, par, a.bar, tns, s_red)) {
     set_status(a.info, CPM_BARRIER_TIMEOUT);
     return;
   }
@@ -358,27 +710,53 @@ __global__ void __launch_bounds__(kFftThreads, 2) cg_stencil_fft_kernel(const __
   double resid = 0.0;
   if (bnorm == 0.0) {
     // cupyx cg returns b itself for a zero right-hand side
-    for (int64_t dof = d0 + threadIdx.x; dof < d1; dof += kFftThreads)
+    for (int64_t dof = d0 + threadIdx.x; dof < d1; dof += NT)
 #pragma unroll
       for (int u = 0; u < NC; ++u) x[uidx<NC, 1>(n, dof, u)] = b[uidx<NC, 1>(n, dof, u)];
     conv = 1;
   }
-  while (!conv) {
-    // ---- true residual t = b - A64 x (x complete after the last barrier): r = t, d = 0
-    double tt[1] = {0.0};
-    for (int64_t dof = d0 + threadIdx.x; dof < d1; dof += kFftThreads) {
-      double y[NC];
-      apply<double, NC, 1>(a.S, x, (int)dof, y);
+  // ---- direct refinement: x += A^-1 t with the anchored exact inverse, one FFT solve per step
+  while (!conv && a.anchor >= 0) {
+    const int an = a.anchor;
+    double v[1 + NC];
+    true_residual64<NC, NT, true>(a, d0, d1, v);
+    if (!grid_sum<1 + NC, NW, NT>(v, a.part, par, a.bar, tns, s_red)) { status = CPM_BARRIER_TIMEOUT; break; }
+    resid = sqrt(v[0]);
+    if (!isfinite(resid)) { status = CPM_NONFINITE; break; }
+    if (resid <= atol) { conv = 1; break; }
+    if (iters >= a.maxiter) break;
+    outer += 1;
+    iters += 1;
+    // the anchored rows are identity rows: t_a = b_a - x_a
+    double ta[NC];
+#pragma unroll
+    for (int c = 0; c < NC; ++c) ta[c] = b[(int64_t)c * n + an] - x[(int64_t)c * n + an];
+    if (blockIdx.x == 0) anchor_rhs<NC>(a, ta, v, r);
+    if (!grid_sync(a.bar, gridDim.x, tns)) { status = CPM_BARRIER_TIMEOUT; break; }
+    float rzf = 0.0f;
+    if (!precondition<LAYOUT>(a.F, r, z, s0, s1, twx, twy, twz, a.bar, tns, rzf) ||
+        !grid_sync(a.bar, gridDim.x, tns)) {
+      status = CPM_BARRIER_TIMEOUT;
+      break;
+    }
+    // e = z + 1 (t_a - z_a): x += e (own unknowns), then a barrier before the next residual
+    double gam[NC];
+#pragma unroll
+    for (int c = 0; c < NC; ++c) gam[c] = ta[c] - (double)z[(int64_t)c * n + an];
+    if (!isfinite(gam[0])) { status = CPM_NONFINITE; break; }
+    for (int64_t dof = d0 + threadIdx.x; dof < d1; dof += NT)
 #pragma unroll
       for (int u = 0; u < NC; ++u) {
         const int64_t i = uidx<NC, 1>(n, dof, u);
-        const double t = b[i] - y[u];
-        r[i] = (float)t;
-        d[i] = 0.0f;
-        tt[0] = fma(t, t, tt[0]);
+        x[i] += (double)z[i] + gam[u];
       }
-    }
-    if (!grid_sum<1>(tt, a.part, par, a.bar, tns, s_red)) { status = CPM_BARRIER_TIMEOUT; break; }
+    if (!grid_sync(a.bar, gridDim.x, tns)) { status = CPM_BARRIER_TIMEOUT; break; }
+  }
+  while (!conv && a.anchor < 0 && status == CPM_OK) {
+    // ---- true residual t = b - A64 x (x complete after the last barrier): r = t, d = 0
+    double tt[1];
+    true_residual64<NC, NT, false>(a, d0, d1, tt);
+    if (!grid_sum<1, NW, NT>(tt, a.part, par, a.bar, tns, s_red)) { status = CPM_BARRIER_TIMEOUT; break; }
     resid = sqrt(tt[0]);
     if (!isfinite(resid)) { status = CPM_NONFINITE; break; }
     if (resid <= atol) { conv = 1; break; }
@@ -387,23 +765,20 @@ __global__ void __launch_bounds__(kFftThreads, 2) cg_stencil_fft_kernel(const __
     const double target = fmax(a.inner_tol * resid, 0.5 * atol);
     double rho_old = 0.0;
     for (int it = 0; it < kInnerMax && iters < a.maxiter; ++it) {
-      // ---- z = M r
-      pass_z_fwd(a.F, r, s0, s1);
-      if (!grid_sync(a.bar, gridDim.x, tns)) { status = CPM_BARRIER_TIMEOUT; break; }
-      pass_y(a.F, false, s0, s1);
-      if (!grid_sync(a.bar, gridDim.x, tns)) { status = CPM_BARRIER_TIMEOUT; break; }
-      pass_x_solve(a.F, s0, s1);
-      if (!grid_sync(a.bar, gridDim.x, tns)) { status = CPM_BARRIER_TIMEOUT; break; }
-      pass_y(a.F, true, s0, s1);
-      if (!grid_sync(a.bar, gridDim.x, tns)) { status = CPM_BARRIER_TIMEOUT; break; }
-      double rz[1] = {(double)pass_z_inv(a.F, z, r, s0, s1)};
-      if (!grid_sum<1>(rz, a.part, par, a.bar, tns, s_red)) { status = CPM_BARRIER_TIMEOUT; break; }
+      // ---- z = M r, r.z
+      float rzf = 0.0f;
+      if (!precondition<LAYOUT>(a.F, r, z, s0, s1, twx, twy, twz, a.bar, tns, rzf)) {
+        status = CPM_BARRIER_TIMEOUT;
+        break;
+      }
+      double rz[1] = {(double)rzf};
+      if (!grid_sum<1, NW, NT>(rz, a.part, par, a.bar, tns, s_red)) { status = CPM_BARRIER_TIMEOUT; break; }
       const double rho = rz[0];
       const float beta = it == 0 ? 0.0f : (float)(rho / rho_old);
       if (!isfinite(rho) || !isfinite((double)beta)) { status = CPM_NONFINITE; break; }
       rho_old = rho;
       // ---- p = z + beta p
-      for (int64_t dof = d0 + threadIdx.x; dof < d1; dof += kFftThreads)
+      for (int64_t dof = d0 + threadIdx.x; dof < d1; dof += NT)
 #pragma unroll
         for (int u = 0; u < NC; ++u) {
           const int64_t i = uidx<NC, 1>(n, dof, u);
@@ -411,33 +786,13 @@ __global__ void __launch_bounds__(kFftThreads, 2) cg_stencil_fft_kernel(const __
         }
       if (!grid_sync(a.bar, gridDim.x, tns)) { status = CPM_BARRIER_TIMEOUT; break; }
       // ---- q = A32 p, p.q
-      float pqf[1] = {0.0f};
-      if (a.quads) {
-        for (int64_t qd = d0 + 4 * threadIdx.x; qd < d1; qd += 4 * kFftThreads) {
-          float y[4][NC];
-          apply4_c<float, NC, 1>(a.S, a.S.c32, p, (int)qd, y);
-          quad_store<float, NC, 1>(q, n, qd, y);
-          quad_dot<NC, 1>(p, n, qd, y, pqf);
-        }
-      } else {
-        for (int64_t dof = d0 + threadIdx.x; dof < d1; dof += kFftThreads) {
-          float y[NC];
-          apply<float, NC, 1>(a.S, p, (int)dof, y);
-#pragma unroll
-          for (int u = 0; u < NC; ++u) {
-            const int64_t i = uidx<NC, 1>(n, dof, u);
-            q[i] = y[u];
-            pqf[0] = fmaf(p[i], y[u], pqf[0]);
-          }
-        }
-      }
-      double pq[1] = {(double)pqf[0]};
-      if (!grid_sum<1>(pq, a.part, par, a.bar, tns, s_red)) { status = CPM_BARRIER_TIMEOUT; break; }
+      double pq[1] = {(double)product32<NC, NT>(a, d0, d1)};
+      if (!grid_sum<1, NW, NT>(pq, a.part, par, a.bar, tns, s_red)) { status = CPM_BARRIER_TIMEOUT; break; }
       const float alpha = (float)(rho / pq[0]);
       if (!isfinite((double)alpha)) { status = CPM_NONFINITE; break; }
       // ---- d += alpha p, r -= alpha q, r.r
       float rrf = 0.0f;
-      for (int64_t dof = d0 + threadIdx.x; dof < d1; dof += kFftThreads)
+      for (int64_t dof = d0 + threadIdx.x; dof < d1; dof += NT)
 #pragma unroll
         for (int u = 0; u < NC; ++u) {
           const int64_t i = uidx<NC, 1>(n, dof, u);
@@ -447,14 +802,14 @@ __global__ void __launch_bounds__(kFftThreads, 2) cg_stencil_fft_kernel(const __
           rrf = fmaf(rn, rn, rrf);
         }
       double rr[1] = {(double)rrf};
-      if (!grid_sum<1>(rr, a.part, par, a.bar, tns, s_red)) { status = CPM_BARRIER_TIMEOUT; break; }
+      if (!grid_sum<1, NW, NT>(rr, a.part, par, a.bar, tns, s_red)) { status = CPM_BARRIER_TIMEOUT; break; }
       iters += 1;
       if (!isfinite(rr[0])) { status = CPM_NONFINITE; break; }
       if (sqrt(rr[0]) <= target) break;
     }
     if (status != CPM_OK) break;
     // ---- x += d (own unknowns), then a barrier before the next true residual gathers x
-    for (int64_t dof = d0 + threadIdx.x; dof < d1; dof += kFftThreads)
+    for (int64_t dof = d0 + threadIdx.x; dof < d1; dof += NT)
 #pragma unroll
       for (int u = 0; u < NC; ++u) {
         const int64_t i = uidx<NC, 1>(n, dof, u);
@@ -477,19 +832,31 @@ __global__ void __launch_bounds__(kFftThreads, 2) cg_stencil_fft_kernel(const __
 }
 
 // ---------------------------------------------------------------- M r alone (tests)
-__global__ void __launch_bounds__(kFftThreads) fft_pass_kernel(const __grid_constant__ FftGrid g, int which,
-                                                               const float *r, float *zout) {
+// One pass of z = M r per launch (the launches order the passes): slab passes 0..2, five-pass 0..4.
+__global__ void __launch_bounds__(512) fft_pass_kernel(const __grid_constant__ FftGrid g, int which,
+                                                       const float *r, float *zout) {
   extern __shared__ float2 fsm[];
-  float2 *s0 = fsm, *s1 = fsm + kFftTile;
-  if (which == 0) pass_z_fwd(g, r, s0, s1);
-  else if (which == 1) pass_y(g, false, s0, s1);
-  else if (which == 2) pass_x_solve(g, s0, s1);
-  else if (which == 3) pass_y(g, true, s0, s1);
-  else pass_z_inv(g, zout, nullptr, s0, s1);
+  float2 *s0 = fsm, *s1 = fsm + fft_region(g);
+  const float2 *twx, *twy, *twz;
+  load_twiddles(g, fsm, twx, twy, twz);
+  if (g.layout == CPM_FFT_LAYOUT_SLAB) {
+    if (which == 0) slab_fwd(g, r, s0, s1, twy, twz);
+    else if (which == 1) slab_x_solve(g, s0, s1, twx);
+    else slab_inv(g, zout, nullptr, s0, s1, twy, twz);
+  } else {
+    if (which == 0) pass_z_fwd(g, r, s0, s1, twz);
+    else if (which == 1) pass_y(g, false, s0, s1, twy);
+    else if (which == 2) pass_x_solve(g, s0, s1, twx);
+    else if (which == 3) pass_y(g, true, s0, s1, twy);
+    else pass_z_inv(g, zout, nullptr, s0, s1, twz);
+  }
 }
 
 static int precond_check(const cpm_fft_precond *P, const char *who) {
-  if (!P || !P->dev || !precond_dims_ok(P->nx, P->ny, P->nz, P->ncomp)) {
+  if (!P || !P->dev || !precond_dims_ok(P->nx, P->ny, P->nz, P->ncomp) ||
+      (P->layout != CPM_FFT_LAYOUT_SLAB && P->layout != CPM_FFT_LAYOUT_PASSES) ||
+      (P->layout == CPM_FFT_LAYOUT_SLAB && !slab_fits(P->nx, P->ny, P->nz, P->ncomp)) || P->anchor < -1 ||
+      (int64_t)P->anchor >= (int64_t)P->nx * P->ny * P->nz) {
     set_error("%s: bad preconditioner plan", who);
     return CPM_BAD_ARG;
   }
@@ -512,7 +879,7 @@ static size_t fft_cg_layout(int64_t n, int nc, char *base, Workspace *w, float2 
   t.q32 = (float *)take(4 * nv);
   t.d32 = (float *)take(4 * nv);
   float *zz = (float *)take(4 * nv);
-  float2 *cc = (float2 *)take(8 * nv);
+  float2 *cc = (float2 *)take(8 * nv);  // the full spectrum (the slab layout uses about half)
   if (w) *w = t;
   if (C) *C = cc;
   if (z) *z = zz;
@@ -535,6 +902,16 @@ extern "C" int cpm_fft_precond_build(const cpm_stencil *S, void *dev, int64_t by
               "aligned device buffer)");
     return CPM_BAD_ARG;
   }
+  const int want = P->layout;
+  if (want != CPM_FFT_LAYOUT_AUTO && want != CPM_FFT_LAYOUT_SLAB && want != CPM_FFT_LAYOUT_PASSES) {
+    set_error("cpm_fft_precond_build: unknown layout %d", want);
+    return CPM_BAD_ARG;
+  }
+  if (want == CPM_FFT_LAYOUT_SLAB && !slab_fits(S->nx, S->ny, S->nz, S->ncomp)) {
+    set_error("cpm_fft_precond_build: an x-plane of the %dx%dx%d grid does not fit the slab layout's shared "
+              "memory", S->nx, S->ny, S->nz);
+    return CPM_BAD_ARG;
+  }
   const PrecondLayout L = precond_layout(S->nx, S->ny, S->nz, S->ncomp);
   if (bytes < (int64_t)L.total) {
     set_error("cpm_fft_precond_build: buffer too small (%lld < %zu bytes)", (long long)bytes, L.total);
@@ -544,6 +921,12 @@ extern "C" int cpm_fft_precond_build(const cpm_stencil *S, void *dev, int64_t by
   P->ny = S->ny;
   P->nz = S->nz;
   P->ncomp = S->ncomp;
+  const int64_t nodes = (int64_t)S->nx * S->ny * S->nz;
+  if (P->anchor < -1 || P->anchor >= nodes || (P->anchor >= 0 && !S->flags)) {
+    set_error("cpm_fft_precond_build: anchor %d is not a node of the grid, or the stencil has no flags", P->anchor);
+    return CPM_BAD_ARG;
+  }
+  P->layout = want == CPM_FFT_LAYOUT_AUTO ? auto_layout(S->nx, S->ny, S->nz, S->ncomp) : want;
   P->dev = dev;
   P->bytes = (int64_t)L.total;
   cudaStream_t st = (cudaStream_t)stream;
@@ -570,6 +953,8 @@ extern "C" int cpm_fft_precond_build(const cpm_stencil *S, void *dev, int64_t by
   s.ny = S->ny;
   s.nz = S->nz;
   s.nc = S->ncomp;
+  s.slab = P->layout == CPM_FFT_LAYOUT_SLAB;
+  s.h = S->nz / 2 + 1;
   const int nc2 = 27 * S->ncomp * S->ncomp;
   for (int i = 0; i < 243; ++i) s.c[i] = i < nc2 ? S->coef[i] : 0.0;
   // the zero wave vector (the translations, singular in the circulant part) gets the operator's diagonal
@@ -588,7 +973,23 @@ extern "C" int cpm_fft_precond_build(const cpm_stencil *S, void *dev, int64_t by
   const int64_t n = (int64_t)S->nx * S->ny * S->nz;
   const int g = (int)std::max<int64_t>(1, std::min<int64_t>((n + 255) / 256, (int64_t)sm_count() * 16));
   fft_symbol_kernel<<<g, 256, 0, st>>>(s);
-  return check_launch("cpm_fft_precond_build");
+  if (int e = check_launch("cpm_fft_precond_build")) return e;
+  if (P->anchor >= 0) {
+    // the direct solve inverts exactly the circulant with one pinned node: check the flags say so
+    int *bad = (int *)(base + L.check);
+    CPM_TRY(cudaMemsetAsync(bad, 0, sizeof(int), st));
+    anchor_check_kernel<<<g, 256, 0, st>>>(S->flags, n, P->anchor, bad);
+    if (int e = check_launch("cpm_fft_precond_build")) return e;
+    int h_bad = 0;
+    CPM_TRY(cudaMemcpyAsync(&h_bad, bad, sizeof(int), cudaMemcpyDeviceToHost, st));
+    CPM_TRY(cudaStreamSynchronize(st));
+    if (h_bad) {
+      set_error("cpm_fft_precond_build: the stencil's flags are not one pinned node at %d (%d nodes differ)",
+                P->anchor, h_bad);
+      return CPM_BAD_ARG;
+    }
+  }
+  return CPM_OK;
 }
 
 extern "C" int cpm_fft_precond_apply(const cpm_fft_precond *P, const float *r, float *z, void *work,
@@ -601,13 +1002,15 @@ extern "C" int cpm_fft_precond_apply(const cpm_fft_precond *P, const float *r, f
               (long long)(8 * n * P->ncomp));
     return CPM_BAD_ARG;
   }
-  const FftGrid g = grid_of(P, (float2 *)work);
-  const size_t smem = 2 * kFftTile * sizeof(float2);
+  const bool slab = P->layout == CPM_FFT_LAYOUT_SLAB;
+  const int G = sm_count() * 2;
+  const FftGrid g = grid_of(P, (float2 *)work, G);
+  const size_t smem = fft_smem_bytes(g);
   CPM_TRY(cudaFuncSetAttribute((const void *)fft_pass_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                (int)smem));
   cudaStream_t st = (cudaStream_t)stream;
-  for (int w = 0; w < 5; ++w) {
-    fft_pass_kernel<<<sm_count() * 2, kFftThreads, smem, st>>>(g, w, r, z);
+  for (int w = 0; w < (slab ? 3 : 5); ++w) {
+    fft_pass_kernel<<<G, slab ? 512 : 256, smem, st>>>(g, w, r, z);
     if (int e = check_launch("cpm_fft_precond_apply")) return e;
   }
   return CPM_OK;
@@ -650,7 +1053,6 @@ extern "C" int cpm_cg_solve_stencil_fft(const cpm_stencil *S, const cpm_fft_prec
     a.S.c64[i] = i < ncoef ? S->coef[i] : 0.0;
     a.S.c32[i] = (float)a.S.c64[i];
   }
-  a.F = grid_of(P, C);
   a.b = b;
   a.x = x;
   a.tol = o->tol;
@@ -669,11 +1071,20 @@ extern "C" int cpm_cg_solve_stencil_fft(const cpm_stencil *S, const cpm_fft_prec
   const double tmo = o->barrier_timeout_s > 0 ? o->barrier_timeout_s : 2.0;
   a.timeout_ns = (unsigned long long)(tmo * 1e9);
   a.quads = (S->nz & 3) == 0 && ((uintptr_t)S->flags & 3) == 0;
-  const void *fn = nc == 3 ? (const void *)cg_stencil_fft_kernel<3> : (const void *)cg_stencil_fft_kernel<1>;
-  const size_t smem = 2 * kFftTile * sizeof(float2);
+  a.anchor = (P->anchor >= 0 && o->form != CPM_CG_FORM_FFT_PCG) ? P->anchor : -1;
+  const bool slab = P->layout == CPM_FFT_LAYOUT_SLAB;
+  const void *fn = slab ? (nc == 3 ? (const void *)cg_stencil_fft_kernel<3, CPM_FFT_LAYOUT_SLAB>
+                                   : (const void *)cg_stencil_fft_kernel<1, CPM_FFT_LAYOUT_SLAB>)
+                        : (nc == 3 ? (const void *)cg_stencil_fft_kernel<3, CPM_FFT_LAYOUT_PASSES>
+                                   : (const void *)cg_stencil_fft_kernel<1, CPM_FFT_LAYOUT_PASSES>);
+  const int threads = slab ? FftShape<CPM_FFT_LAYOUT_SLAB>::threads : FftShape<CPM_FFT_LAYOUT_PASSES>::threads;
+  // the tiles depend on the grid size and the shared memory on the layout; the grid size on the
+  // occupancy of that shared memory (the region size does not depend on G)
+  FftGrid g0 = grid_of(P, C, 1);
+  const size_t smem = fft_smem_bytes(g0);
   CPM_TRY(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   int occ = 0;
-  CPM_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fn, kFftThreads, smem));
+  CPM_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fn, threads, smem));
   if (occ < 1) {
     set_error("cpm_cg_solve_stencil_fft: kernel cannot be resident on an SM");
     return CPM_CUDA_ERROR;
@@ -683,9 +1094,10 @@ extern "C" int cpm_cg_solve_stencil_fft(const cpm_stencil *S, const cpm_fft_prec
   per = (per + 31) / 32 * 32;
   G = std::max<int64_t>(1, (n + per - 1) / per);
   a.dofs_per_cta = per;
+  a.F = grid_of(P, C, G);
   CPM_TRY(cudaMemsetAsync(w.bar, 0, sizeof(GridBarrier), (cudaStream_t)stream));
   CPM_TRY(cudaMemsetAsync(info, 0, sizeof(cpm_cg_info), (cudaStream_t)stream));
   void *args[] = {&a};
-  CPM_TRY(cudaLaunchCooperativeKernel(fn, dim3((unsigned)G), dim3(kFftThreads), args, smem, (cudaStream_t)stream));
+  CPM_TRY(cudaLaunchCooperativeKernel(fn, dim3((unsigned)G), dim3(threads), args, smem, (cudaStream_t)stream));
   return CPM_OK;
 }

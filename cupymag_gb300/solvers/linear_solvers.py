@@ -33,6 +33,7 @@ class CGSolver:
         self.barrier_timeout_s = 2.0
         self.inner_tol = 0.1   # reliable-update factor of the mixed-precision solver
         self.max_outer = 60
+        self.fft_layout = N.FFT_LAYOUT_AUTO  # spectrum layout of the FFT-preconditioned solves
 
     def workspace(self, n, nrhs, prec):
         key = (n, nrhs, prec)
@@ -50,13 +51,15 @@ class CGSolver:
 
         form (FP32 stencil solves): N.CG_FORM_DEFAULT (three grid barriers per iteration),
         N.CG_FORM_THREE_BARRIER or N.CG_FORM_TWO_BARRIER (opt-in).
-        precond="fft" (FP32 form on a stencil operator with one right-hand side): CG preconditioned by
-        the operator's circulant inverse inside FP64 refinement (inner_tol: the residual drop of each
-        inner solve); the plain FP32 form is used where the grid has no FFT plan."""
+        precond="fft" (FP32 form on a stencil operator with one right-hand side): FP64 refinement
+        whose steps solve with the operator's circulant inverse, exactly (one FFT solve per step)
+        where the operator pins one node, else as the preconditioner of FP32 CG (inner_tol: the
+        residual drop of each inner solve; form=N.CG_FORM_FFT_PCG asks for that form); the plain
+        FP32 form is used where the grid has no FFT plan."""
         prec = PRECISIONS[precision] if isinstance(precision, str) else int(precision)
         if precond == "fft" and prec == 1 and hasattr(A, "fft_plan") and b.dim() == 1 and A.fft_plan() is not None:
             return self._launch_fft(A, b, x, info, tol=tol, maxiter=maxiter, use_init=use_init,
-                                    use_init_dev=use_init_dev, inner_tol=inner_tol)
+                                    use_init_dev=use_init_dev, inner_tol=inner_tol, form=form)
         if prec == 1:
             A.ensure_fp32()
         n = A.shape[0]
@@ -82,7 +85,7 @@ class CGSolver:
                    info.data_ptr(), N.stream_ptr()), "cpm_cg_solve")
 
 
-    def _launch_fft(self, A, b, x, info, *, tol, maxiter, use_init, use_init_dev, inner_tol):
+    def _launch_fft(self, A, b, x, info, *, tol, maxiter, use_init, use_init_dev, inner_tol, form=0):
         if b.shape[0] != A.shape[0] or x.shape != b.shape or b.dtype != torch.float64 or x.dtype != torch.float64 \
                 or not (b.is_contiguous() and x.is_contiguous()):
             raise ValueError("b and x must be contiguous float64 device vectors of the operator's size")
@@ -99,8 +102,10 @@ class CGSolver:
         o.use_init_dev = use_init_dev.data_ptr() if use_init_dev is not None else None
         o.precision = 1
         o.inner_tol = 1e-4 if inner_tol is None else float(inner_tol)
+        o.form = int(form)
         o.barrier_timeout_s = self.barrier_timeout_s
-        N.check(N.lib().cpm_cg_solve_stencil_fft(A.struct(), A.fft_plan(), b.data_ptr(), x.data_ptr(), C.byref(o),
+        N.check(N.lib().cpm_cg_solve_stencil_fft(A.struct(), A.fft_plan(self.fft_layout), b.data_ptr(),
+                                                 x.data_ptr(), C.byref(o),
                                                  ws.data_ptr(), ws.numel(), info.data_ptr(), N.stream_ptr()),
                 "cpm_cg_solve_stencil_fft")
 

@@ -24,8 +24,13 @@ class StencilOperator:
         self.coef_host = coef.copy()
         self._dev = torch.device(dev)
         self.n = self.nx * self.ny * self.nz
+        # the one node whose rows and columns the operator pins (the reference's anchor), or -1
+        self.anchor = -1
         if flags is not None:
             flags = self.mark_neighbours(np.asarray(flags, dtype=np.uint8).copy())
+            marked = np.flatnonzero(flags & 7)
+            if marked.size == 1 and (flags[marked[0]] & 7) == (ROW_IDENTITY | COL_EXCLUDED):
+                self.anchor = int(marked[0])
         self.flags = None if flags is None else torch.as_tensor(flags, device=dev)
         self.shape = (self.n * self.ncomp, self.n * self.ncomp)
         self._struct = None
@@ -84,10 +89,11 @@ class StencilOperator:
     def __matmul__(self, x):
         return self.spmv(x)
 
-    def fft_plan(self):
-        """The circulant-inverse preconditioner of this operator (built once; None when the grid's
-        dimensions are not supported)."""
-        if getattr(self, "_fft", None) is None:
+    def fft_plan(self, layout: int = N.FFT_LAYOUT_AUTO):
+        """The circulant-inverse preconditioner of this operator in the given spectrum layout
+        (N.FFT_LAYOUT_*; built once per layout; None when the grid's dimensions are not supported)."""
+        plans = self.__dict__.setdefault("_fft", {})
+        if layout not in plans:
             nb = int(N.lib().cpm_fft_precond_bytes(self.nx, self.ny, self.nz, self.ncomp))
             if nb <= 0:
                 return None
@@ -95,14 +101,17 @@ class StencilOperator:
             if mem.data_ptr() % 256:
                 raise RuntimeError("plan memory is not 256-byte aligned")
             plan = N.FftPrecondC()
+            plan.layout = int(layout)
+            plan.anchor = self.anchor
             N.check(N.lib().cpm_fft_precond_build(self.struct(), mem.data_ptr(), nb, plan, N.stream_ptr()),
                     "cpm_fft_precond_build")
-            self._fft = (plan, mem)
-        return self._fft[0]
+            plans[layout] = (plan, mem)
+        return plans[layout][0]
 
-    def precondition32(self, r: torch.Tensor, out: torch.Tensor = None) -> torch.Tensor:
+    def precondition32(self, r: torch.Tensor, out: torch.Tensor = None,
+                       layout: int = N.FFT_LAYOUT_AUTO) -> torch.Tensor:
         """z = M r with M the circulant-inverse preconditioner (FP32), as the preconditioned solve applies it."""
-        plan = self.fft_plan()
+        plan = self.fft_plan(layout)
         if plan is None:
             raise ValueError(f"no FFT preconditioner for a {self.nx} x {self.ny} x {self.nz} grid")
         r = r.contiguous()

@@ -66,7 +66,9 @@ typedef struct {
   double inner_tol;        /* reliable update when the FP32 residual fell by this factor (default 0.1) */
   int32_t max_outer;       /* unused (kept for layout) */
   int32_t form;            /* FP32 stencil solvers: CPM_CG_FORM_DEFAULT (= three grid barriers per
-                              iteration), CPM_CG_FORM_THREE_BARRIER, CPM_CG_FORM_TWO_BARRIER */
+                              iteration), CPM_CG_FORM_THREE_BARRIER, CPM_CG_FORM_TWO_BARRIER;
+                              FFT solves: CPM_CG_FORM_DEFAULT (direct refinement with an anchored
+                              plan) or CPM_CG_FORM_FFT_PCG */
   double barrier_timeout_s;/* bound on every grid-barrier wait (seconds) */
 } cpm_cg_opts;
 
@@ -76,7 +78,7 @@ typedef struct {
  * sums instead of two reductions and a third barrier.  The two-barrier form is
  * opt-in: on GB300 it measured slower per iteration, and its FP32 recurrences
  * drift enough to stall the 128^3 elastic and demag solves. */
-enum { CPM_CG_FORM_DEFAULT = 0, CPM_CG_FORM_THREE_BARRIER = 1, CPM_CG_FORM_TWO_BARRIER = 2 };
+enum { CPM_CG_FORM_DEFAULT = 0, CPM_CG_FORM_THREE_BARRIER = 1, CPM_CG_FORM_TWO_BARRIER = 2, CPM_CG_FORM_FFT_PCG = 3 };
 
 /* ---- library ---- */
 const char *cpm_version(void);
@@ -295,18 +297,35 @@ int cpm_volavg(int64_t n, int ncomp, const double *f, const double *w, double vo
  * (per wave vector k: 1 float, or the 6 floats of a symmetric 3x3 block; the
  * singular k = 0 block is replaced by the operator's diagonal).  Every line
  * length works (any prime factors).  The host struct is filled by the build
- * call; `dev` is caller-owned device memory of cpm_fft_precond_bytes(). */
+ * call; `dev` is caller-owned device memory of cpm_fft_precond_bytes().
+ *
+ * Layouts of the spectrum: SLAB keeps the nz/2 + 1 non-negative z frequencies
+ * of the real field and does the z and y DFTs of one x-plane in one pass
+ * (three passes per apply; needs an x-plane's half spectrum, about
+ * ny (nz/2 + 1) complex values twice, in the 227 KB of shared memory of an SM:
+ * every grid up to 160^3); PASSES does five passes over the full complex field
+ * (any grid).  AUTO picks SLAB where it fits. */
+enum {
+  CPM_FFT_LAYOUT_AUTO = 0,
+  CPM_FFT_LAYOUT_SLAB = 1,
+  CPM_FFT_LAYOUT_PASSES = 2
+};
+
 typedef struct {
   int32_t nx, ny, nz, ncomp;
   void *dev;               /* device memory of the plan (twiddles, inverse symbol) */
   int64_t bytes;
   int32_t npass[3];        /* radix passes per axis */
   int32_t radix[3][16];
+  int32_t layout;          /* in: the requested CPM_FFT_LAYOUT_*; out: the plan's (SLAB or PASSES) */
+  int32_t anchor;          /* in: the node whose rows and columns the operator pins (flags 1|4 there,
+                              no flag but 8 elsewhere; the build checks), or -1 */
 } cpm_fft_precond;
 
 /* Device bytes of a plan for an nx x ny x nz grid (ncomp 1 or 3); 0 when unsupported. */
 int64_t cpm_fft_precond_bytes(int32_t nx, int32_t ny, int32_t nz, int32_t ncomp);
-/* Build the plan of stencil operator S into dev (256-byte aligned). */
+/* Build the plan of stencil operator S into dev (256-byte aligned), in the layout P->layout asks
+ * for (CPM_BAD_ARG for SLAB on a grid it does not fit). */
 int cpm_fft_precond_build(const cpm_stencil *S, void *dev, int64_t bytes, cpm_fft_precond *P, void *stream);
 /* z = M r alone (FP32; r, z of ncomp*n values, [x|y|z] blocks for ncomp 3); work: a complex
  * buffer of 8 * ncomp * n bytes, 16-byte aligned. */
@@ -314,9 +333,16 @@ int cpm_fft_precond_apply(const cpm_fft_precond *P, const float *r, float *z, vo
                           void *stream);
 /* The solve: same contract as cpm_cg_solve_stencil (b, x FP64, tol, maxiter, warm-start flag,
  * stopping test ||b - A x|| <= tol ||b|| on the FP64 residual, zero b returns b, the
- * reference's status on maxiter), for nrhs 1.  opts->inner_tol is the residual drop of each
- * FP32 preconditioned inner solve (default 1e-4); info->iters[0] counts inner iterations and
- * info->outer the FP64 residuals. */
+ * reference's status on maxiter), for nrhs 1.
+ *
+ * With an anchored plan (P->anchor >= 0) the solve is direct refinement: A = [[I, 0], [0, C_rr]]
+ * (C the circulant, node a pinned) is inverted exactly by e = C+ t~ + 1 (t_a - (C+ t~)_a), where
+ * t~ = t plus C_ra t_a on the free nodes and minus the sum of those at a (so t~ sums to zero,
+ * orthogonal to the translations that span ker C), C+ t~ the FFT apply.  Each outer step is one
+ * FP64 residual and one FP32 FFT solve; info->iters[0] and info->outer count the steps.
+ * Otherwise (or with opts->form = CPM_CG_FORM_FFT_PCG) FP32 CG preconditioned by C'^-1 runs
+ * inside the refinement: opts->inner_tol is the residual drop of each inner solve (default
+ * 1e-4); info->iters[0] counts inner iterations and info->outer the FP64 residuals. */
 size_t cpm_cg_fft_workspace_bytes(int32_t nx, int32_t ny, int32_t nz, int32_t ncomp);
 int cpm_cg_solve_stencil_fft(const cpm_stencil *S, const cpm_fft_precond *P, const double *b, double *x,
                              const cpm_cg_opts *opts, void *workspace, size_t workspace_bytes,

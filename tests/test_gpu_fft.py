@@ -6,10 +6,16 @@ circulant part (the singular zero wave vector replaced by the operator's
 diagonal) with DFTs along each axis in shared memory.  Checked here:
 
 * z = M r against the same inverse computed on the host with numpy's FFT, on
-  grids whose line lengths have factors 2, 3, 4, 5, 7, 11 and primes;
-* the preconditioned solve meets the FP64 stopping test ||b - A x|| <= tol ||b||
-  (status ok) in far fewer iterations than plain FP32 CG, cold and warm, and
-  returns b for b = 0 (cupyx semantics, cupymag/solvers/linear_solvers.py:59-74).
+  grids whose line lengths have factors 2, 3, 4, 5, 7, 8, 11 and primes, in
+  both spectrum layouts (the half spectrum of x-planes in shared memory, and
+  five passes over the full spectrum);
+* both FFT solves meet the FP64 stopping test ||b - A x|| <= tol ||b|| (status
+  ok) in far fewer iterations than plain FP32 CG, cold and warm, and return b
+  for b = 0 (cupyx semantics, cupymag/solvers/linear_solvers.py:59-74): the
+  direct refinement (the anchored operator inverted exactly by one FFT solve
+  per FP64 step) and FP32 CG preconditioned by the circulant inverse;
+* the direct step alone is the exact inverse of the anchored operator: one
+  step from x = 0 against the host's dense solve.
 """
 import numpy as np
 import pytest
@@ -44,22 +50,51 @@ def _host_inverse(coef, nc, dims, r):
     return np.fft.ifftn(U, axes=(1, 2, 3)).real.reshape(-1)
 
 
-@pytest.mark.parametrize("dims", [(8, 8, 8), (6, 10, 12), (5, 7, 11), (12, 16, 20), (9, 4, 3), (13, 6, 14)])
-def test_fft_preconditioner_is_the_circulant_inverse(dims):
+LAYOUTS = ["slab", "passes"]
+
+
+def _layout(name):
+    from cupymag_gb300 import _native as N
+    return {"slab": N.FFT_LAYOUT_SLAB, "passes": N.FFT_LAYOUT_PASSES}[name]
+
+
+@pytest.mark.parametrize("layout", LAYOUTS)
+@pytest.mark.parametrize("dims", [(8, 8, 8), (6, 10, 12), (5, 7, 11), (12, 16, 20), (9, 4, 3), (13, 6, 14),
+                                  (16, 24, 32)])
+def test_fft_preconditioner_is_the_circulant_inverse(dims, layout):
     S, p = _sim(Nx=dims[0], Ny=dims[1], Nz=dims[2], Ndx=1, Ndy=1, Ndz=1, ME=True)
     so = S.stencil_operators()
     rng = np.random.default_rng(sum(dims))
     for name in ("A_demag", "A_el"):
         op = so[name]
         r = rng.normal(size=op.shape[0]).astype(np.float32)
-        z = op.precondition32(torch.as_tensor(r, device="cuda")).cpu().numpy()
+        z = op.precondition32(torch.as_tensor(r, device="cuda"), layout=_layout(layout)).cpu().numpy()
+        assert op.fft_plan(_layout(layout)).layout == _layout(layout)
         ref = _host_inverse(op.coef_host, op.ncomp, dims, r.astype(np.float64))
         err = np.abs(z - ref).max() / np.abs(ref).max()
-        assert err <= 1e-4, (name, dims, err)
+        assert err <= 1e-4, (name, dims, layout, err)
 
 
+def test_fft_plan_picks_the_slab_layout_where_it_fits():
+    from cupymag_gb300 import _native as N
+    S, p = _sim(Nx=12, Ny=10, Nz=14, Ndx=3, Ndy=3, Ndz=3, ME=True)
+    so = S.stencil_operators()
+    for name in ("A_demag", "A_el"):
+        assert so[name].fft_plan().layout == N.FFT_LAYOUT_SLAB
+
+
+METHODS = ["direct", "pcg"]
+
+
+def _form(method):
+    from cupymag_gb300 import _native as N
+    return N.CG_FORM_DEFAULT if method == "direct" else N.CG_FORM_FFT_PCG
+
+
+@pytest.mark.parametrize("method", METHODS)
+@pytest.mark.parametrize("layout", LAYOUTS)
 @pytest.mark.parametrize("dims", [(16, 16, 16), (15, 15, 15), (12, 10, 14)])
-def test_fft_preconditioned_cg_meets_the_fp64_stopping_test(dims):
+def test_fft_solves_meet_the_fp64_stopping_test(dims, layout, method):
     from cupymag_gb300 import _native as N
     from cupymag_gb300.solvers.linear_solvers import CGSolver, decode_info, new_info
     S, p = _sim(Nx=dims[0], Ny=dims[1], Nz=dims[2], Ndx=3, Ndy=3, Ndz=3, ME=True)
@@ -73,34 +108,42 @@ def test_fft_preconditioned_cg_meets_the_fp64_stopping_test(dims):
         b[[0, n, 2 * n] if name == "A_el" else [0]] = 0.0
         bd = torch.as_tensor(b, device="cuda")
         res = {}
+        solver = CGSolver()
+        solver.fft_layout = _layout(layout)
         for precond in ("fft", None):
             x = torch.zeros_like(bd)
             info = new_info(1)
-            CGSolver().launch(so[name], bd, x, info[0], tol=1e-10, maxiter=20000, precision="IR",
-                              inner_tol=1e-4 if precond else 0.1, precond=precond)
+            solver.launch(so[name], bd, x, info[0], tol=1e-10, maxiter=20000, precision="IR",
+                          inner_tol=1e-4 if precond else 0.1, precond=precond,
+                          form=_form(method) if precond else 0)
             inf = decode_info(info[0].cpu().numpy())
             assert inf["status"] == N.CPM_OK, (name, precond, inf)
             xs = x.cpu().numpy()
             assert np.linalg.norm(b - A @ xs) <= 1e-10 * np.linalg.norm(b) * 1.001, (name, precond)
             res[precond] = (inf["iters"][0], xs)
-        print(name, dims, "FFT-preconditioned", res["fft"][0], "plain", res[None][0])
+        print(name, dims, layout, method, "FFT", res["fft"][0], "plain", res[None][0])
         assert res["fft"][0] * 3 <= res[None][0], (name, dims, res["fft"][0], res[None][0])
+        if method == "direct":
+            assert so[name].anchor == 0 and res["fft"][0] <= 4, (name, dims, res["fft"][0])
         # warm start from the solution: converged at the first FP64 residual, no inner iteration
         x = torch.as_tensor(res["fft"][1], device="cuda")
         info = new_info(1)
-        CGSolver().launch(so[name], bd, x, info[0], tol=1e-10, maxiter=20000, precision="IR", use_init=True,
-                          precond="fft")
+        solver.launch(so[name], bd, x, info[0], tol=1e-10, maxiter=20000, precision="IR", use_init=True,
+                      precond="fft", form=_form(method))
         inf = decode_info(info[0].cpu().numpy())
         assert inf["status"] == N.CPM_OK and inf["iters"][0] == 0, inf
         # zero right-hand side: x = b
         z = torch.zeros_like(bd)
         x = torch.full_like(bd, 3.0)
-        CGSolver().launch(so[name], z, x, info[0], tol=1e-10, maxiter=20000, precision="IR", precond="fft")
+        solver.launch(so[name], z, x, info[0], tol=1e-10, maxiter=20000, precision="IR", precond="fft",
+                      form=_form(method))
         inf = decode_info(info[0].cpu().numpy())
         assert inf["status"] == N.CPM_OK and float(x.abs().max()) == 0.0
 
 
-def test_fft_solve_reports_maxiter_like_the_reference():
+@pytest.mark.parametrize("method", METHODS)
+@pytest.mark.parametrize("layout", LAYOUTS)
+def test_fft_solve_reports_maxiter_like_the_reference(layout, method):
     from cupymag_gb300 import _native as N
     from cupymag_gb300.solvers.linear_solvers import CGSolver, decode_info, new_info
     S, p = _sim(Nx=12, Ny=12, Nz=12, Ndx=3, Ndy=3, Ndz=3, ME=True)
@@ -110,6 +153,33 @@ def test_fft_solve_reports_maxiter_like_the_reference():
     b[[0, op.n, 2 * op.n]] = 0.0
     x = torch.zeros_like(b)
     info = new_info(1)
-    CGSolver().launch(op, b, x, info[0], tol=1e-10, maxiter=3, precision="IR", precond="fft")
+    solver = CGSolver()
+    solver.fft_layout = _layout(layout)
+    cap = 1 if method == "direct" else 3
+    solver.launch(op, b, x, info[0], tol=1e-10, maxiter=cap, precision="IR", precond="fft", form=_form(method))
     inf = decode_info(info[0].cpu().numpy())
-    assert inf["status"] == N.CPM_NOT_CONVERGED and inf["iters"][0] == 3, inf
+    assert inf["status"] == N.CPM_NOT_CONVERGED and inf["iters"][0] == cap, inf
+
+
+@pytest.mark.parametrize("layout", LAYOUTS)
+@pytest.mark.parametrize("dims", [(6, 7, 8), (9, 4, 5)])
+def test_direct_step_is_the_exact_inverse_of_the_anchored_operator(dims, layout):
+    """One direct step from x = 0 (maxiter 1) solves A x = b to FP32 accuracy, b with a nonzero
+    value at the anchor (the correction terms at its neighbours and at the anchor all act)."""
+    from cupymag_gb300.solvers.linear_solvers import CGSolver, new_info
+    S, p = _sim(Nx=dims[0], Ny=dims[1], Nz=dims[2], Ndx=1, Ndy=1, Ndz=1, ME=True)
+    so = S.stencil_operators()
+    csr = S.host_operators()
+    rng = np.random.default_rng(5)
+    for name in ("A_demag", "A_el"):
+        A = csr[name].toarray()
+        b = rng.normal(size=A.shape[0])
+        ref = np.linalg.solve(A, b)
+        x = torch.zeros(A.shape[0], dtype=torch.float64, device="cuda")
+        info = new_info(1)
+        solver = CGSolver()
+        solver.fft_layout = _layout(layout)
+        solver.launch(so[name], torch.as_tensor(b, device="cuda"), x, info[0], tol=1e-30, maxiter=1,
+                      precision="IR", precond="fft")
+        err = np.abs(x.cpu().numpy() - ref).max() / np.abs(ref).max()
+        assert err <= 1e-4, (name, dims, layout, err)
