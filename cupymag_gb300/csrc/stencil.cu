@@ -210,7 +210,13 @@ __global__ void __launch_bounds__(kCGThreads) cg_stencil_fp64_kernel(const __gri
 // the recursive residual, so its step length is the exact line search
 // alpha = (t.p) / (p.A p).  The update costs no extra grid barrier.
 // info->outer counts the reliable updates.  With nz % 4 == 0 the FP32
-// product runs on quads of 4 DOFs along z (apply4_c).  The CG state lives in
+// product runs on quads of 4 DOFs along z (apply4_c).  Pinned DOFs (identity
+// row, excluded column: the defects of A1/A2, the anchors) are solved from the
+// start (x = b there, the reference's solution of those rows), so r, p and q
+// stay zero there and the FP32 product needs no per-neighbour column tests:
+// flagged quads keep the register-blocked form (measured on GB300, 128^3 A1
+// with a 16^3 defect: the CTAs holding the defect's quads had made every other
+// CTA wait 14 us of a 47 us iteration).  The CG state lives in
 // shared memory (IRState), updated by thread 0 after each reduction, so the
 // DOF loops keep only alpha/beta and bitmasks in registers.
 // 256-thread CTAs, four per SM (measured faster than one 1024-thread CTA per
@@ -244,13 +250,17 @@ __global__ void __launch_bounds__(kIRThreads, 4) cg_stencil_ir_kernel(const __gr
   for (int j = 0; j < 2 * NS; ++j) v[j] = 0.0;
   for (int64_t dof = d0 + threadIdx.x; dof < d1; dof += TH) {
     double y[U];
-    if (use_init) apply<double, NC, NR>(a.S, x, (int)dof, y);
+    // a pinned DOF (identity row, excluded column) is solved by x = b: its residual, and so every
+    // FP32 vector there, stays zero (the FP32 product relies on it)
+    const bool pin = a.S.flags && (a.S.flags[dof] & (kRowIdentity | kColExcluded)) == (kRowIdentity | kColExcluded);
+    if (use_init && !pin) apply<double, NC, NR>(a.S, x, (int)dof, y);
 #pragma unroll
     for (int u = 0; u < U; ++u) {
       const int64_t i = uidx<NC, NR>(n, dof, u);
       const double bi = b[i];
-      const double ri = use_init ? bi - y[u] : bi;
-      if (!use_init) x[i] = 0.0;
+      const double ri = pin ? 0.0 : use_init ? bi - y[u] : bi;
+      if (pin) x[i] = bi;
+      else if (!use_init) x[i] = 0.0;
       const float rf = (float)ri;
       r32[i] = rf;
       p32[i] = rf;
@@ -293,7 +303,7 @@ __global__ void __launch_bounds__(kIRThreads, 4) cg_stencil_ir_kernel(const __gr
     if (quads) {
       for (int64_t qd = d0 + 4 * threadIdx.x; qd < d1; qd += 4 * TH) {
         float y[4][U];
-        apply4_c<float, NC, NR>(a.S, a.S.c32, p32, (int)qd, y);
+        apply4_c<float, NC, NR, true, true>(a.S, a.S.c32, p32, (int)qd, y);
         quad_store<float, NC, NR>(q32, n, qd, y);
         quad_dot<NC, NR>(p32, n, qd, y, pqf);
       }

@@ -6,7 +6,7 @@
 
 namespace cpm {
 
-enum : uint8_t { kRowIdentity = 1, kRowZero = 2, kColExcluded = 4, kNearExcluded = 8 };
+enum : uint8_t { kRowIdentity = 1, kRowZero = 2, kColExcluded = 4, kNearExcluded = 8, kNearUnpinned = 16 };
 
 // Operator description carried in the kernel's launch parameters: the
 // coefficients are read from the parameter (constant) bank with compile-time
@@ -245,9 +245,41 @@ __device__ __forceinline__ void quad_columns(const T *c, const XS &x, const int 
 // form is slower than the per-DOF product (each lane's loads are 16 bytes
 // apart, so every load instruction moves four cache lines through L1); only
 // the FP32 product entry point offers it.
-template <typename T, int NC, int NR, bool VEC = true, typename Geo, typename XS>
+//
+// PINS: the operand is zero at every pinned DOF (identity row and excluded
+// column: flags 1|4), as the FP32 CG keeps it, so an excluded pinned column
+// adds nothing and needs no test.  A flagged quad then takes the register-
+// blocked product too and only its unit / empty rows are overwritten; only a
+// quad next to an excluded column whose row is not an identity row (flag 16)
+// takes the per-DOF checked product.
+template <typename T, int NC, int NR, bool VEC = true, bool PINS = false, typename Geo, typename XS>
 __device__ __forceinline__ void apply4_c(const Geo &S, const T *c, const XS &x, int d0,
                                          T (&y)[4][NC * NR]) {
+  if (PINS && VEC && S.flags) {
+    const uint32_t w = *reinterpret_cast<const uint32_t *>(S.flags + d0);
+    if (w & 0x10101010u) {
+      apply4_per_dof<T, NC, NR, VEC>(S, c, x, d0, y);
+      return;
+    }
+    const Nbr b = neighbours(S, d0);
+    const int k0 = b.zk[1];
+    const int km = b.zk[0];
+    const int kp = (k0 + 4 == S.nz) ? 0 : k0 + 4;
+    quad_columns<T, NC, NR, VEC>(c, x, b.xi, b.yj, k0, km, kp, (int64_t)S.n, y);
+    if (w & 0x03030303u) {
+#pragma unroll
+      for (int kk = 0; kk < 4; ++kk) {
+        const uint32_t f = (w >> (8 * kk)) & 3u;
+        if (!f) continue;
+#pragma unroll
+        for (int u = 0; u < NC * NR; ++u)
+          y[kk][u] = (f & kRowIdentity)
+                         ? ld<T>(x, NC == 1 ? (int64_t)(d0 + kk) * NR + u : (int64_t)u * S.n + d0 + kk, u)
+                         : T(0);
+      }
+    }
+    return;
+  }
   if (VEC && S.flags && *reinterpret_cast<const uint32_t *>(S.flags + d0) != 0u) {
     apply4_per_dof<T, NC, NR, VEC>(S, c, x, d0, y);
     return;

@@ -12,7 +12,7 @@ import torch
 
 from .. import _native as N
 
-ROW_IDENTITY, ROW_ZERO, COL_EXCLUDED, NEAR_EXCLUDED = 1, 2, 4, 8
+ROW_IDENTITY, ROW_ZERO, COL_EXCLUDED, NEAR_EXCLUDED, NEAR_UNPINNED = 1, 2, 4, 8, 16
 
 
 class StencilOperator:
@@ -40,14 +40,23 @@ class StencilOperator:
         return self._dev
 
     def mark_neighbours(self, f):
-        """Set NEAR_EXCLUDED on every DOF that has an excluded column among its 27 neighbours."""
-        ex = (f & COL_EXCLUDED).astype(bool).reshape(self.nx, self.ny, self.nz)
-        near = np.zeros_like(ex)
-        for dx in (-1, 0, 1):
-            for dy in (-1, 0, 1):
-                for dz in (-1, 0, 1):
-                    near |= np.roll(ex, (dx, dy, dz), axis=(0, 1, 2))
-        f[near.reshape(-1)] |= NEAR_EXCLUDED
+        """Set NEAR_EXCLUDED on every DOF that has an excluded column among its 27 neighbours, and
+        NEAR_UNPINNED where one of those excluded columns is not also an identity row."""
+        shape = (self.nx, self.ny, self.nz)
+        ex = (f & COL_EXCLUDED).astype(bool).reshape(shape)
+        unpinned = ex & ~(f & ROW_IDENTITY).astype(bool).reshape(shape)
+
+        def near(m):
+            out = np.zeros_like(m)
+            for dx in (-1, 0, 1):
+                for dy in (-1, 0, 1):
+                    for dz in (-1, 0, 1):
+                        out |= np.roll(m, (dx, dy, dz), axis=(0, 1, 2))
+            return out.reshape(-1)
+
+        f[near(ex)] |= NEAR_EXCLUDED
+        if unpinned.any():
+            f[near(unpinned)] |= NEAR_UNPINNED
         return f
 
     def ensure_fp32(self):

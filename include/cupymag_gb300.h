@@ -147,7 +147,10 @@ int cpm_cg_solve_noalloc(const cpm_csr *A, const double *b, double *x, int nrhs,
  * DOFs of A1/A2), 2 = empty row (defect rows of the mass matrix), 4 = the
  * DOF's column is dropped from every other row (final_assembly.py:59-158),
  * 8 = some neighbour of this DOF carries flag 4 (its row takes the checked
- * path; all other rows skip the per-neighbour flag tests). */
+ * path; all other rows skip the per-neighbour flag tests), 16 = some
+ * neighbour carries flag 4 without flag 1 (the FP32 refinement solver keeps
+ * its vectors zero at pinned DOFs, flags 1|4, and tests columns only in rows
+ * with flag 16). */
 typedef struct {
   int32_t nx, ny, nz;      /* cells per axis (>= 3), n = nx*ny*nz DOFs */
   int32_t ncomp;           /* 1: scalar operator; 3: elastic operator on [ux|uy|uz] */

@@ -101,6 +101,33 @@ def test_stencil_cg_converges_like_csr(prec, edge):
         assert np.linalg.norm(b - A @ xs) <= 1e-10 * np.linalg.norm(b) * 1.001, name
 
 
+@pytest.mark.parametrize("nrhs", [1, 3])
+def test_fp32_cg_solves_pinned_dofs_exactly_from_any_start(nrhs):
+    """The FP32 refinement CG on A1, whose defect DOFs are pinned (identity rows, excluded columns),
+    with b != 0 at those DOFs and a warm start that is wrong there: they come out as x = b exactly
+    (the solution of those rows) and the FP64 stopping test holds for every right-hand side."""
+    from cupymag_gb300.solvers.linear_solvers import CGSolver, decode_info, new_info
+    S, p = _sim(Nx=16, Ny=16, Nz=16, Ndx=5, Ndy=5, Ndz=5)
+    op = S.stencil_operators()["A1"]
+    A = S.host_operators()["A1"]
+    n = A.shape[0]
+    rng = np.random.default_rng(8)
+    shape = (n, nrhs) if nrhs > 1 else (n,)
+    b = rng.normal(size=shape)
+    x0 = rng.normal(size=shape)
+    bd = torch.as_tensor(b, device="cuda").contiguous()
+    x = torch.as_tensor(x0, device="cuda").contiguous()
+    info = new_info(1)
+    CGSolver().launch(op, bd, x, info[0], tol=1e-10, maxiter=20000, precision="IR", use_init=True)
+    inf = decode_info(info[0].cpu().numpy())
+    assert inf["status"] == 0, inf
+    xs = x.cpu().numpy()
+    assert len(S.DefDOF) > 0 and np.array_equal(xs[S.DefDOF], b[S.DefDOF])
+    bb, xx = b.reshape(n, -1), xs.reshape(n, -1)
+    for r in range(nrhs):
+        assert np.linalg.norm(bb[:, r] - A @ xx[:, r]) <= 1e-10 * np.linalg.norm(bb[:, r]) * 1.001, r
+
+
 @pytest.mark.parametrize("case", ["hex_plain", "hex_me_rot", "hex_me_norot"])
 def test_llg_step_on_stencils_matches_reference(case):
     from cupymag_gb300.physics.llg import LLGSolver

@@ -264,3 +264,28 @@ def test_memory_estimate_grows_with_size_and_coupling():
     assert a < b < c
     # matrix-free operators: about 500 bytes per DOF at 96^3 with coupling
     assert 0.3e9 < estimate_bytes(hex_params(96, 12, True, True)) < 0.8e9
+
+
+def test_flags_mark_neighbours_of_excluded_and_of_unpinned_columns():
+    """Bit 8 on the 27-point neighbourhood of every excluded column, bit 16 only around excluded
+    columns whose rows are not identity rows (pinned DOFs, flags 1|4, need no column tests in the
+    FP32 refinement solver)."""
+    from cupymag_gb300.utils.stencil_operator import (COL_EXCLUDED, NEAR_EXCLUDED, NEAR_UNPINNED, ROW_IDENTITY,
+                                                      StencilOperator)
+    nx = ny = nz = 6
+    n = nx * ny * nz
+    f = np.zeros(n, dtype=np.uint8)
+    node = lambda i, j, k: (i * ny + j) * nz + k  # noqa: E731
+    f[node(0, 0, 0)] = ROW_IDENTITY | COL_EXCLUDED      # pinned (wraps around the periodic grid)
+    f[node(3, 3, 3)] = COL_EXCLUDED                     # excluded column, regular row
+    S = StencilOperator(nx, ny, nz, np.ones(27), f, device="cpu")
+    g = S.flags.numpy()
+    near_pin = {node(i % nx, j % ny, k % nz) for i in (-1, 0, 1) for j in (-1, 0, 1) for k in (-1, 0, 1)}
+    near_free = {node(3 + i, 3 + j, 3 + k) for i in (-1, 0, 1) for j in (-1, 0, 1) for k in (-1, 0, 1)}
+    for d in range(n):
+        assert bool(g[d] & NEAR_EXCLUDED) == (d in near_pin or d in near_free), d
+        assert bool(g[d] & NEAR_UNPINNED) == (d in near_free), d
+    assert S.anchor == -1
+    pin_only = np.zeros(n, dtype=np.uint8)
+    pin_only[node(2, 1, 4)] = ROW_IDENTITY | COL_EXCLUDED
+    assert StencilOperator(nx, ny, nz, np.ones(27), pin_only, device="cpu").anchor == node(2, 1, 4)
