@@ -211,12 +211,13 @@ __global__ void __launch_bounds__(kCGThreads) cg_stencil_fp64_kernel(const __gri
 // alpha = (t.p) / (p.A p).  The update costs no extra grid barrier.
 // info->outer counts the reliable updates.  With nz % 4 == 0 the FP32
 // product runs on quads of 4 DOFs along z (apply4_c).  Pinned DOFs (identity
-// row, excluded column: the defects of A1/A2, the anchors) are solved from the
-// start (x = b there, the reference's solution of those rows), so r, p and q
-// stay zero there and the FP32 product needs no per-neighbour column tests:
-// flagged quads keep the register-blocked form (measured on GB300, 128^3 A1
-// with a 16^3 defect: the CTAs holding the defect's quads had made every other
-// CTA wait 14 us of a 47 us iteration).  The CG state lives in
+// row, excluded column: the defects of A1/A2, the anchors) decouple: their
+// solution is x = b, written when the solve ends; until then x, r, p and q
+// stay zero there and their rows' residual is zero, so neither the FP32
+// product nor the FP64 residual needs per-neighbour column tests: flagged
+// quads keep the register-blocked form (measured on GB300, 128^3 A1 with a
+// 16^3 defect: the CTAs holding the defect's quads had made every other CTA
+// wait 14 us of a 47 us iteration).  The CG state lives in
 // shared memory (IRState), updated by thread 0 after each reduction, so the
 // DOF loops keep only alpha/beta and bitmasks in registers.
 // 256-thread CTAs, four per SM (measured faster than one 1024-thread CTA per
@@ -250,17 +251,17 @@ __global__ void __launch_bounds__(kIRThreads, 4) cg_stencil_ir_kernel(const __gr
   for (int j = 0; j < 2 * NS; ++j) v[j] = 0.0;
   for (int64_t dof = d0 + threadIdx.x; dof < d1; dof += TH) {
     double y[U];
-    // a pinned DOF (identity row, excluded column) is solved by x = b: its residual, and so every
-    // FP32 vector there, stays zero (the FP32 product relies on it)
-    const bool pin = a.S.flags && (a.S.flags[dof] & (kRowIdentity | kColExcluded)) == (kRowIdentity | kColExcluded);
+    // a pinned DOF (identity row, excluded column) is solved by x = b, written when the solve ends;
+    // until then x, its residual and every FP32 vector stay zero there, so the products need no
+    // column tests
+    const bool pin = is_pinned(a.S, dof);
     if (use_init && !pin) apply<double, NC, NR>(a.S, x, (int)dof, y);
 #pragma unroll
     for (int u = 0; u < U; ++u) {
       const int64_t i = uidx<NC, NR>(n, dof, u);
       const double bi = b[i];
       const double ri = pin ? 0.0 : use_init ? bi - y[u] : bi;
-      if (pin) x[i] = bi;
-      else if (!use_init) x[i] = 0.0;
+      if (pin || !use_init) x[i] = 0.0;
       const float rf = (float)ri;
       r32[i] = rf;
       p32[i] = rf;
@@ -327,19 +328,41 @@ __global__ void __launch_bounds__(kIRThreads, 4) cg_stencil_ir_kernel(const __gr
       pt[2 * NS + j] = 0.0;
     }
     if (needm) {
-      // d was folded into x by the previous direction phase
-      for (int64_t dof = d0 + threadIdx.x; dof < d1; dof += TH) {
-        double yt[U];
-        apply<double, NC, NR>(a.S, x, (int)dof, yt);
+      // d was folded into x by the previous direction phase; pinned rows keep t = 0
+      if (quads) {
+        for (int64_t qd = d0 + 4 * threadIdx.x; qd < d1; qd += 4 * TH) {
+          double yt[4][U];
+          apply4_c<double, NC, NR, true, true>(a.S, a.S.c64, x, (int)qd, yt);
 #pragma unroll
-        for (int u = 0; u < U; ++u) {
-          const int s = sys_of<NC, NR>(u);
-          if (!((needm >> s) & 1)) continue;
-          const int64_t i = uidx<NC, NR>(n, dof, u);
-          const double t = b[i] - yt[u];
-          r32[i] = (float)t;
-          pt[NS + s] = fma(t, t, pt[NS + s]);
-          pt[2 * NS + s] = fma(t, (double)p32[i], pt[2 * NS + s]);
+          for (int kk = 0; kk < 4; ++kk) {
+            const bool pin = is_pinned(a.S, qd + kk);
+#pragma unroll
+            for (int u = 0; u < U; ++u) {
+              const int s = sys_of<NC, NR>(u);
+              if (!((needm >> s) & 1)) continue;
+              const int64_t i = uidx<NC, NR>(n, qd + kk, u);
+              const double t = pin ? 0.0 : b[i] - yt[kk][u];
+              r32[i] = (float)t;
+              pt[NS + s] = fma(t, t, pt[NS + s]);
+              pt[2 * NS + s] = fma(t, (double)p32[i], pt[2 * NS + s]);
+            }
+          }
+        }
+      } else {
+        for (int64_t dof = d0 + threadIdx.x; dof < d1; dof += TH) {
+          double yt[U];
+          apply<double, NC, NR>(a.S, x, (int)dof, yt);
+          const bool pin = is_pinned(a.S, dof);
+#pragma unroll
+          for (int u = 0; u < U; ++u) {
+            const int s = sys_of<NC, NR>(u);
+            if (!((needm >> s) & 1)) continue;
+            const int64_t i = uidx<NC, NR>(n, dof, u);
+            const double t = pin ? 0.0 : b[i] - yt[u];
+            r32[i] = (float)t;
+            pt[NS + s] = fma(t, t, pt[NS + s]);
+            pt[2 * NS + s] = fma(t, (double)p32[i], pt[2 * NS + s]);
+          }
         }
       }
     }
@@ -428,6 +451,12 @@ __global__ void __launch_bounds__(kIRThreads, 4) cg_stencil_ir_kernel(const __gr
       }
     }
   }
+  // the pinned DOFs' solution
+  if (a.S.flags)
+    for (int64_t dof = d0 + threadIdx.x; dof < d1; dof += TH)
+      if (is_pinned(a.S, dof))
+#pragma unroll
+        for (int u = 0; u < U; ++u) x[uidx<NC, NR>(n, dof, u)] = b[uidx<NC, NR>(n, dof, u)];
   if (blockIdx.x == 0 && threadIdx.x == 0) {
     int stt = status;
     for (int j = 0; j < NS; ++j) {

@@ -130,6 +130,12 @@ __device__ __forceinline__ void apply_c(const Geo &S, const T *c, const XS &x, i
   }
 }
 
+// A pinned DOF: identity row and excluded column (the system decouples there: x = b).
+template <typename Geo>
+__device__ __forceinline__ bool is_pinned(const Geo &S, int64_t dof) {
+  return S.flags && (S.flags[dof] & (kRowIdentity | kColExcluded)) == (kRowIdentity | kColExcluded);
+}
+
 // ---------------------------------------------------------------- four DOFs along z
 // The quad DOF by DOF (flagged quads; for the scalar form of apply4_c also
 // quads that leave their z-line); outputs past the end of the grid are zero.
