@@ -17,14 +17,24 @@
 //                       (assemble_elasticity.py:461-527)
 //
 // Every product is FP64 with the coefficients in the launch parameters
-// (constant bank operands of the FMAs).  The work per DOF is 81 (deriv),
-// 243 (strain) and 486 (F_el) FP64 FMAs over 27 neighbours against 3-6
-// gathered values, so all three are bound by GB300's FP64 pipe (about 2 FP64
-// FMAs per clock per SM); a few warps per SM keep it busy, so the kernels use
-// the registers they need (no occupancy cap, no spills).  Neighbours are summed
-// in lexicographic offset order (dx, dy, dz), the CSR's column order away from
-// the periodic seams; results agree with the CSR products to rounding.
+// (constant bank operands of the FMAs), so all three are bound by GB300's FP64
+// pipe (about 2 FP64 operations per clock per SM); a few warps per SM keep it
+// busy, so the kernels use the registers they need (no occupancy cap).
+//
+// The stencils are odd in the offset, c(-d) = -c(d) with c(0) = 0: on the
+// periodic grid F_i[p, q] = integral of N_p dN_q/dx_i integrates by parts into
+// -F_i[q, p], and F_el = B^T C S is a first-derivative operator the same way
+// (the assembled coefficients are odd to 1e-16 of their size).  Each pair of
+// opposite neighbours then enters once, as the difference of the two gathered
+// values times the odd part (c(d) - c(-d)) / 2, and the difference serves every
+// output: FP64 operations per DOF 81 -> 52 (Hd), 162 -> 78 (demag right-hand
+// side: the mean shift cancels in the difference), 243 -> 156 (strain) and
+// 486 -> 312 (F_el).  The host checks the oddness of the caller's stencil
+// (|c(d) + c(-d)| <= 1e-12 max |c|, |c(0)| as small) and otherwise sums all 27
+// neighbours in lexicographic offset order.  Results agree with the CSR
+// products to rounding.
 #include <algorithm>
+#include <cmath>
 
 #include "stencil_ops.cuh"
 
@@ -36,6 +46,7 @@ struct DerivArgs {
   int nx, ny, nz, n;
   const uint8_t *flags;  // unused (neighbours() takes any record with these fields)
   double f[3][27];
+  double h[3][13];       // odd part (f[d] - f[26 - d]) / 2 of offsets d < 13 (the pair d, 26 - d)
 };
 
 struct FelArgs {
@@ -43,7 +54,15 @@ struct FelArgs {
   const uint8_t *flags;
   int anchor;
   double c[3 * 6 * 27];
+  double h[3 * 6 * 13];  // odd part, as DerivArgs::h, per (output, input)
 };
+
+// The neighbours d and 26 - d (opposite offsets) of a DOF with wrapped offsets b, d < 13.
+__device__ __forceinline__ void pair_nodes(const Nbr &b, int d, int &qp, int &qm) {
+  const int ia = d / 9, ib = (d / 3) % 3, ic = d % 3;
+  qp = b.xi[ia] + b.yj[ib] + b.zk[ic];
+  qm = b.xi[2 - ia] + b.yj[2 - ib] + b.zk[2 - ic];
+}
 
 static inline int64_t deriv_grid(int64_t n) {
   const int64_t cap = (int64_t)sm_count() * 8;
@@ -51,7 +70,7 @@ static inline int64_t deriv_grid(int64_t n) {
 }
 
 // ---------------------------------------------------------------- Hd and the demag right-hand side
-template <int MODE>
+template <int MODE, bool ODD>
 __global__ void __launch_bounds__(kDerivThreads) deriv_kernel(const __grid_constant__ DerivArgs a,
                                                               const double *__restrict__ x, double *__restrict__ y,
                                                               double alpha, const double *shift, int64_t pin) {
@@ -65,12 +84,30 @@ __global__ void __launch_bounds__(kDerivThreads) deriv_kernel(const __grid_const
   for (int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; p < a.n; p += stride) {
     const Nbr b = neighbours(a, (int)p);
     double acc0 = 0.0, acc1 = 0.0, acc2 = 0.0;
+    if (ODD) {
+#pragma unroll
+      for (int d = 0; d < 13; ++d) {
+        int qp, qm;
+        pair_nodes(b, d, qp, qm);
+        if (MODE == 0) {
+          const double v = __ldg(x + qp) - __ldg(x + qm);
+          acc0 = fma(a.h[0][d], v, acc0);
+          acc1 = fma(a.h[1][d], v, acc1);
+          acc2 = fma(a.h[2][d], v, acc2);
+        } else {
+          acc0 = fma(a.h[0][d], __ldg(x + 3 * (int64_t)qp + 0) - __ldg(x + 3 * (int64_t)qm + 0), acc0);
+          acc1 = fma(a.h[1][d], __ldg(x + 3 * (int64_t)qp + 1) - __ldg(x + 3 * (int64_t)qm + 1), acc1);
+          acc2 = fma(a.h[2][d], __ldg(x + 3 * (int64_t)qp + 2) - __ldg(x + 3 * (int64_t)qm + 2), acc2);
+        }
+      }
+    }
 #pragma unroll
     for (int ia = 0; ia < 3; ++ia)
 #pragma unroll
       for (int ib = 0; ib < 3; ++ib)
 #pragma unroll
         for (int ic = 0; ic < 3; ++ic) {
+          if (ODD) continue;
           const int q = b.xi[ia] + b.yj[ib] + b.zk[ic];
           const int d = (ia * 3 + ib) * 3 + ic;
           if (MODE == 0) {
@@ -95,6 +132,7 @@ __global__ void __launch_bounds__(kDerivThreads) deriv_kernel(const __grid_const
 }
 
 // ---------------------------------------------------------------- strain from u
+template <bool ODD>
 __global__ void __launch_bounds__(kDerivThreads) strain_stencil_kernel(const __grid_constant__ DerivArgs a,
                                                                        const double *__restrict__ u,
                                                                        const double *R9, double *__restrict__ E) {
@@ -108,8 +146,21 @@ __global__ void __launch_bounds__(kDerivThreads) strain_stencil_kernel(const __g
   for (int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; p < n; p += stride) {
     const Nbr b = neighbours(a, (int)p);
     double d[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};  // d[a][b] = (F_a u_b)_p
+    if (ODD) {
 #pragma unroll
-    for (int ia = 0; ia < 3; ++ia)
+      for (int s = 0; s < 13; ++s) {
+        int qp, qm;
+        pair_nodes(b, s, qp, qm);
+        const double uu[3] = {__ldg(u + qp) - __ldg(u + qm), __ldg(u + n + qp) - __ldg(u + n + qm),
+                              __ldg(u + 2 * n + qp) - __ldg(u + 2 * n + qm)};
+#pragma unroll
+        for (int k = 0; k < 3; ++k)
+#pragma unroll
+          for (int c = 0; c < 3; ++c) d[k][c] = fma(a.h[k][s], uu[c], d[k][c]);
+      }
+    }
+#pragma unroll
+    for (int ia = 0; ia < 3 && !ODD; ++ia)
 #pragma unroll
       for (int ib = 0; ib < 3; ++ib)
 #pragma unroll
@@ -150,14 +201,31 @@ __global__ void __launch_bounds__(kDerivThreads) strain_stencil_kernel(const __g
 }
 
 // ---------------------------------------------------------------- b_el = F_el E0
-__global__ void __launch_bounds__(kDerivThreads, 4) fel_stencil_kernel(const __grid_constant__ FelArgs a,
+template <bool ODD>
+__global__ void __launch_bounds__(kDerivThreads, 3) fel_stencil_kernel(const __grid_constant__ FelArgs a,
                                                                     const double *__restrict__ E0,
                                                                     double *__restrict__ y) {
   const int64_t n = a.n;
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
   for (int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; p < n; p += stride) {
     double acc[3] = {0.0, 0.0, 0.0};
-    if (!(a.anchor && p == 0)) {
+    if (ODD && !(a.anchor && p == 0)) {
+      const Nbr b = neighbours(a, (int)p);
+#pragma unroll
+      for (int d = 0; d < 13; ++d) {
+        int qp, qm;
+        pair_nodes(b, d, qp, qm);
+        const double2 *ep = reinterpret_cast<const double2 *>(E0 + 6 * (int64_t)qp);
+        const double2 *em = reinterpret_cast<const double2 *>(E0 + 6 * (int64_t)qm);
+        const double2 p01 = __ldg(ep), p23 = __ldg(ep + 1), p45 = __ldg(ep + 2);
+        const double2 m01 = __ldg(em), m23 = __ldg(em + 1), m45 = __ldg(em + 2);
+        const double v[6] = {p01.x - m01.x, p01.y - m01.y, p23.x - m23.x, p23.y - m23.y, p45.x - m45.x, p45.y - m45.y};
+#pragma unroll
+        for (int r = 0; r < 3; ++r)
+#pragma unroll
+          for (int k = 0; k < 6; ++k) acc[r] = fma(a.h[(r * 6 + k) * 13 + d], v[k], acc[r]);
+      }
+    } else if (!(a.anchor && p == 0)) {
       const Nbr b = neighbours(a, (int)p);
 #pragma unroll
       for (int ia = 0; ia < 3; ++ia)
@@ -198,7 +266,23 @@ static DerivArgs deriv_args(const cpm_deriv_stencil *D) {
     a.f[1][d] = D->fy[d];
     a.f[2][d] = D->fz[d];
   }
+  for (int k = 0; k < 3; ++k)
+    for (int d = 0; d < 13; ++d) a.h[k][d] = 0.5 * (a.f[k][d] - a.f[k][26 - d]);
   return a;
+}
+
+// Whether each run of 27 coefficients is odd in the offset (to 1e-12 of its largest magnitude).
+static bool stencils_odd(const double *c, int count) {
+  for (int s = 0; s < count; ++s) {
+    const double *v = c + 27 * s;
+    double big = 0.0;
+    for (int d = 0; d < 27; ++d) big = std::max(big, std::fabs(v[d]));
+    const double tol = 1e-12 * big;
+    if (std::fabs(v[13]) > tol) return false;
+    for (int d = 0; d < 13; ++d)
+      if (std::fabs(v[d] + v[26 - d]) > tol) return false;
+  }
+  return true;
 }
 
 }  // namespace cpm
@@ -213,10 +297,14 @@ extern "C" int cpm_stencil_deriv(const cpm_deriv_stencil *D, const double *x, do
   const DerivArgs a = deriv_args(D);
   cudaStream_t st = (cudaStream_t)stream;
   const int g = (int)deriv_grid(a.n);
-  if (mode == 0)
-    deriv_kernel<0><<<g, kDerivThreads, 0, st>>>(a, x, y, alpha, nullptr, -1);
-  else
-    deriv_kernel<1><<<g, kDerivThreads, 0, st>>>(a, x, y, alpha, shift, pin);
+  const bool odd = stencils_odd(&a.f[0][0], 3);
+  if (mode == 0) {
+    if (odd) deriv_kernel<0, true><<<g, kDerivThreads, 0, st>>>(a, x, y, alpha, nullptr, -1);
+    else deriv_kernel<0, false><<<g, kDerivThreads, 0, st>>>(a, x, y, alpha, nullptr, -1);
+  } else {
+    if (odd) deriv_kernel<1, true><<<g, kDerivThreads, 0, st>>>(a, x, y, alpha, shift, pin);
+    else deriv_kernel<1, false><<<g, kDerivThreads, 0, st>>>(a, x, y, alpha, shift, pin);
+  }
   return check_launch("cpm_stencil_deriv");
 }
 
@@ -228,7 +316,11 @@ extern "C" int cpm_stencil_strain(const cpm_deriv_stencil *D, const double *u, c
     return CPM_BAD_ARG;
   }
   const DerivArgs a = deriv_args(D);
-  strain_stencil_kernel<<<(int)deriv_grid(a.n), kDerivThreads, 0, (cudaStream_t)stream>>>(a, u, R9, E);
+  const int g = (int)deriv_grid(a.n);
+  if (stencils_odd(&a.f[0][0], 3))
+    strain_stencil_kernel<true><<<g, kDerivThreads, 0, (cudaStream_t)stream>>>(a, u, R9, E);
+  else
+    strain_stencil_kernel<false><<<g, kDerivThreads, 0, (cudaStream_t)stream>>>(a, u, R9, E);
   return check_launch("cpm_stencil_strain");
 }
 
@@ -246,6 +338,12 @@ extern "C" int cpm_stencil_fel(const cpm_fel_stencil *F, const double *E0, doubl
   a.flags = nullptr;
   a.anchor = F->anchor ? 1 : 0;
   for (int i = 0; i < 3 * 6 * 27; ++i) a.c[i] = F->coef[i];
-  fel_stencil_kernel<<<(int)deriv_grid(a.n), kDerivThreads, 0, (cudaStream_t)stream>>>(a, E0, b_el);
+  for (int s = 0; s < 18; ++s)
+    for (int d = 0; d < 13; ++d) a.h[s * 13 + d] = 0.5 * (a.c[s * 27 + d] - a.c[s * 27 + 26 - d]);
+  const int g = (int)deriv_grid(a.n);
+  if (stencils_odd(a.c, 18))
+    fel_stencil_kernel<true><<<g, kDerivThreads, 0, (cudaStream_t)stream>>>(a, E0, b_el);
+  else
+    fel_stencil_kernel<false><<<g, kDerivThreads, 0, (cudaStream_t)stream>>>(a, E0, b_el);
   return check_launch("cpm_stencil_fel");
 }

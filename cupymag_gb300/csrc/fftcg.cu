@@ -585,6 +585,8 @@ struct FftCGArgs {
   int64_t dofs_per_cta;
   int quads;
   int anchor;  // >= 0: direct refinement with this pinned node; -1: preconditioned CG
+  int even;    // elastic stencil even in the offset: the FP64 residual sums opposite neighbours first
+  double e64[9 * 14];  // even part (c(d) + c(26 - d)) / 2 per block (p, q) for d < 13, then c(13)
 };
 
 constexpr int kInnerMax = 200;  // iterations of one inner preconditioned solve (a safety bound)
@@ -618,6 +620,33 @@ __device__ __forceinline__ float product32(const FftCGArgs &a, int64_t d0, int64
   return pqf[0];
 }
 
+// y = A64 x at one unflagged DOF of the elastic operator whose blocks are even in the offset
+// (c(-d) = c(d), to 1e-16 of their size: the symmetric element stiffness on identical cells):
+// each pair of opposite neighbours is summed once per component and serves the three rows, 165
+// FP64 operations where the 27-point form takes 243.
+__device__ __forceinline__ void apply_even3(const FftCGArgs &a, const double *x, int dof, double (&y)[3]) {
+  const int64_t n = a.S.n;
+  const Nbr b = neighbours(a.S, dof);
+  const double x0 = x[dof], x1 = x[n + dof], x2 = x[2 * n + dof];
+#pragma unroll
+  for (int p = 0; p < 3; ++p) {
+    const double *e = a.e64 + (p * 3) * 14;
+    y[p] = fma(e[13], x0, fma(e[14 + 13], x1, e[28 + 13] * x2));
+  }
+#pragma unroll
+  for (int d = 0; d < 13; ++d) {
+    const int ia = d / 9, ib = (d / 3) % 3, ic = d % 3;
+    const int qp = b.xi[ia] + b.yj[ib] + b.zk[ic];
+    const int qm = b.xi[2 - ia] + b.yj[2 - ib] + b.zk[2 - ic];
+    const double s0 = x[qp] + x[qm], s1 = x[n + qp] + x[n + qm], s2 = x[2 * n + qp] + x[2 * n + qm];
+#pragma unroll
+    for (int p = 0; p < 3; ++p) {
+      const double *e = a.e64 + (p * 3) * 14;
+      y[p] = fma(e[d], s0, fma(e[14 + d], s1, fma(e[28 + d], s2, y[p])));
+    }
+  }
+}
+
 // t = b - A64 x on this CTA's DOFs: r = t (FP32), d = 0; v[0] = the thread's FP64 partial of t . t
 // and, with SUMS, v[1 + c] = its partial of the sum of component c of t.
 template <int NC, int NT, bool SUMS, int NV>
@@ -627,7 +656,12 @@ __device__ __forceinline__ void true_residual64(const FftCGArgs &a, int64_t d0, 
   for (int j = 0; j < NV; ++j) v[j] = 0.0;
   for (int64_t dof = d0 + threadIdx.x; dof < d1; dof += NT) {
     double y[NC];
-    apply<double, NC, 1>(a.S, a.x, (int)dof, y);
+    if constexpr (NC == 3) {
+      if (a.even && !(a.S.flags && a.S.flags[dof])) apply_even3(a, a.x, (int)dof, y);
+      else apply<double, NC, 1>(a.S, a.x, (int)dof, y);
+    } else {
+      apply<double, NC, 1>(a.S, a.x, (int)dof, y);
+    }
 #pragma unroll
     for (int u = 0; u < NC; ++u) {
       const int64_t i = uidx<NC, 1>(n, dof, u);
@@ -1072,6 +1106,20 @@ extern "C" int cpm_cg_solve_stencil_fft(const cpm_stencil *S, const cpm_fft_prec
   a.timeout_ns = (unsigned long long)(tmo * 1e9);
   a.quads = (S->nz & 3) == 0 && ((uintptr_t)S->flags & 3) == 0;
   a.anchor = (P->anchor >= 0 && o->form != CPM_CG_FORM_FFT_PCG) ? P->anchor : -1;
+  if (nc == 3) {
+    // even blocks (to 1e-12 of their largest coefficient): the pair-summed FP64 residual
+    a.even = 1;
+    for (int blk = 0; blk < 9; ++blk) {
+      const double *c = S->coef + 27 * blk;
+      double big = 0.0;
+      for (int d = 0; d < 27; ++d) big = std::max(big, std::fabs(c[d]));
+      for (int d = 0; d < 13; ++d) {
+        if (std::fabs(c[d] - c[26 - d]) > 1e-12 * big) a.even = 0;
+        a.e64[blk * 14 + d] = 0.5 * (c[d] + c[26 - d]);
+      }
+      a.e64[blk * 14 + 13] = c[13];
+    }
+  }
   const bool slab = P->layout == CPM_FFT_LAYOUT_SLAB;
   const void *fn = slab ? (nc == 3 ? (const void *)cg_stencil_fft_kernel<3, CPM_FFT_LAYOUT_SLAB>
                                    : (const void *)cg_stencil_fft_kernel<1, CPM_FFT_LAYOUT_SLAB>)
