@@ -181,12 +181,18 @@ IR_STENCIL_DRAM_BYTES_PER_UNKNOWN_ITER = 20.6
 
 
 def fft_launch_bytes(A, iters, outer):
-    """Algorithmic bytes of an FFT-preconditioned solve launch (csrc/fftcg.cu), per unknown:
-    inner iteration 120 B + the inverse symbol (8 B elastic: 24 B per DOF; 4 B scalar): M r = DFT
-    passes along z (read r 4, write the complex field 8), y (16), x with the symbol solve (16), y (16),
-    z (read 8, write z 4, read r 4); p = z + beta p (12); q = A p (8); d, r update (24).  Each FP64
-    residual and fold: 44 B (read x, b, write r, d; read x, d, write x)."""
+    """Algorithmic bytes of an FFT solve launch (csrc/fftcg.cu), per unknown.
+
+    Direct refinement (operators pinned at one anchor node, the default): each FP64 residual 20 B (read
+    x, b; write r), one more residual than steps; each step 52 B plus the inverse symbol of the half
+    spectrum (4 B elastic, 2 B scalar): slab pass 1 (read r 4, write the half spectrum 4), pass 2 (read
+    and write it, 8), pass 3 (read it 4, write z 4, read r 4), x += z + shift (read z 4, x 16); read b once
+    (8).  Preconditioned CG: inner iteration 120 B + the full symbol (8 B elastic, 4 B scalar), each FP64
+    residual and fold 44 B."""
     u = A.shape[0]
+    if getattr(A, "anchor", -1) >= 0:
+        steps = max(outer, 0)
+        return u * (20 * (steps + 1) + (52 + (4 if A.ncomp == 3 else 2)) * steps + 8)
     per_inner = 120 + (8 if A.ncomp == 3 else 4)
     return u * (per_inner * iters + 44 * max(outer, 1) + 8)
 

@@ -548,15 +548,11 @@ extern "C" int cpm_strain_from_u(const cpm_csr *Fx, const double *vals_y, const 
   const int64_t tiles = (n + kStrainThreads / G - 1) / (kStrainThreads / G);
   cudaStream_t st = (cudaStream_t)stream;
   const void *fn = Fx->indptr_is64 ? (const void *)strain_kernel<int64_t> : (const void *)strain_kernel<int32_t>;
-  static int occ = 0;
-  if (occ == 0) {
-    cudaFuncSetAttribute((const void *)strain_kernel<int64_t>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         multi_smem<3>());
-    cudaFuncSetAttribute((const void *)strain_kernel<int32_t>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         multi_smem<3>());
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fn, kStrainThreads, multi_smem<3>());
-    if (occ < 1) occ = 1;
-  }
+  // the shared-memory attribute is per device: set it (cheaply) on every call, then query the occupancy
+  int occ = 0;
+  CPM_TRY(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, multi_smem<3>()));
+  CPM_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fn, kStrainThreads, multi_smem<3>()));
+  if (occ < 1) occ = 1;
   int64_t g = (int64_t)occ * sm_count();
   if (g > tiles) g = tiles;
   if (Fx->indptr_is64)

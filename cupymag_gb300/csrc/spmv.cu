@@ -6,6 +6,8 @@
 // order is fixed, so results are deterministic.  Matrices of the hex grid have
 // 27 (scalar), 81 (elastic stiffness) or 162 (elastic coupling) non-zeros per
 // row.
+#include <algorithm>
+
 #include "cpm_common.cuh"
 #include "csr_tile.cuh"
 
@@ -13,56 +15,53 @@ namespace cpm {
 
 constexpr int kSpThreads = 256;
 
-// Staged thread-group-per-row kernels (see csr_tile.cuh): one FP64 FMA per
+// Staged thread-group-per-row kernel of the three-matrix product (see csr_tile.cuh): one FP64 FMA per
 // non-zero and value, tiles of rows handed out grid-stride.
+// The shared-memory attribute is a per-device setting, so it is set on every call (cheap) and the
+// occupancy is queried with it.
 static int tile_grid(int64_t tiles, const void *fn, int smem) {
-  static int occ_cache[8] = {};
-  static const void *fn_cache[8] = {};
   int occ = 0;
-  for (int i = 0; i < 8; ++i)
-    if (fn_cache[i] == fn) occ = occ_cache[i];
-  if (occ == 0) {
-    cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fn, kSpThreads, smem);
-    if (occ < 1) occ = 1;
-    for (int i = 0; i < 8; ++i)
-      if (fn_cache[i] == nullptr) {
-        fn_cache[i] = fn;
-        occ_cache[i] = occ;
-        break;
-      }
-  }
+  cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fn, kSpThreads, smem);
+  if (occ < 1) occ = 1;
   int64_t g = (int64_t)occ * sm_count();
   if (g > tiles) g = tiles;
   return (int)(g < 1 ? 1 : g);
 }
 
-template <typename IT, int NV>
-__global__ void __launch_bounds__(kSpThreads) spmv_kernel(int64_t rows, const IT *__restrict__ rp,
-                                                          const int *__restrict__ ci, const double *__restrict__ av,
-                                                          const double *__restrict__ x, double *__restrict__ y,
-                                                          double alpha, int G) {
-  extern __shared__ __align__(16) unsigned char smem[];
-  const MultiTile<1> t = multi_tile_smem<1>(smem);
-  const int R = kSpThreads / G;
-  const double *vals[1] = {av};
-  const int64_t ntiles = (rows + R - 1) / R;
-  for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
-    const int64_t t0 = tile * R, t1 = min(rows, t0 + R);
+// Rows read in place by groups of G lanes (G = 4 for rows of 16 or more entries, else 2): the group's
+// lanes take entries k = start + sub, start + sub + G, ..., so each load instruction of a warp fills
+// whole 32-byte sectors of 32 / G rows (no staging, no shared memory, full occupancy), and the row sum
+// costs log2(G) FP64 shuffle-adds per lane.  On GB300 the FP64 pipe, not HBM, bounds a CSR SpMV (one
+// FMA per 12-byte non-zero at about 2 FP64 operations per clock per SM); the 16-lane groups of the
+// staged kernel spent 64 lane-slots of FP64 adds per 162-entry row (28 % of the FP64 work), these 8.
+template <typename IT, int NV, int G>
+__global__ void __launch_bounds__(kSpThreads) spmv_rows_kernel(int64_t rows, const IT *__restrict__ rp,
+                                                               const int *__restrict__ ci,
+                                                               const double *__restrict__ av,
+                                                               const double *__restrict__ x, double *__restrict__ y,
+                                                               double alpha) {
+  const int sub = threadIdx.x % G;
+  const int64_t step = (int64_t)gridDim.x * (blockDim.x / G);
+  for (int64_t row = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / G; row < rows; row += step) {
+    const int64_t rs = (int64_t)__ldg(rp + row), re = (int64_t)__ldg(rp + row + 1);
     double acc[NV];
 #pragma unroll
     for (int j = 0; j < NV; ++j) acc[j] = 0.0;
-    const int64_t row = visit_tile<1, IT>(rp, ci, vals, t0, t1, G, t, [&](const double (&a)[1], int64_t c) {
+#pragma unroll 4
+    for (int64_t k = rs + sub; k < re; k += G) {
+      const double a = __ldcs(av + k);
+      const int64_t c = __ldcs(ci + k);
 #pragma unroll
-      for (int j = 0; j < NV; ++j) acc[j] = fma(a[0], __ldg(x + c * NV + j), acc[j]);
-    });
+      for (int j = 0; j < NV; ++j) acc[j] = fma(a, __ldg(x + c * NV + j), acc[j]);
+    }
 #pragma unroll
-    for (int j = 0; j < NV; ++j) acc[j] = group_sum(acc[j], G);
-    if (row >= 0 && (threadIdx.x % G) == 0) {
+    for (int o = 1; o < G; o <<= 1)
+#pragma unroll
+      for (int j = 0; j < NV; ++j) acc[j] += __shfl_xor_sync(0xffffffffu, acc[j], o);
+    if (sub == 0)
 #pragma unroll
       for (int j = 0; j < NV; ++j) y[row * NV + j] = alpha * acc[j];
-    }
-    __syncthreads();
   }
 }
 
@@ -150,13 +149,21 @@ extern "C" int cpm_spmv_csr(const cpm_csr *A, const double *x, double *y, double
   }
   if (A->rows == 0) return CPM_OK;
   cudaStream_t st = (cudaStream_t)stream;
-  const int G = group_size_cap(max_row(A), kSpThreads, multi_cap<1>());
-  const int64_t tiles = (A->rows + kSpThreads / G - 1) / (kSpThreads / G);
+  // rows of 16 or more entries: groups of 4 lanes; shorter rows: pairs.  Five CTAs per SM: the rows in
+  // flight then span a few tens of MB of the matrix; measured on GB300 (128^3 F_el, A_el, A_demag; 64^3
+  // F_el, A_el) 0.63 / 0.60 / 0.64 / 0.75 / 0.69 of HBM, against 0.54 / 0.51 / 0.63 / 0.71 / 0.68 with
+  // sixteen (more rows in flight, less reuse of the gathered vector) and 0.42 / 0.39 with two
+  const int G = max_row(A) >= 16 ? 4 : 2;
+  const int64_t want = (A->rows * G + kSpThreads - 1) / kSpThreads;
+  const int grid = (int)std::max<int64_t>(1, std::min<int64_t>(want, (int64_t)sm_count() * 5));
 #define CPM_SP1(IT, NV)                                                                                          \
   do {                                                                                                           \
-    const void *fn = (const void *)spmv_kernel<IT, NV>;                                                          \
-    spmv_kernel<IT, NV><<<tile_grid(tiles, fn, multi_smem<1>()), kSpThreads, multi_smem<1>(), st>>>(           \
-        A->rows, (const IT *)A->indptr, A->indices, A->vals, x, y, alpha, G);                                    \
+    if (G == 4)                                                                                                  \
+      spmv_rows_kernel<IT, NV, 4><<<grid, kSpThreads, 0, st>>>(A->rows, (const IT *)A->indptr, A->indices,       \
+                                                               A->vals, x, y, alpha);                            \
+    else                                                                                                         \
+      spmv_rows_kernel<IT, NV, 2><<<grid, kSpThreads, 0, st>>>(A->rows, (const IT *)A->indptr, A->indices,       \
+                                                               A->vals, x, y, alpha);                            \
   } while (0)
   if (A->indptr_is64) {
     if (nvec == 1) CPM_SP1(int64_t, 1); else CPM_SP1(int64_t, 3);
