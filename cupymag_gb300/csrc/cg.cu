@@ -60,6 +60,9 @@ struct CGArgs {
   int group;                               // threads per row in the staged SpMV
 };
 
+// Lanes per row of the FP32 product of the refinement form (group_row in csr_tile.cuh).
+constexpr int kCsrGroup = 4;
+
 template <typename IT>
 __device__ __forceinline__ void row_range(const IT *rp, int64_t row, int64_t &s, int64_t &e) {
   s = (int64_t)__ldg(rp + row);
@@ -240,21 +243,20 @@ __global__ void __launch_bounds__(kCGThreads) cg_fp64_kernel(CGArgs<NR, IT> a) {
 // iteration's first phase also computes the true residual t = b - A64 x with
 // the FP64 values (staged tiles; the direction phase before it folded d into
 // x), t replaces r and rho and decides convergence, and that iteration's step
-// is the exact line search (t.p) / (p.A p).  Three grid barriers per iteration;
-// the FP32 product uses the same staged tiles and thread groups per row as
-// the FP64 solver.  The CG state lives in shared memory (IRState).
+// is the exact line search (t.p) / (p.A p).  Three grid barriers per iteration.
+// Every product reads its rows in place by 4-lane groups (group_row): no
+// shared-memory tiles, so more CTAs per SM hide the gathers.  Measured on GB300
+// (FP32 product, 3 RHS scalar / elastic / tet rows): tet96 elasticity 373 -> 289
+// us per iteration, demag 66 -> 53, hex 64^3 elasticity 179 -> 129, against the
+// staged tiles, which the FP64 solver keeps (faster there: tet96 elasticity 520
+// against 668 us in place).  The CG state lives in shared memory (IRState).
 template <int NR, typename IT>
 __global__ void __launch_bounds__(kCGThreads) cg_ir_kernel(CGArgs<NR, IT> a) {
   __shared__ double s_red[9][kCGWarps];
   __shared__ IRState st[NR];
   __shared__ float s_ab[NR];
   __shared__ int s_mask[3];  // active, need, status
-  extern __shared__ __align__(16) unsigned char s_tile[];
-  const TileSmem tile = tile_smem(s_tile);
-  const TileSmem32 tile32 = tile_smem32(s_tile);
-  const int G = a.group;
-  const int R = kCGThreads / G;
-  const bool lead = (threadIdx.x % G) == 0;
+  const bool lead = (threadIdx.x % kCsrGroup) == 0;
   const int64_t r0 = min(a.n, (int64_t)blockIdx.x * a.rows_per_cta);
   const int64_t r1 = min(a.n, r0 + a.rows_per_cta);
   const bool use_init = a.use_init_dev ? (__ldcg(a.use_init_dev) != 0) : (a.use_init_host != 0);
@@ -268,10 +270,11 @@ __global__ void __launch_bounds__(kCGThreads) cg_ir_kernel(CGArgs<NR, IT> a) {
 #pragma unroll
   for (int j = 0; j < 2 * NR; ++j) v[j] = 0.0;
   if (use_init) {
-    for (int64_t t0 = r0; t0 < r1; t0 += R) {
+    for (int64_t t0 = r0; t0 < r1; t0 += kCGThreads / kCsrGroup) {
       double acc[NR];
-      const int64_t row = tile_rows<NR, IT>(a.rp, a.ci, a.av, x, t0, min(r1, t0 + R), G, tile, acc);
-      if (row >= 0 && lead) {
+      const int64_t row = t0 + threadIdx.x / kCsrGroup;
+      group_row<NR, kCsrGroup, IT>(a.rp, a.ci, a.av, x, row, r1, acc);
+      if (row < r1 && lead) {
 #pragma unroll
         for (int j = 0; j < NR; ++j) {
           const double bj = a.b[row * NR + j];
@@ -325,14 +328,15 @@ __global__ void __launch_bounds__(kCGThreads) cg_ir_kernel(CGArgs<NR, IT> a) {
   int status = CPM_OK;
   for (int k = 0; activem && k <= a.maxiter; ++k) {
     if (k > 0 && !grid_sync(a.bar, gridDim.x, tns)) { status = CPM_BARRIER_TIMEOUT; break; }
-    // ---- phase 1: q = A32 p (staged FP32 tiles), p.q; pending: t = b - A64 x, r32 = t, t.t, t.p
+    // ---- phase 1: q = A32 p, p.q; pending: t = b - A64 x, r32 = t, t.t, t.p
     float pqf[NR];
 #pragma unroll
     for (int j = 0; j < NR; ++j) pqf[j] = 0.0f;
-    for (int64_t t0 = r0; t0 < r1; t0 += R) {
+    for (int64_t t0 = r0; t0 < r1; t0 += kCGThreads / kCsrGroup) {
       float acc[NR];
-      const int64_t row = tile_rows32<NR, IT>(a.rp, a.ci, a.av32, p32, t0, min(r1, t0 + R), G, tile32, acc);
-      if (row >= 0 && lead) {
+      const int64_t row = t0 + threadIdx.x / kCsrGroup;
+      group_row<NR, kCsrGroup, IT, float>(a.rp, a.ci, a.av32, p32, row, r1, acc);
+      if (row < r1 && lead) {
 #pragma unroll
         for (int j = 0; j < NR; ++j) {
           q32[row * NR + j] = acc[j];
@@ -349,10 +353,11 @@ __global__ void __launch_bounds__(kCGThreads) cg_ir_kernel(CGArgs<NR, IT> a) {
     }
     if (needm) {
       // d was folded into x by the previous direction phase
-      for (int64_t t0 = r0; t0 < r1; t0 += R) {
+      for (int64_t t0 = r0; t0 < r1; t0 += kCGThreads / kCsrGroup) {
         double acc[NR];
-        const int64_t row = tile_rows<NR, IT>(a.rp, a.ci, a.av, x, t0, min(r1, t0 + R), G, tile, acc);
-        if (row >= 0 && lead) {
+        const int64_t row = t0 + threadIdx.x / kCsrGroup;
+        group_row<NR, kCsrGroup, IT>(a.rp, a.ci, a.av, x, row, r1, acc);
+        if (row < r1 && lead) {
 #pragma unroll
           for (int j = 0; j < NR; ++j) {
             if (!((needm >> j) & 1)) continue;
@@ -488,7 +493,7 @@ static int launch_cg(const cpm_csr *A, const double *b, double *x, const cpm_cg_
 
   const bool fp64 = o->precision == 0;
   const void *fn = fp64 ? (const void *)cg_fp64_kernel<NR, IT> : (const void *)cg_ir_kernel<NR, IT>;
-  const int smem = kTileSmemBytes;
+  const int smem = fp64 ? kTileSmemBytes : 0;  // staged tiles (FP64 solver) or none (refinement form)
   // occupancy (and the shared-memory attribute, a per-device setting) resolved once per device and
   // kernel variant, under a lock: host threads may launch on different devices at once
   const int dev = device_id();

@@ -292,6 +292,34 @@ __device__ __forceinline__ int64_t visit_tile(const IT *__restrict__ rp, const i
   return row < t1 ? row : -1;
 }
 
+// Row `row` (< rows) summed by the G lanes of its group (lane sub = threadIdx.x % G takes entries
+// start + sub, start + sub + G, ...), entries read in place: each load instruction of a warp fills whole
+// 32-byte sectors of its 32 / G rows.  The sum of the group's lanes ends in every lane (log2(G) shuffle-
+// adds); every lane of the warp must call it (a row past the end sums zero).  NR right-hand sides are
+// interleaved in x; TA is the arithmetic type (FP64, or FP32 for the refinement form's products).
+template <int NR, int G, typename IT, typename TA = double, typename TV = double, typename TX = double>
+__device__ __forceinline__ void group_row(const IT *__restrict__ rp, const int *__restrict__ ci,
+                                          const TV *__restrict__ av, const TX *x, int64_t row, int64_t rows,
+                                          TA (&acc)[NR]) {
+#pragma unroll
+  for (int j = 0; j < NR; ++j) acc[j] = TA(0);
+  if (row < rows) {
+    const int sub = threadIdx.x % G;
+    const int64_t rs = (int64_t)__ldg(rp + row), re = (int64_t)__ldg(rp + row + 1);
+#pragma unroll 4
+    for (int64_t k = rs + sub; k < re; k += G) {
+      const TA a = (TA)__ldcs(av + k);
+      const int64_t c = __ldcs(ci + k);
+#pragma unroll
+      for (int j = 0; j < NR; ++j) acc[j] = fma(a, (TA)x[c * NR + j], acc[j]);
+    }
+  }
+#pragma unroll
+  for (int o = 1; o < G; o <<= 1)
+#pragma unroll
+    for (int j = 0; j < NR; ++j) acc[j] += __shfl_xor_sync(0xffffffffu, acc[j], o);
+}
+
 __device__ __forceinline__ double group_sum(double v, int G) {
   for (int o = 1; o < G; o <<= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
   return v;

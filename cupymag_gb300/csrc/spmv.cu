@@ -41,25 +41,13 @@ __global__ void __launch_bounds__(kSpThreads) spmv_rows_kernel(int64_t rows, con
                                                                const double *__restrict__ av,
                                                                const double *__restrict__ x, double *__restrict__ y,
                                                                double alpha) {
-  const int sub = threadIdx.x % G;
-  const int64_t step = (int64_t)gridDim.x * (blockDim.x / G);
-  for (int64_t row = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / G; row < rows; row += step) {
-    const int64_t rs = (int64_t)__ldg(rp + row), re = (int64_t)__ldg(rp + row + 1);
+  // the row loop is uniform over the CTA, so every lane reaches the shuffles (rows past the end sum zero)
+  const int64_t per_cta = blockDim.x / G;
+  for (int64_t base = (int64_t)blockIdx.x * per_cta; base < rows; base += (int64_t)gridDim.x * per_cta) {
+    const int64_t row = base + threadIdx.x / G;
     double acc[NV];
-#pragma unroll
-    for (int j = 0; j < NV; ++j) acc[j] = 0.0;
-#pragma unroll 4
-    for (int64_t k = rs + sub; k < re; k += G) {
-      const double a = __ldcs(av + k);
-      const int64_t c = __ldcs(ci + k);
-#pragma unroll
-      for (int j = 0; j < NV; ++j) acc[j] = fma(a, __ldg(x + c * NV + j), acc[j]);
-    }
-#pragma unroll
-    for (int o = 1; o < G; o <<= 1)
-#pragma unroll
-      for (int j = 0; j < NV; ++j) acc[j] += __shfl_xor_sync(0xffffffffu, acc[j], o);
-    if (sub == 0)
+    group_row<NV, G, IT>(rp, ci, av, x, row, rows, acc);
+    if (row < rows && threadIdx.x % G == 0)
 #pragma unroll
       for (int j = 0; j < NV; ++j) y[row * NV + j] = alpha * acc[j];
   }
