@@ -1,9 +1,10 @@
 """Time the CG solver on one operator of a structured hex grid.
 
-    python -m cupymag_gb300.cgbench [--edge 128] [--op A_el|A_demag|A1|A2] [--nrhs 1|3]
+    python -m cupymag_gb300.cgbench [--edge 128] [--op A_el|A_demag|A1|A2|F_el] [--nrhs 1|3]
                                     [--precision IR|DP] [--operators stencil|csr]
                                     [--solves 3] [--maxiter 20000] [--batch 1] [--batched]
-                                    [--form 0|1|2|3] [--precond fft]
+                                    [--form 0|1|2|3] [--precond fft] [--fft-layout auto|slab|passes]
+                                    [--spmv]
 
 Builds only the requested operator (the magnetoelastic 128^3 material), a
 seeded right-hand side with the reference's pins (b[0] = 0 for A_demag,
@@ -13,7 +14,8 @@ updates, ms per solve, ms per iteration and the algorithmic GB/s of the
 launch (vector traffic only for stencil operators, matrix + vectors for CSR).
 With --batch B > 1 (or --batched) the solve is B copies of the system in one
 block-diagonal launch of the serving solver.  A capped --maxiter keeps a profiled launch short; the status is then
-reported, not raised.
+reported, not raised.  With --operators csr --spmv it times the CSR product y = A x alone (F_el, the
+magnetoelastic coupling, is available only there).
 """
 from __future__ import annotations
 
@@ -34,10 +36,32 @@ def _bytes(op, nrhs, iters, outer, fp32, csr):
     return 2 * u * 8 + iters * (spmv + 6 * u * (4 if fp32 else 8))
 
 
+def _time_spmv(args, A, torch):
+    """y = A x (cpm_spmv_csr) --solves times after one warm-up; algorithmic bytes: values and indices
+    (12 B per non-zero), row pointers, x read and y written once."""
+    nvec = 1 if args.op in ("A_el", "F_el") else args.nrhs
+    cols = A.shape[1]
+    x = torch.randn((cols, nvec) if nvec > 1 else (cols,), dtype=torch.float64, device="cuda")
+    y = A.spmv(x)
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(args.solves):
+        A.spmv(x, out=y)
+    e1.record()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / args.solves
+    nnz = int(A.indices.numel())
+    nbytes = nnz * 12 + (A.shape[0] + 1) * A.indptr.element_size() + (A.shape[0] + cols) * 8 * nvec
+    print(json.dumps({"op": args.op, "edge": args.edge, "rows": A.shape[0], "nnz": nnz, "nvec": nvec,
+                      "kernel": "spmv", "ms_per_product": round(ms, 4), "GB/s": round(nbytes / ms / 1e6, 1)}))
+
+
 def main(argv=None):
     ap = argparse.ArgumentParser()
     ap.add_argument("--edge", type=int, default=128)
-    ap.add_argument("--op", default="A_el", choices=["A_el", "A_demag", "A1", "A2"])
+    ap.add_argument("--op", default="A_el", choices=["A_el", "A_demag", "A1", "A2", "F_el"])
     ap.add_argument("--nrhs", type=int, default=1, choices=[1, 3])
     ap.add_argument("--precision", default="IR", choices=["IR", "DP"])
     ap.add_argument("--operators", default="stencil", choices=["stencil", "csr"])
@@ -53,6 +77,8 @@ def main(argv=None):
                          "FFT solves: 0 direct refinement (anchored operators), 3 preconditioned CG")
     ap.add_argument("--fft-layout", default="auto", choices=["auto", "slab", "passes"],
                     help="spectrum layout of the FFT preconditioner")
+    ap.add_argument("--spmv", action="store_true",
+                    help="time the CSR product y = A x alone (cpm_spmv_csr), --solves times; needs --operators csr")
     ap.add_argument("--precond", default=None, choices=["fft"],
                     help="FP32 stencil solve preconditioned by the circulant inverse (FFT) inside FP64 refinement")
     args = ap.parse_args(argv)
@@ -63,14 +89,21 @@ def main(argv=None):
     from .workloads import hex_params
     N.require_cuda()
     N.load()
-    p = hex_params(args.edge, args.edge // 8, args.op == "A_el", True)
+    p = hex_params(args.edge, args.edge // 8, args.op in ("A_el", "F_el"), True)
     S = SimulationOperators(p)
     csr = args.operators == "csr"
+    if args.op == "F_el" and not (csr and args.spmv):
+        raise SystemExit("F_el is timed as a CSR product only (--operators csr --spmv)")
     if csr:
-        op = {"A_el": lambda: S.csr_elasticity()[0], "A_demag": lambda: S.csr_demag_and_deriv()[0],
+        op = {"A_el": lambda: S.csr_elasticity()[0], "F_el": lambda: S.csr_elasticity()[1],
+              "A_demag": lambda: S.csr_demag_and_deriv()[0],
               "A1": lambda: S.csr_GS()[0], "A2": lambda: S.csr_GS()[1]}[args.op]()
     else:
         op = S.stencil_operators()[args.op]
+    if args.spmv:
+        if not csr:
+            raise SystemExit("--spmv times the CSR product: add --operators csr")
+        return _time_spmv(args, op, torch)
     nrhs = 1 if args.op == "A_el" else args.nrhs
     n = op.shape[0]
     rng = np.random.default_rng(7)

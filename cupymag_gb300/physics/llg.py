@@ -47,8 +47,10 @@ SOLVE_NAMES = ["elasticity", "demag", "Gauss-Seidel g1n/g2n/g3n", "Gauss-Seidel 
 # residual has fallen by this factor).  Measured on GB300 at 64^3-128^3: the ill-conditioned
 # elasticity solve converges in the fewest iterations with 0.1 (smaller factors add 25-40 %
 # iterations); the Gauss-Seidel solves (A1, A2; ~30-55 iterations) converge in the same
-# iterations with any factor, so fewer FP64 products win (1e-4); demag is best near 1e-3.
-INNER_TOL = [0.1, 1e-3, 1e-4, 1e-4, 1e-4, 1e-4]
+# iterations down to 1e-5, so fewer FP64 products win: at 128^3 (cold, 1 and 3 right-hand sides)
+# 1e-4 takes three FP64 residuals, 1e-5 two at the same iteration counts (7-10 % faster), 1e-6
+# adds an iteration; demag is best near 1e-3.
+INNER_TOL = [0.1, 1e-3, 1e-5, 1e-5, 1e-5, 1e-5]
 
 # Solves that the precision form runs as FFT-preconditioned CG on stencil operators: elasticity and demag,
 # whose operators are circulant apart from the anchor at DOF 0 (the Gauss-Seidel operators A1/A2 carry
