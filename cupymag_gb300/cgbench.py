@@ -4,7 +4,7 @@
                                     [--precision IR|DP] [--operators stencil|csr]
                                     [--solves 3] [--maxiter 20000] [--batch 1] [--batched]
                                     [--form 0|1|2|3] [--precond fft] [--fft-layout auto|slab|passes]
-                                    [--spmv]
+                                    [--spmv] [--precond-apply] [--workload tet96_me]
 
 Builds only the requested operator (the magnetoelastic 128^3 material), a
 seeded right-hand side with the reference's pins (b[0] = 0 for A_demag,
@@ -58,6 +58,26 @@ def _time_spmv(args, A, torch):
                       "kernel": "spmv", "ms_per_product": round(ms, 4), "GB/s": round(nbytes / ms / 1e6, 1)}))
 
 
+def _time_precond(args, op, torch):
+    """z = M r alone (cpm_fft_precond_apply: one launch per pass) --solves times after one warm-up."""
+    from . import _native as N
+    layout = {"auto": N.FFT_LAYOUT_AUTO, "slab": N.FFT_LAYOUT_SLAB, "passes": N.FFT_LAYOUT_PASSES}[args.fft_layout]
+    r = torch.randn(op.shape[0], dtype=torch.float32, device="cuda")
+    z = op.precondition32(r, layout=layout)
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(args.solves):
+        op.precondition32(r, z, layout=layout)
+    e1.record()
+    torch.cuda.synchronize()
+    plan = op.fft_plan(layout)
+    print(json.dumps({"op": args.op, "edge": args.edge, "n": op.shape[0], "kernel": "fft_apply",
+                      "layout": {N.FFT_LAYOUT_SLAB: "slab", N.FFT_LAYOUT_PASSES: "passes"}[plan.layout],
+                      "us_per_apply": round(1000 * e0.elapsed_time(e1) / args.solves, 1)}))
+
+
 def main(argv=None):
     ap = argparse.ArgumentParser()
     ap.add_argument("--edge", type=int, default=128)
@@ -77,6 +97,11 @@ def main(argv=None):
                          "FFT solves: 0 direct refinement (anchored operators), 3 preconditioned CG")
     ap.add_argument("--fft-layout", default="auto", choices=["auto", "slab", "passes"],
                     help="spectrum layout of the FFT preconditioner")
+    ap.add_argument("--workload", default=None,
+                    help="take the grid and material of a named workload (cupymag_gb300.workloads, e.g. tet96_me "
+                         "for the tet mesh; CSR operators) instead of the hex grid of --edge")
+    ap.add_argument("--precond-apply", action="store_true",
+                    help="time z = M r alone (the FFT apply of a stencil operator), --solves times")
     ap.add_argument("--spmv", action="store_true",
                     help="time the CSR product y = A x alone (cpm_spmv_csr), --solves times; needs --operators csr")
     ap.add_argument("--precond", default=None, choices=["fft"],
@@ -86,11 +111,15 @@ def main(argv=None):
     from . import _native as N
     from .core.assemble_simulation_operators import SimulationOperators
     from .solvers.linear_solvers import CGSolver, decode_info, new_info
-    from .workloads import hex_params
+    from .workloads import hex_params, workload
     N.require_cuda()
     N.load()
-    p = hex_params(args.edge, args.edge // 8, args.op in ("A_el", "F_el"), True)
-    S = SimulationOperators(p)
+    if args.workload:
+        p, w = workload(args.workload)
+        S = SimulationOperators(p, mesh=w.get("mesh"))
+    else:
+        p = hex_params(args.edge, args.edge // 8, args.op in ("A_el", "F_el"), True)
+        S = SimulationOperators(p)
     csr = args.operators == "csr"
     if args.op == "F_el" and not (csr and args.spmv):
         raise SystemExit("F_el is timed as a CSR product only (--operators csr --spmv)")
@@ -104,6 +133,10 @@ def main(argv=None):
         if not csr:
             raise SystemExit("--spmv times the CSR product: add --operators csr")
         return _time_spmv(args, op, torch)
+    if args.precond_apply:
+        if csr or not hasattr(op, "precondition32"):
+            raise SystemExit("--precond-apply times the FFT apply of a stencil operator")
+        return _time_precond(args, op, torch)
     nrhs = 1 if args.op == "A_el" else args.nrhs
     n = op.shape[0]
     rng = np.random.default_rng(7)

@@ -27,8 +27,9 @@ __device__ __forceinline__ double *block_sum_scratch() {
 // NT: the block's thread count.
 template <int NV, int NW, int NT = kCGThreads>
 __device__ __forceinline__ void block_sum(double (&v)[NV], double (*s)[NW], int nv = NV) {
-  // per value: every thread stores its value, one warp adds NT/32 per lane (threads
-  // l NT/32 .. (l+1) NT/32 - 1, in order) and then the 32 lane sums with a fixed shuffle tree
+  // per value: every thread stores its value, one warp adds NT/32 per lane (threads l, l + 32,
+  // l + 64, ..., in order: consecutive lanes read consecutive words, no bank conflicts) and then the
+  // 32 lane sums with a fixed shuffle tree
   double *s_all = block_sum_scratch<NT>();
   const int lane = threadIdx.x & 31;
 #pragma unroll
@@ -39,7 +40,7 @@ __device__ __forceinline__ void block_sum(double (&v)[NV], double (*s)[NW], int 
     if (threadIdx.x < kWarp) {
       double t = 0.0;
 #pragma unroll
-      for (int k = 0; k < NT / kWarp; ++k) t += s_all[lane * (NT / kWarp) + k];
+      for (int k = 0; k < NT / kWarp; ++k) t += s_all[k * kWarp + lane];
       t = warp_sum(t);
       if (lane == 0) s[j][0] = t;
     }
@@ -244,7 +245,7 @@ __device__ __forceinline__ void block_sum_wide(double (&v)[NV], double *tot, dou
     if (j0 + warp < nv && j0 + warp < NV) {
       double t = 0.0;
 #pragma unroll
-      for (int k = 0; k < kCGThreads / kWarp; ++k) t += s_w[warp][lane * (kCGThreads / kWarp) + k];
+      for (int k = 0; k < kCGThreads / kWarp; ++k) t += s_w[warp][k * kWarp + lane];
       t = warp_sum(t);
       if (lane == 0) tot[j0 + warp] = t;
     }
