@@ -1,8 +1,9 @@
 """Benchmark: LLG steps/s of the GSPM step on one GB300 (replicas across GPUs).
 
 Default workload: 128^3 hex with magnetoelastic coupling and the [111]
-rotation (cfg "hex128_me"), in the precision form: FP32 CG with FP64
-reliable updates on the matrix-free stencil operators.  A "step" is one
+rotation (cfg "hex128_me"), in the precision form on the matrix-free stencil
+operators: the elastic and demag solves by FFT inside FP64 refinement, the
+Gauss-Seidel solves by FP32 CG with FP64 reliable updates.  A "step" is one
 Gauss-Seidel-projection LLG step at the next field of the 500-step sweep,
 with all operators and state resident in HBM.
 
@@ -17,14 +18,16 @@ e2e:    the same steps through the public API with the magnetisation copied in
 fp64:   the same steps from the same m0 in plain FP64 on the same GPU, with
         max |m - m_FP64| and the relative <m> error.
 roofline: the CG launches (dominant kernel): algorithmic bytes per launch
-        (stencil CG: 44 B per unknown-iteration in FP32, 88 B in FP64) / the
-        CUDA-event launch time, against MEASURED_PEAKS.json.
+        (stencil CG: 44 B per unknown-iteration in FP32, 88 B in FP64; FFT
+        solve: fft_launch_bytes) / the CUDA-event launch time, against
+        MEASURED_PEAKS.json.
 serving: a sample of the 256-request serving stream through the engine,
         beside the same requests run one at a time in plain FP64.
 cpu_baseline: the CPU oracle (NumPy/SciPy restatement of the reference's step)
         on this machine's host cores.
---impl reference: the oracle's CPU step as the whole measurement (the
-        reference itself needs CuPy and a CUDA GPU; its CPU path is the oracle).
+--impl reference: the oracle's CPU step as the whole measurement, every CG
+        uncapped (the reference itself needs CuPy and a CUDA GPU; its CPU path is
+        the oracle); at 128^3 one cold then one timed step, about 4 min each.
 Multi-GPU: independent replicas (one per rank, no collective on the data path).
 """
 from __future__ import annotations

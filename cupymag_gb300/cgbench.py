@@ -163,7 +163,7 @@ def main(argv=None):
         launch = plan.launch
         info_of = lambda: systems[0].info  # noqa: E731
     else:
-        # the FFT-preconditioned inner solve drops its residual by 1e-4 (a circulant inverse leaves few
+        # the FFT solves' preconditioned-CG form drops its residual by 1e-4 (a circulant inverse leaves few
         # directions to resolve); plain FP32 CG restarts after the --inner-tol drop
         inner_tol = 1e-4 if args.precond else args.inner_tol
         solver = CGSolver()

@@ -52,10 +52,12 @@ SOLVE_NAMES = ["elasticity", "demag", "Gauss-Seidel g1n/g2n/g3n", "Gauss-Seidel 
 # adds an iteration; demag is best near 1e-3.
 INNER_TOL = [0.1, 1e-3, 1e-5, 1e-5, 1e-5, 1e-5]
 
-# Solves that the precision form runs as FFT-preconditioned CG on stencil operators: elasticity and demag,
-# whose operators are circulant apart from the anchor at DOF 0 (the Gauss-Seidel operators A1/A2 carry
-# the defect rows and columns, and plain FP32 CG already needs only 20-55 iterations there).  Each inner
-# preconditioned solve lowers the residual 1e4-fold before the next FP64 residual.
+# Solves that the precision form runs with the FFT solver on stencil operators: elasticity and demag,
+# whose operators are circulant apart from the anchor at node 0, so each FP64 refinement step solves
+# them exactly with one FFT apply (two steps per solve at 128^3).  The Gauss-Seidel operators A1/A2 carry
+# the defect rows and columns; plain FP32 CG needs only 20-55 iterations there, and the circulant inverse
+# as a preconditioner does not lower that.  FFT_INNER_TOL is the inner drop of the preconditioned-CG form,
+# used where an operator has no single anchor.
 FFT_SLOTS = (0, 1)
 FFT_INNER_TOL = 1e-4
 
@@ -79,9 +81,9 @@ class LLGSolver:
 
     def __init__(self, sim_ops, params, precision="DP", device=None, ops=None, operators="csr", info=None,
                  precond="auto"):
-        """precond: "fft" runs the elastic and demag solves of the precision form as FFT-preconditioned CG
-        (stencil operators only), None runs every solve as plain CG; "auto" is "fft" for the precision
-        form on stencil operators."""
+        """precond: "fft" runs the elastic and demag solves of the precision form with the FFT solver
+        (stencil operators only: the exact solve of the anchored operator inside FP64 refinement), None
+        runs every solve as plain CG; "auto" is "fft" for the precision form on stencil operators."""
         self.p = params
         self.precision = "DP" if precision == "DP" else "IR"
         if precond == "auto":

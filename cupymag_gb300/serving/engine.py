@@ -44,8 +44,8 @@ from ..solvers.linear_solvers import decode_info
 from .blockdiag import BlockDiagPlan, BlockSystem, coef_key, work_bytes
 
 NSLOTS = len(SOLVE_NAMES)
-# Runs of at least this many DOFs solve elasticity and demag with the FFT-preconditioned solver, one launch
-# per run; smaller runs keep them in the block-diagonal launches (latency-bound either way).
+# Runs of at least this many DOFs solve elasticity and demag with the FFT solver, one launch per run;
+# smaller runs keep them in the block-diagonal launches (latency-bound either way).
 FFT_MIN_DOFS = 32 ** 3
 
 
@@ -54,14 +54,13 @@ def estimate_bytes(p, precision="IR") -> int:
     solved operators, F1, Fx, Fy, Fz and F_el), so per DOF it is: 33 FP64 vectors of the step (51 with
     magnetoelastic coupling), the volume-average weights, five flag arrays and the defect mask, the
     block-diagonal CG vectors of the largest solve (3n unknowns: five FP32 or three FP64 vectors), and
-    for runs that solve elasticity and demag with the FFT-preconditioned solver its workspace and
-    plans."""
+    for runs that solve elasticity and demag with the FFT solver its workspace and plans."""
     n = int(p.Nx) * int(p.Ny) * int(p.Nz)
     per = (51 if p.ME else 33) * 8 + 8 + 6
     per += 3 * (20 if precision != "DP" else 24)
     if precision != "DP" and n >= FFT_MIN_DOFS:
-        # FFT-preconditioned solves: workspace (five FP32 vectors and a complex field of 3n unknowns) and
-        # the plans' inverse symbols (6 floats per DOF elastic, 1 demag)
+        # FFT solves: workspace (five FP32 vectors and a complex field of 3n unknowns) and the plans'
+        # inverse symbols (6 floats per DOF elastic, 1 demag)
         per += 3 * (20 + 8) + 4 * (6 + 1)
     return int(per * n * 1.05) + (8 << 20)
 
@@ -239,7 +238,7 @@ class ServingEngine:
 
     # ------------------------------------------------------------------ one batched step of a group
     def _fft_solve(self, L, k, A):
-        """Whether slot k of run L is solved alone with the FFT-preconditioned solver (precision form,
+        """Whether slot k of run L is solved alone with the FFT solver (precision form,
         elasticity or demag, a grid of at least FFT_MIN_DOFS DOFs with an FFT plan) instead of in the
         block-diagonal launch.  It depends on the run alone, so a run's result is the same in any mix."""
         return (self.precision == "IR" and L.precond == "fft" and k in FFT_SLOTS and L.n >= FFT_MIN_DOFS

@@ -33,7 +33,7 @@ class CGSolver:
         self.barrier_timeout_s = 2.0
         self.inner_tol = 0.1   # reliable-update factor of the mixed-precision solver
         self.max_outer = 60
-        self.fft_layout = N.FFT_LAYOUT_AUTO  # spectrum layout of the FFT-preconditioned solves
+        self.fft_layout = N.FFT_LAYOUT_AUTO  # spectrum layout of the FFT solves
 
     def workspace(self, n, nrhs, prec):
         key = (n, nrhs, prec)
