@@ -183,21 +183,29 @@ def stencil_launch_bytes(A, nvec, iters, outer, fp32):
 IR_STENCIL_DRAM_BYTES_PER_UNKNOWN_ITER = 20.6
 
 
-def fft_launch_bytes(A, iters, outer):
+def fft_launch_bytes(A, iters, outer, warm=True, carry=False):
     """Algorithmic bytes of an FFT solve launch (csrc/fftcg.cu), per unknown.
 
     Direct refinement (operators pinned at one anchor node, the default): each FP64 residual 20 B (read
-    x, b; write r), one more residual than steps; each step 52 B plus the inverse symbol of the half
-    spectrum (4 B elastic, 2 B scalar): slab pass 1 (read r 4, write the half spectrum 4), pass 2 (read
-    and write it, 8), pass 3 (read it 4, write z 4, read r 4), x += z + shift (read z 4, x 16); read b once
-    (8).  Preconditioned CG: inner iteration 120 B + the full symbol (8 B elastic, 4 B scalar), each FP64
-    residual and fold 44 B."""
+    x, b; write r) plus 8 B with a residual carry (write t), one more residual than steps; the first of a
+    cold start reads no x (x = 0: 12 B, and 8 B more with a carry, which also takes b); the first of a
+    warm start with a carry is read from it (b, the carry's b and t; write r, b, t: 44 B) and, when it
+    already meets the test, confirmed by an FP64 residual.  Each step 52 B plus the inverse symbol of the
+    half spectrum (4 B elastic, 2 B scalar): slab pass 1 (read r 4, write the half spectrum 4), pass 2
+    (read and write it, 8), pass 3 (read it 4, write z 4, read r 4), x += z + shift (read z 4, x 16); read
+    b once (8).  Preconditioned CG: inner iteration 120 B + the full symbol (8 B elastic, 4 B scalar),
+    each FP64 residual and fold 44 B (36 B for a cold start's first)."""
     u = A.shape[0]
     if getattr(A, "anchor", -1) >= 0:
         steps = max(outer, 0)
-        return u * (20 * (steps + 1) + (52 + (4 if A.ncomp == 3 else 2)) * steps + 8)
+        ct = 8 if carry else 0
+        if warm and carry:
+            first, rest = 44, max(steps, 1)
+        else:
+            first, rest = (20 if warm else 12) + 2 * ct, steps
+        return u * (first + (20 + ct) * rest + (52 + (4 if A.ncomp == 3 else 2)) * steps + 8)
     per_inner = 120 + (8 if A.ncomp == 3 else 4)
-    return u * (per_inner * iters + 44 * max(outer, 1) + 8)
+    return u * (per_inner * iters + 44 * max(outer, 1) - (0 if warm else 8) + 8)
 
 
 def cg_launch_bytes(A, nvec, iters, warm):
@@ -444,7 +452,7 @@ def run_ours(args):
         fp32 = args.precision != "DP"
         if hasattr(A, "ncomp") and fp32 and L.precond == "fft" and k in FFT_SLOTS and nv == 1 and \
                 A.fft_plan() is not None:
-            kn, b = "cg_stencil_fft_kernel", fft_launch_bytes(A, its, inf["outer"])
+            kn, b = "cg_stencil_fft_kernel", fft_launch_bytes(A, its, inf["outer"], warm, k in L.carry)
         elif hasattr(A, "ncomp"):
             kn = "cg_stencil_ir_kernel" if fp32 else "cg_stencil_fp64_kernel"
             b = stencil_launch_bytes(A, nv, its, inf["outer"], fp32)
@@ -559,7 +567,8 @@ def run_ours(args):
             "config": workload_config(args, w, S, p, world, ops_kind),
             "run": {"timed_steps": f"{args.warmup}..{args.warmup + args.steps - 1}",
                     "resident_gb": round(resident_gb, 2), "csr_operator_gb": round(op_gb, 2),
-                    "setup_s": round(t_setup, 1), "cg_iterations_per_step": [round(x, 1) for x in its_mean]},
+                    "setup_s": round(t_setup, 1), "cg_iterations_per_step": [round(x, 1) for x in its_mean],
+                    "warm_started_steps": int(sum(int(w.item()) for w in warm_hist))},
             "e2e": {"value": round(e2e_value, 4), "unit": "steps/s",
                     "h2d_bytes_per_step": S.n_dof * 3 * 8, "d2h_bytes_per_step": S.n_dof * 3 * 8 + 24},
             "gpu_launches": launches,

@@ -44,7 +44,8 @@ class CGInfo(C.Structure):
 
 class CGOpts(C.Structure):
     _fields_ = [("tol", dbl), ("maxiter", i32), ("use_init_host", i32), ("use_init_dev", vp), ("precision", i32),
-                ("inner_tol", dbl), ("max_outer", i32), ("form", i32), ("barrier_timeout_s", dbl)]
+                ("inner_tol", dbl), ("max_outer", i32), ("form", i32), ("barrier_timeout_s", dbl),
+                ("carry_b", vp), ("carry_t", vp), ("carry_valid", vp)]
 
 
 class FieldParams(C.Structure):

@@ -586,6 +586,8 @@ struct FftCGArgs {
   int quads;
   int anchor;  // >= 0: direct refinement with this pinned node; -1: preconditioned CG
   int even;    // elastic stencil even in the offset: the FP64 residual sums opposite neighbours first
+  double *cb, *ct;  // residual carry of the direct solve: b and t = b - A64 x of the last residual pass
+  int *carry_valid;  // device flag: cb, ct belong to the current x (read at entry, written at exit)
   double e64[9 * 14];  // even part (c(d) + c(26 - d)) / 2 per block (p, q) for d < 13, then c(13)
 };
 
@@ -648,15 +650,21 @@ __device__ __forceinline__ void apply_even3(const FftCGArgs &a, const double *x,
 }
 
 // t = b - A64 x on this CTA's DOFs: r = t (FP32), d = 0; v[0] = the thread's FP64 partial of t . t
-// and, with SUMS, v[1 + c] = its partial of the sum of component c of t.
+// and, with SUMS, v[1 + c] = its partial of the sum of component c of t.  With SUMS and a carry,
+// t goes to the carry too (and b, on the solve's first pass: wb).  x0: x = 0 (a cold start's first
+// pass), so t = b exactly and the product is skipped.
 template <int NC, int NT, bool SUMS, int NV>
-__device__ __forceinline__ void true_residual64(const FftCGArgs &a, int64_t d0, int64_t d1, double (&v)[NV]) {
+__device__ __forceinline__ void true_residual64(const FftCGArgs &a, int64_t d0, int64_t d1, double (&v)[NV],
+                                                bool wb, bool x0) {
   const int64_t n = a.S.n;
 #pragma unroll
   for (int j = 0; j < NV; ++j) v[j] = 0.0;
   for (int64_t dof = d0 + threadIdx.x; dof < d1; dof += NT) {
     double y[NC];
-    if constexpr (NC == 3) {
+    if (x0) {
+#pragma unroll
+      for (int u = 0; u < NC; ++u) y[u] = 0.0;
+    } else if constexpr (NC == 3) {
       if (a.even && !(a.S.flags && a.S.flags[dof])) apply_even3(a, a.x, (int)dof, y);
       else apply<double, NC, 1>(a.S, a.x, (int)dof, y);
     } else {
@@ -665,13 +673,39 @@ __device__ __forceinline__ void true_residual64(const FftCGArgs &a, int64_t d0, 
 #pragma unroll
     for (int u = 0; u < NC; ++u) {
       const int64_t i = uidx<NC, 1>(n, dof, u);
-      const double t = a.b[i] - y[u];
+      const double bi = a.b[i], t = bi - y[u];
       a.r[i] = (float)t;
       if (!SUMS) a.d[i] = 0.0f;
       v[0] = fma(t, t, v[0]);
-      if (SUMS) v[1 + u] += t;
+      if (SUMS) {
+        v[1 + u] += t;
+        if (a.ct) {
+          a.ct[i] = t;
+          if (wb) a.cb[i] = bi;
+        }
+      }
     }
   }
+}
+
+// The first residual of a warm start from the x of the carry: t = (b - b_c) + t_c, no product
+// (b - A x = (b - b_c) + (b_c - A x)).  Same outputs as true_residual64 with SUMS; the carry takes b and t.
+template <int NC, int NT>
+__device__ __forceinline__ void carried_residual(const FftCGArgs &a, int64_t d0, int64_t d1, double (&v)[1 + NC]) {
+  const int64_t n = a.S.n;
+#pragma unroll
+  for (int j = 0; j < 1 + NC; ++j) v[j] = 0.0;
+  for (int64_t dof = d0 + threadIdx.x; dof < d1; dof += NT)
+#pragma unroll
+    for (int u = 0; u < NC; ++u) {
+      const int64_t i = uidx<NC, 1>(n, dof, u);
+      const double bi = a.b[i], t = (bi - a.cb[i]) + a.ct[i];
+      a.r[i] = (float)t;
+      a.cb[i] = bi;
+      a.ct[i] = t;
+      v[0] = fma(t, t, v[0]);
+      v[1 + u] += t;
+    }
 }
 
 // The right-hand side t~ of the direct step (CTA 0, after the residual's grid sum): the free
@@ -736,6 +770,7 @@ __global__ void __launch_bounds__(FftShape<LAYOUT>::threads, FftShape<LAYOUT>::b
     }
   if (!grid_sum<1, NW, NT>(v, a.part, par, a.bar, tns, s_red)) {
     set_status(a.info, CPM_BARRIER_TIMEOUT);
+    if (a.carry_valid && blockIdx.x == 0 && threadIdx.x == 0) *a.carry_valid = 0;
     return;
   }
   const double bnorm = sqrt(v[0]);
@@ -749,16 +784,29 @@ __global__ void __launch_bounds__(FftShape<LAYOUT>::threads, FftShape<LAYOUT>::b
       for (int u = 0; u < NC; ++u) x[uidx<NC, 1>(n, dof, u)] = b[uidx<NC, 1>(n, dof, u)];
     conv = 1;
   }
-  // ---- direct refinement: x += A^-1 t with the anchored exact inverse, one FFT solve per step
+  // ---- direct refinement: x += A^-1 t with the anchored exact inverse, one FFT solve per step.
+  // A warm start from the x of a valid carry takes its first residual from the carry; a carried
+  // residual that already meets the test is confirmed by an FP64 residual before the solve stops.
+  // `settled`: the loop left right after a residual pass of the final x (the carry then stays valid).
+  bool carry = a.ct && use_init && !conv && __ldcg(a.carry_valid) == 1;
+  bool first = true, settled = false;
   while (!conv && a.anchor >= 0) {
     const int an = a.anchor;
     double v[1 + NC];
-    true_residual64<NC, NT, true>(a, d0, d1, v);
+    const bool carried = carry;
+    if (carried) carried_residual<NC, NT>(a, d0, d1, v);
+    else true_residual64<NC, NT, true>(a, d0, d1, v, first, first && !use_init);
+    carry = first = false;
     if (!grid_sum<1 + NC, NW, NT>(v, a.part, par, a.bar, tns, s_red)) { status = CPM_BARRIER_TIMEOUT; break; }
     resid = sqrt(v[0]);
     if (!isfinite(resid)) { status = CPM_NONFINITE; break; }
-    if (resid <= atol) { conv = 1; break; }
-    if (iters >= a.maxiter) break;
+    if (resid <= atol) {
+      if (carried) continue;
+      conv = 1;
+      settled = true;
+      break;
+    }
+    if (iters >= a.maxiter) { settled = true; break; }
     outer += 1;
     iters += 1;
     // the anchored rows are identity rows: t_a = b_a - x_a
@@ -789,7 +837,7 @@ __global__ void __launch_bounds__(FftShape<LAYOUT>::threads, FftShape<LAYOUT>::b
   while (!conv && a.anchor < 0 && status == CPM_OK) {
     // ---- true residual t = b - A64 x (x complete after the last barrier): r = t, d = 0
     double tt[1];
-    true_residual64<NC, NT, false>(a, d0, d1, tt);
+    true_residual64<NC, NT, false>(a, d0, d1, tt, false, outer == 0 && !use_init);
     if (!grid_sum<1, NW, NT>(tt, a.part, par, a.bar, tns, s_red)) { status = CPM_BARRIER_TIMEOUT; break; }
     resid = sqrt(tt[0]);
     if (!isfinite(resid)) { status = CPM_NONFINITE; break; }
@@ -860,6 +908,7 @@ __global__ void __launch_bounds__(FftShape<LAYOUT>::threads, FftShape<LAYOUT>::b
     a.info->bnorm[0] = bnorm;
     a.info->outer = outer;
     set_status(a.info, st);
+    if (a.carry_valid) *a.carry_valid = (settled && status == CPM_OK) ? 1 : 0;
   } else if (status != CPM_OK && threadIdx.x == 0) {
     set_status(a.info, status);
   }
@@ -1106,6 +1155,19 @@ extern "C" int cpm_cg_solve_stencil_fft(const cpm_stencil *S, const cpm_fft_prec
   a.timeout_ns = (unsigned long long)(tmo * 1e9);
   a.quads = (S->nz & 3) == 0 && ((uintptr_t)S->flags & 3) == 0;
   a.anchor = (P->anchor >= 0 && o->form != CPM_CG_FORM_FFT_PCG) ? P->anchor : -1;
+  const int ncarry = !!o->carry_b + !!o->carry_t + !!o->carry_valid;
+  if (ncarry != 0 && ncarry != 3) {
+    set_error("cpm_cg_solve_stencil_fft: carry_b, carry_t and carry_valid are given together or not at all");
+    return CPM_BAD_ARG;
+  }
+  if (ncarry == 3 && (o->carry_b == b || o->carry_t == b || o->carry_b == x || o->carry_t == x ||
+                      o->carry_b == o->carry_t)) {
+    set_error("cpm_cg_solve_stencil_fft: the carry vectors must not alias b, x or each other");
+    return CPM_BAD_ARG;
+  }
+  a.cb = o->carry_b;
+  a.ct = o->carry_t;
+  a.carry_valid = o->carry_valid;
   if (nc == 3) {
     // even blocks (to 1e-12 of their largest coefficient): the pair-summed FP64 residual
     a.even = 1;

@@ -35,7 +35,7 @@ import numpy as np
 import torch
 
 from .. import _native as N
-from ..solvers.linear_solvers import CGSolver, decode_info, new_info, raise_for
+from ..solvers.linear_solvers import CGSolver, ResidualCarry, decode_info, new_info, raise_for
 from ..utils.rot_111_matrices import get_M_matrix, get_R_matrix
 from ..utils.sigma_matrices import get_Ebar_sigma
 
@@ -150,6 +150,12 @@ class LLGSolver:
         self.M36_dev = torch.as_tensor(M.reshape(-1), **f64)
         self.MinvT36_dev = torch.as_tensor(np.linalg.inv(M).T.reshape(-1).copy(), **f64)
         self.Es_dev = torch.as_tensor(get_Ebar_sigma(params), **f64)
+        # residual carries of the FFT solves (elasticity: 3n unknowns, demag: n), keyed by slot
+        self.carry = {}
+        if self.precond == "fft" and self.precision == "IR":
+            self.carry[1] = ResidualCarry(n, dev)
+            if self.ME:
+                self.carry[0] = ResidualCarry(3 * n, dev)
         self.thresh = params.use_init_factor * (n * params.LLG_accuracy_factor)
         self.nstep = 0
         self.launches = 0          # kernels this solver has launched (C-ABI calls that start one kernel)
@@ -163,6 +169,8 @@ class LLGSolver:
         self.m_prev.copy_(self.m)
         self.Avg.average_into(self.m, self.avg_m)
         self.use_init.zero_()
+        for c in self.carry.values():
+            c.invalidate()
         self.sumsq.fill_(math.inf)
         self.nstep = 0
 
@@ -182,11 +190,14 @@ class LLGSolver:
     def _state_tensors(self):
         """Every device tensor that carries over from one step to the next: m, m_prev, <m>, sumsq,
         the warm-start flag, the previous solutions the warm-started solves start from (U, the g's,
-        m**, and u with magnetoelastic coupling) and the field-schedule position."""
+        m**, and u with magnetoelastic coupling), the FFT solves' residual carries and the field-schedule
+        position."""
         t = {"m": self.m, "m_prev": self.m_prev, "avg_m": self.avg_m, "sumsq": self.sumsq, "use_init": self.use_init,
              "U": self.U, "g": self.g, "g1s": self.g1s, "g2s": self.g2s, "mss": self.mss}
         if self.ME:
             t["u"] = self.u
+        for k, c in self.carry.items():
+            t.update({f"carry{k}_b": c.b, f"carry{k}_t": c.t, f"carry{k}_valid": c.valid})
         if self.hsched is not None:
             t.update(hsched=self.hsched, hstep=self.hstep, hist=self.hist)
         return t
@@ -217,8 +228,13 @@ class LLGSolver:
             self.set_field_schedule(d["hsched"])
         for k, t in self._state_tensors().items():
             if k not in d:
+                if k.startswith("carry"):
+                    continue  # a checkpoint without carries: the next FFT solves start from FP64 residuals
                 raise ValueError(f"checkpoint lacks {k}")
             t.copy_(torch.as_tensor(d[k], device=self.dev))
+        for k, c in self.carry.items():
+            if f"carry{k}_valid" not in d:
+                c.invalidate()
         self.nstep = int(d["nstep"])
 
     # ------------------------------------------------------------------ building blocks
@@ -241,7 +257,8 @@ class LLGSolver:
         fft = self.precond == "fft" and k in FFT_SLOTS
         self.solver.launch(A, b, x, self.info[k], tol=self.p.tol, maxiter=self.p.maxiter,
                            use_init_dev=self.use_init, precision=self.precision,
-                           inner_tol=FFT_INNER_TOL if fft else INNER_TOL[k], precond="fft" if fft else None)
+                           inner_tol=FFT_INNER_TOL if fft else INNER_TOL[k], precond="fft" if fft else None,
+                           carry=self.carry.get(k) if fft else None)
 
     def cg_request(self, A, b, x, k):
         """A solve of this step, for an executor that batches solves of several runs."""

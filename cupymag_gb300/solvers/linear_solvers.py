@@ -46,7 +46,7 @@ class CGSolver:
 
     def launch(self, A: DeviceCSR, b: torch.Tensor, x: torch.Tensor, info: torch.Tensor, *, tol, maxiter,
                use_init=False, use_init_dev: torch.Tensor = None, precision="DP", inner_tol=None, form=0,
-               precond=None):
+               precond=None, carry=None):
         """Asynchronous solve; x is read as x0 when use_init, and overwritten.
 
         form (FP32 stencil solves): N.CG_FORM_DEFAULT (three grid barriers per iteration),
@@ -55,11 +55,13 @@ class CGSolver:
         whose steps solve with the operator's circulant inverse, exactly (one FFT solve per step)
         where the operator pins one node, else as the preconditioner of FP32 CG (inner_tol: the
         residual drop of each inner solve; form=N.CG_FORM_FFT_PCG asks for that form); the plain
-        FP32 form is used where the grid has no FFT plan."""
+        FP32 form is used where the grid has no FFT plan.  carry (a ResidualCarry of the system's size):
+        the direct FFT solve keeps its last FP64 residual there, and a warm start from that solve's x
+        takes its first residual from it instead of a product (other solves ignore it)."""
         prec = PRECISIONS[precision] if isinstance(precision, str) else int(precision)
         if precond == "fft" and prec == 1 and hasattr(A, "fft_plan") and b.dim() == 1 and A.fft_plan() is not None:
             return self._launch_fft(A, b, x, info, tol=tol, maxiter=maxiter, use_init=use_init,
-                                    use_init_dev=use_init_dev, inner_tol=inner_tol, form=form)
+                                    use_init_dev=use_init_dev, inner_tol=inner_tol, form=form, carry=carry)
         if prec == 1:
             A.ensure_fp32()
         n = A.shape[0]
@@ -85,7 +87,7 @@ class CGSolver:
                    info.data_ptr(), N.stream_ptr()), "cpm_cg_solve")
 
 
-    def _launch_fft(self, A, b, x, info, *, tol, maxiter, use_init, use_init_dev, inner_tol, form=0):
+    def _launch_fft(self, A, b, x, info, *, tol, maxiter, use_init, use_init_dev, inner_tol, form=0, carry=None):
         if b.shape[0] != A.shape[0] or x.shape != b.shape or b.dtype != torch.float64 or x.dtype != torch.float64 \
                 or not (b.is_contiguous() and x.is_contiguous()):
             raise ValueError("b and x must be contiguous float64 device vectors of the operator's size")
@@ -104,10 +106,29 @@ class CGSolver:
         o.inner_tol = 1e-4 if inner_tol is None else float(inner_tol)
         o.form = int(form)
         o.barrier_timeout_s = self.barrier_timeout_s
+        if carry is not None:
+            if carry.b.shape[0] != b.shape[0] or carry.b.device != b.device:
+                raise ValueError("the residual carry must match the system's size and device")
+            o.carry_b, o.carry_t, o.carry_valid = carry.b.data_ptr(), carry.t.data_ptr(), carry.valid.data_ptr()
         N.check(N.lib().cpm_cg_solve_stencil_fft(A.struct(), A.fft_plan(self.fft_layout), b.data_ptr(),
                                                  x.data_ptr(), C.byref(o),
                                                  ws.data_ptr(), ws.numel(), info.data_ptr(), N.stream_ptr()),
                 "cpm_cg_solve_stencil_fft")
+
+
+class ResidualCarry:
+    """Device storage of the direct FFT solve's residual carry for one system of n unknowns: the b and
+    the FP64 residual t = b - A x of its last residual pass, and a flag (int32) that the solve sets when
+    x is still the x of that pass.  invalidate() after any change of x other than by the solve."""
+
+    def __init__(self, n, device=None):
+        f64 = dict(dtype=torch.float64, device=device or "cuda")
+        self.b = torch.zeros(int(n), **f64)
+        self.t = torch.zeros(int(n), **f64)
+        self.valid = torch.zeros(1, dtype=torch.int32, device=self.b.device)
+
+    def invalidate(self):
+        self.valid.zero_()
 
 
 def new_info(count=1, device=None) -> torch.Tensor:

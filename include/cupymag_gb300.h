@@ -70,6 +70,17 @@ typedef struct {
                               FFT solves: CPM_CG_FORM_DEFAULT (direct refinement with an anchored
                               plan) or CPM_CG_FORM_FFT_PCG */
   double barrier_timeout_s;/* bound on every grid-barrier wait (seconds) */
+  /* Residual carry of the FFT direct solve (cpm_cg_solve_stencil_fft with an anchored plan; all three
+   * NULL: none).  carry_b and carry_t hold one vector each of the system's size, carry_valid one int,
+   * all on the device.  Each FP64 residual pass stores t = b - A x in carry_t and the solve's b in
+   * carry_b; at exit the solve sets *carry_valid to 1 when its final x is the x of its last residual
+   * pass (converged, or stopped at maxiter) and to 0 otherwise.  A warm-started solve that finds
+   * *carry_valid = 1 takes (b - carry_b) + carry_t as its first residual, three vector reads in place
+   * of an FP64 product; if that residual already meets the stopping test an FP64 residual confirms it.
+   * The caller zeroes *carry_valid whenever x changes other than by the solve that wrote the carry. */
+  double *carry_b;
+  double *carry_t;
+  int32_t *carry_valid;
 } cpm_cg_opts;
 
 /* Iteration forms of the FP32 stencil CG (cpm_cg_opts.form).  Both run CG to

@@ -15,7 +15,9 @@ diagonal) with DFTs along each axis in shared memory.  Checked here:
   direct refinement (the anchored operator inverted exactly by one FFT solve
   per FP64 step) and FP32 CG preconditioned by the circulant inverse;
 * the direct step alone is the exact inverse of the anchored operator: one
-  step from x = 0 against the host's dense solve.
+  step from x = 0 against the host's dense solve;
+* the residual carry of the direct solve (the first residual of a warm start
+  taken from the previous solve's FP64 residual) against warm starts without it.
 """
 import numpy as np
 import pytest
@@ -183,3 +185,92 @@ def test_direct_step_is_the_exact_inverse_of_the_anchored_operator(dims, layout)
                       precision="IR", precond="fft")
         err = np.abs(x.cpu().numpy() - ref).max() / np.abs(ref).max()
         assert err <= 1e-4, (name, dims, layout, err)
+
+
+@pytest.mark.parametrize("layout", LAYOUTS)
+def test_direct_solve_residual_carry(layout):
+    """The residual carry of the direct solve: after a solve it holds b and the FP64 residual of the
+    returned x (flag 1, also when maxiter stops the solve); warm starts that take their first residual
+    from it meet the FP64 stopping test like warm starts without it; a changed x with the flag cleared
+    is solved from an FP64 residual; b = 0 and the preconditioned-CG form clear the flag; the C-ABI
+    refuses a partial or aliased carry."""
+    import types
+    from cupymag_gb300 import _native as N
+    from cupymag_gb300.solvers.linear_solvers import CGSolver, ResidualCarry, decode_info, new_info
+    S, p = _sim(Nx=12, Ny=10, Nz=14, Ndx=3, Ndy=3, Ndz=3, ME=True)
+    so = S.stencil_operators()
+    csr = S.host_operators()
+    rng = np.random.default_rng(11)
+    solver = CGSolver()
+    solver.fft_layout = _layout(layout)
+    eps = np.finfo(np.float64).eps
+    for name in ("A_demag", "A_el"):
+        A = csr[name]
+        n = A.shape[0] // so[name].ncomp
+        pins = [0, n, 2 * n] if name == "A_el" else [0]
+        b0 = rng.normal(size=A.shape[0])
+        b0[pins] = 0.0
+        delta = rng.normal(size=A.shape[0])
+        delta[pins] = 0.0
+        carry = ResidualCarry(A.shape[0])
+        info = new_info(1)
+
+        def solve(b, x, use_init, carry=carry, maxiter=20000, form=_form("direct")):
+            solver.launch(so[name], torch.as_tensor(b, device="cuda"), x, info[0], tol=1e-10, maxiter=maxiter,
+                          precision="IR", use_init=use_init, precond="fft", form=form, carry=carry)
+            return decode_info(info[0].cpu().numpy())
+
+        def carry_matches(b, x):
+            xs = x.cpu().numpy()
+            bound = 64 * eps * (abs(A) @ np.abs(xs) + np.abs(b))
+            assert np.array_equal(carry.b.cpu().numpy(), b), name
+            assert np.all(np.abs(carry.t.cpu().numpy() - (b - A @ xs)) <= bound), name
+            assert int(carry.valid.item()) == 1, name
+
+        # cold solve: the carry holds b and the residual of x
+        x = torch.zeros(A.shape[0], dtype=torch.float64, device="cuda")
+        inf = solve(b0, x, False)
+        assert inf["status"] == N.CPM_OK, inf
+        carry_matches(b0, x)
+        # warm starts from the carry against warm starts without it
+        x_plain = x.clone()
+        for k in range(1, 4):
+            b = b0 + 1e-3 * k * delta
+            inf = solve(b, x, True)
+            inf_plain = solve(b, x_plain, True, carry=None)
+            for xx, ii in ((x, inf), (x_plain, inf_plain)):
+                assert ii["status"] == N.CPM_OK, (name, k, ii)
+                assert np.linalg.norm(b - A @ xx.cpu().numpy()) <= 1e-10 * np.linalg.norm(b) * 1.001, (name, k)
+            assert abs(inf["iters"][0] - inf_plain["iters"][0]) <= 1, (name, k, inf, inf_plain)
+            carry_matches(b, x)
+        # the same b again: the carried residual meets the test, an FP64 residual confirms it, no step
+        inf = solve(b, x, True)
+        assert inf["status"] == N.CPM_OK and inf["iters"][0] == 0, inf
+        carry_matches(b, x)
+        # x changed by the caller, flag cleared: solved from an FP64 residual
+        x += torch.as_tensor(1e-3 * delta, device="cuda")
+        carry.invalidate()
+        inf = solve(b, x, True)
+        assert inf["status"] == N.CPM_OK and inf["iters"][0] >= 1, inf
+        assert np.linalg.norm(b - A @ x.cpu().numpy()) <= 1e-10 * np.linalg.norm(b) * 1.001, name
+        carry_matches(b, x)
+        # stopped by maxiter: the carry still describes the returned x
+        x.zero_()
+        inf = solve(b0, x, False, maxiter=1)
+        assert inf["status"] == N.CPM_NOT_CONVERGED, inf
+        carry_matches(b0, x)
+        # b = 0 (x = b) and the preconditioned-CG form leave no valid carry
+        inf = solve(np.zeros_like(b0), x, True)
+        assert inf["status"] == N.CPM_OK and int(carry.valid.item()) == 0, inf
+        x.zero_()
+        solve(b0, x, False)
+        assert int(carry.valid.item()) == 1
+        solve(b0, x, True, form=_form("pcg"))
+        assert int(carry.valid.item()) == 0
+        # a partial carry or one that aliases x is refused before any launch
+        bad = types.SimpleNamespace(b=carry.b, t=carry.t, valid=types.SimpleNamespace(data_ptr=lambda: 0))
+        with pytest.raises(RuntimeError, match="together"):
+            solve(b0, x, True, carry=bad)
+        alias = types.SimpleNamespace(b=x, t=carry.t, valid=carry.valid)
+        with pytest.raises(RuntimeError, match="alias"):
+            solve(b0, x, True, carry=alias)
