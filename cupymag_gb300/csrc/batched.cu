@@ -166,7 +166,7 @@ __device__ __forceinline__ void write_info(cpm_cg_info *info, int status, const 
     info->resid[j] = j < ns ? resid[j] : 0.0;
   }
   info->outer = outer;
-  info->pad = 0;
+  info->df_updates = 0;
   info->status = st;
 }
 
@@ -601,7 +601,7 @@ __global__ void __launch_bounds__(kCGThreads, (NC == 1 && NR == 3) ? 3 : 4) cg_b
       S.info->resid[j] = j < NS ? st[j].resid : 0.0;
     }
     S.info->outer = st[0].updates;
-    S.info->pad = 0;
+    S.info->df_updates = 0;
     S.info->status = sta;
   }
 }
@@ -875,7 +875,7 @@ __global__ void __launch_bounds__(kCGThreads, (NC == 1 && NR == 3) ? 3 : 4) cg_b
       if (j < NS) upd += st[j].updates;
     }
     S.info->outer = upd;
-    S.info->pad = 0;
+    S.info->df_updates = 0;
     S.info->status = sta;
   }
 }

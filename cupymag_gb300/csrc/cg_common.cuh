@@ -88,9 +88,12 @@ __device__ __forceinline__ bool grid_sum(double (&v)[NV], double *part, int &par
 // State of one system of the FP32 CG with lagged FP64 reliable updates
 // (csrc/cg.cu, csrc/stencil.cu, csrc/batched.cu).  The transitions below are the whole
 // scalar logic of that solver; the kernels call them once per reduction.
+// dfe > 0: the pending update may be a double-float residual whose error is at most dfe (csrc/stencil.cu);
+// dfok marks an update scheduled that way, exact forces FP64 updates from then on, dfupd counts the
+// double-float updates.
 struct IRState {
-  double atol, resid, rho, r0;
-  int active, need, iters, unconv, updates, pad;
+  double atol, resid, rho, r0, dfe;
+  int active, need, iters, unconv, updates, dfok, exact, dfupd;
 };
 
 __device__ __forceinline__ void ir_init(IRState &s, double bnorm, double rr0, double tol) {
@@ -98,18 +101,25 @@ __device__ __forceinline__ void ir_init(IRState &s, double bnorm, double rr0, do
   s.rho = rr0;
   s.resid = sqrt(rr0);
   s.r0 = s.resid;
+  s.dfe = 0.0;
   s.active = bnorm != 0.0;
   s.need = 0;
   s.iters = 0;
   s.unconv = 0;
   s.updates = 0;
+  s.dfok = 0;
+  s.exact = 0;
+  s.dfupd = 0;
 }
 
 // After the p.q reduction (pq) with, for a pending update, the true residual
 // norm tt = t.t and tp = t.p: decide convergence on t and return alpha
 // (exact line search along p when t replaced the residual).  Returns true on
 // a non-finite value.
-__device__ __forceinline__ bool ir_after_pq(IRState &s, double pq, double tt, double tp, int maxiter, double &alpha) {
+// With dfpass the residual was double-float: it decides convergence only outside its error bound
+// (resid <= atol - dfe); within dfe of atol every later update is FP64.
+__device__ __forceinline__ bool ir_after_pq(IRState &s, double pq, double tt, double tp, int maxiter, double &alpha,
+                                            bool dfpass = false) {
   bool bad = false;
   alpha = 0.0;
   if (s.need) {
@@ -117,7 +127,10 @@ __device__ __forceinline__ bool ir_after_pq(IRState &s, double pq, double tt, do
     s.r0 = s.resid;
     s.rho = tt;
     if (!isfinite(s.resid)) bad = true;
-    if (s.resid <= s.atol) s.active = 0;
+    if (dfpass) {
+      if (s.resid <= s.atol - s.dfe) s.active = 0;
+      else if (s.resid <= s.atol + s.dfe) s.exact = 1;
+    } else if (s.resid <= s.atol) s.active = 0;
     else if (s.iters >= maxiter) {
       s.active = 0;
       s.unconv = 1;
@@ -141,6 +154,7 @@ __device__ __forceinline__ bool ir_after_rr(IRState &s, double rr, double delta,
   s.iters += 1;
   const double rn = sqrt(rr);
   s.need = (rn < delta * s.r0) || (rn <= s.atol) || (s.iters >= maxiter);
+  s.dfok = s.need && s.dfe > 0.0 && !s.exact && s.iters < maxiter;
   beta = (float)(rr / s.rho);
   s.rho = rr;
   return bad;

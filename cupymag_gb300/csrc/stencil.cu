@@ -50,6 +50,9 @@ struct StencilCG {
   unsigned long long timeout_ns;
   int64_t dofs_per_cta;
   int quads;  // nz % 4 == 0, 4-byte aligned flags, 16-byte aligned x: the FP32 phases run on quads
+  float *xh, *xl;     // x split into floats hi + lo for double-float residual passes (null: FP64 only)
+  df::DF cdf[27];     // the scalar coefficients as double-float values
+  double df_err;      // error bound of a double-float residual as a multiple of ||b|| (<= 0: off)
 };
 
 // Number of independent systems (each with its own CG scalars).
@@ -233,7 +236,7 @@ __global__ void __launch_bounds__(kIRThreads, 4) cg_stencil_ir_kernel(const __gr
   __shared__ double s_red[9][TH / kWarp];
   __shared__ IRState st[NS];
   __shared__ float s_ab[NS];
-  __shared__ int s_mask[3];  // active, need, error status
+  __shared__ int s_mask[4];  // active, need, error status, double-float pass
   const int64_t n = a.S.n;
   const int64_t d0 = min(n, (int64_t)blockIdx.x * a.dofs_per_cta);
   const int64_t d1 = min(n, d0 + a.dofs_per_cta);
@@ -243,18 +246,24 @@ __global__ void __launch_bounds__(kIRThreads, 4) cg_stencil_ir_kernel(const __gr
   const double *__restrict__ b = a.b;
   double *x = a.x;
   float *r32 = a.r32, *p32 = a.p32, *q32 = a.q32, *d32 = a.d32;
+  float *xh = NC == 1 ? a.xh : nullptr, *xl = a.xl;
   int par = 0;
 
-  // ---- prologue: r = b - A64 x (FP64), r32 = p32 = r, d = 0; ||b||, ||r||
-  double v[2 * NS];
+  // ---- prologue: r = b - A64 x (FP64), r32 = p32 = r, d = 0; ||b||, ||r||; with the split form of x,
+  // also the split x and a count of the flagged rows that are not pinned
+  double v[2 * NS + 1];
 #pragma unroll
-  for (int j = 0; j < 2 * NS; ++j) v[j] = 0.0;
+  for (int j = 0; j < 2 * NS + 1; ++j) v[j] = 0.0;
   for (int64_t dof = d0 + threadIdx.x; dof < d1; dof += TH) {
     double y[U];
     // a pinned DOF (identity row, excluded column) is solved by x = b, written when the solve ends;
     // until then x, its residual and every FP32 vector stay zero there, so the products need no
     // column tests
     const bool pin = is_pinned(a.S, dof);
+    if (xh && a.S.flags) {
+      const int fr = a.S.flags[dof] & (kRowIdentity | kRowZero | kColExcluded);
+      if (fr && !pin) v[2 * NS] += 1.0;
+    }
     if (use_init && !pin) apply<double, NC, NR>(a.S, x, (int)dof, y);
 #pragma unroll
     for (int u = 0; u < U; ++u) {
@@ -262,6 +271,7 @@ __global__ void __launch_bounds__(kIRThreads, 4) cg_stencil_ir_kernel(const __gr
       const double bi = b[i];
       const double ri = pin ? 0.0 : use_init ? bi - y[u] : bi;
       if (pin || !use_init) x[i] = 0.0;
+      if (xh) split_store((pin || !use_init) ? 0.0 : x[i], xh, xl, i);
       const float rf = (float)ri;
       r32[i] = rf;
       p32[i] = rf;
@@ -271,7 +281,7 @@ __global__ void __launch_bounds__(kIRThreads, 4) cg_stencil_ir_kernel(const __gr
       v[NS + s] = fma(ri, ri, v[NS + s]);
     }
   }
-  if (!grid_sum<2 * NS>(v, a.part, par, a.bar, tns, s_red)) {
+  if (!grid_sum<2 * NS + 1>(v, a.part, par, a.bar, tns, s_red, xh ? 2 * NS + 1 : 2 * NS)) {
     set_status(a.info, CPM_BARRIER_TIMEOUT);
     return;
   }
@@ -279,15 +289,19 @@ __global__ void __launch_bounds__(kIRThreads, 4) cg_stencil_ir_kernel(const __gr
     int am = 0;
     for (int j = 0; j < NS; ++j) {
       ir_init(st[j], sqrt(v[j]), v[NS + j], a.tol);
+      // the error bound holds where every flagged row is pinned (the operator on the free DOFs is a
+      // principal submatrix of the circulant one)
+      if (xh && v[2 * NS] == 0.0 && a.df_err > 0.0) st[j].dfe = a.df_err * sqrt(v[j]);
       am |= st[j].active << j;
       if (blockIdx.x == 0) a.info->bnorm[j] = sqrt(v[j]);
     }
     s_mask[0] = am;
     s_mask[1] = 0;
     s_mask[2] = CPM_OK;
+    s_mask[3] = 0;
   }
   __syncthreads();
-  int activem = s_mask[0], needm = 0;
+  int activem = s_mask[0], needm = 0, dfpass = 0;
   if (use_init) {
     for (int64_t dof = d0 + threadIdx.x; dof < d1; dof += TH)
 #pragma unroll
@@ -327,7 +341,39 @@ __global__ void __launch_bounds__(kIRThreads, 4) cg_stencil_ir_kernel(const __gr
       pt[NS + j] = 0.0;
       pt[2 * NS + j] = 0.0;
     }
-    if (needm) {
+    if (needm && dfpass) {
+      if constexpr (NC == 1) {
+        // double-float residual: x from its split form, the coefficients as hi + lo floats; one
+        // right-hand side per pass (four outputs and six values per column in registers)
+        const int step = quads ? 4 : 1;
+        for (int64_t dof = d0 + step * threadIdx.x; dof < d1; dof += step * TH) {
+#pragma unroll 1
+          for (int s = 0; s < NR; ++s) {
+            if (!((needm >> s) & 1)) continue;
+            df::DF yt[4][1];
+            if constexpr (NR == 1) {
+              const XSplit xs{xh, xl};
+              if (quads) apply4_c<df::DF, 1, 1, true, true>(a.S, a.cdf, xs, (int)dof, yt);
+              else apply_c<df::DF, 1, 1>(a.S, a.cdf, xs, (int)dof, yt[0]);
+            } else {
+              const XSplitR xs{xh, xl, NR, s};
+              if (quads) apply4_c<df::DF, 1, 1, true, true>(a.S, a.cdf, xs, (int)dof, yt);
+              else apply_c<df::DF, 1, 1>(a.S, a.cdf, xs, (int)dof, yt[0]);
+            }
+#pragma unroll
+            for (int kk = 0; kk < 4; ++kk) {
+              if (kk > 0 && !quads) break;
+              const int64_t i = uidx<NC, NR>(n, dof + kk, s);
+              const double t =
+                  is_pinned(a.S, dof + kk) ? 0.0 : (b[i] - (double)yt[kk][0].hi) - (double)yt[kk][0].lo;
+              r32[i] = (float)t;
+              pt[NS + s] = fma(t, t, pt[NS + s]);
+              pt[2 * NS + s] = fma(t, (double)p32[i], pt[2 * NS + s]);
+            }
+          }
+        }
+      }
+    } else if (needm) {
       // d was folded into x by the previous direction phase; pinned rows keep t = 0
       if (quads) {
         for (int64_t qd = d0 + 4 * threadIdx.x; qd < d1; qd += 4 * TH) {
@@ -375,11 +421,12 @@ __global__ void __launch_bounds__(kIRThreads, 4) cg_stencil_ir_kernel(const __gr
       int am = 0, bad = 0;
       for (int j = 0; j < NS; ++j) {
         double al;
-        bad |= ir_after_pq(st[j], pt[j], pt[NS + j], pt[2 * NS + j], a.maxiter, al);
+        bad |= ir_after_pq(st[j], pt[j], pt[NS + j], pt[2 * NS + j], a.maxiter, al, dfpass != 0);
         s_ab[j] = (float)al;
         am |= st[j].active << j;
       }
       if (needm) st[0].updates += 1;
+      if (needm && dfpass) st[0].dfupd += 1;
       s_mask[0] = am;
       s_mask[2] = bad ? CPM_NONFINITE : CPM_OK;
     }
@@ -415,19 +462,23 @@ __global__ void __launch_bounds__(kIRThreads, 4) cg_stencil_ir_kernel(const __gr
     for (int j = 0; j < NS; ++j) rr[j] = (double)rrf[j];
     if (!grid_sum<NS>(rr, a.part, par, a.bar, tns, s_red)) { status = CPM_BARRIER_TIMEOUT; break; }
     if (threadIdx.x == 0) {
-      int nm = 0, bad = 0;
+      int nm = 0, bad = 0, dfall = 1;
       for (int j = 0; j < NS; ++j) {
         float be;
         bad |= ir_after_rr(st[j], rr[j], a.inner_tol, a.maxiter, be);
         s_ab[j] = be;
         nm |= st[j].need << j;
+        if (st[j].need && !st[j].dfok) dfall = 0;
       }
       s_mask[1] = nm;
       s_mask[2] = bad ? CPM_NONFINITE : CPM_OK;
+      // one pass serves every pending system: double-float only when all of them allow it
+      s_mask[3] = (nm && dfall) ? 1 : 0;
     }
     __syncthreads();
     if (s_mask[2] != CPM_OK) { status = s_mask[2]; break; }
     needm = s_mask[1];
+    dfpass = s_mask[3];
     if (!activem) break;
     float beta[NS];
 #pragma unroll
@@ -435,7 +486,7 @@ __global__ void __launch_bounds__(kIRThreads, 4) cg_stencil_ir_kernel(const __gr
     // ---- phase 3: p = r32 + beta p; pending updates: x += d, d = 0
     if (quads) {
       for (int64_t qd = d0 + 4 * threadIdx.x; qd < d1; qd += 4 * TH)
-        quad_direction<NC, NR, NS>(n, qd, activem, needm, beta, p32, r32, x, d32);
+        quad_direction<NC, NR, NS>(n, qd, activem, needm, beta, p32, r32, x, d32, xh, xl);
     } else {
       for (int64_t dof = d0 + threadIdx.x; dof < d1; dof += TH) {
 #pragma unroll
@@ -444,8 +495,10 @@ __global__ void __launch_bounds__(kIRThreads, 4) cg_stencil_ir_kernel(const __gr
           const int64_t i = uidx<NC, NR>(n, dof, u);
           if ((activem >> s) & 1) p32[i] = fmaf(beta[s], p32[i], r32[i]);
           if ((needm >> s) & 1) {
-            x[i] += (double)d32[i];
+            const double xn = x[i] + (double)d32[i];
+            x[i] = xn;
             d32[i] = 0.0f;
+            if (xh) split_store(xn, xh, xl, i);
           }
         }
       }
@@ -465,6 +518,7 @@ __global__ void __launch_bounds__(kIRThreads, 4) cg_stencil_ir_kernel(const __gr
       a.info->resid[j] = st[j].resid;
     }
     a.info->outer = st[0].updates;
+    a.info->df_updates = st[0].dfupd;
     set_status(a.info, stt);
   } else if (status != CPM_OK && threadIdx.x == 0) {
     set_status(a.info, status);
@@ -797,9 +851,53 @@ static int check_stencil(const cpm_stencil *s, const char *who) {
   return CPM_OK;
 }
 
+// Error bound of the double-float residual t = b - A x of a scalar stencil, as a multiple of ||b||
+// (-1: none).  Each row's double-float sum of 27 terms is within 94 * 2^-48 of the sum of their
+// magnitudes (csrc/stencil_ops.cuh, df::fma), and the final FP64 subtractions add less than 2^-50, so
+// |t_df - t| <= g |A| |x| elementwise with g = 128 * 2^-48, and ||t_df - t|| <= g sum|c| ||x||.  On the
+// free DOFs (every flagged row pinned, checked on the device) A is a principal submatrix of the
+// circulant operator, so its eigenvalues are at least the minimum of the symbol
+// sigma(theta) = sum_d c_d cos(theta . d), and ||x|| <= (||b|| + ||t||) / sigma_min.  The part of c that
+// is even along every axis has a symbol multilinear in (cos theta_x, cos theta_y, cos theta_z), whose
+// minimum is at one of the 8 corners cos = +-1; the rest of c moves sigma by at most the sum of its
+// magnitudes.  With e = g sum|c| / sigma_min, a residual with ||t_df|| <= tol ||b|| - 2 e ||b|| has
+// ||t|| <= (tol ||b|| - e ||b||) / (1 - e) <= tol ||b||: the bound returned is 2 e.
+static double df_error_bound(const cpm_stencil *s) {
+  if (s->ncomp != 1) return -1.0;
+  const double *c = s->coef;
+  double even[27], s1 = 0.0, odd = 0.0;
+  for (int d = 0; d < 27; ++d) {
+    const int ia = d / 9, ib = (d / 3) % 3, ic = d % 3;
+    double acc = 0.0;
+    for (int m = 0; m < 8; ++m) {
+      const int ja = (m & 1) ? 2 - ia : ia, jb = (m & 2) ? 2 - ib : ib, jc = (m & 4) ? 2 - ic : ic;
+      acc += c[(ja * 3 + jb) * 3 + jc];
+    }
+    even[d] = acc / 8.0;
+    s1 += std::fabs(c[d]);
+    odd += std::fabs(c[d] - even[d]);
+  }
+  double smin = INFINITY;
+  for (int m = 0; m < 8; ++m) {
+    const double u[3] = {(m & 1) ? -1.0 : 1.0, (m & 2) ? -1.0 : 1.0, (m & 4) ? -1.0 : 1.0};
+    double sig = 0.0;
+    for (int d = 0; d < 27; ++d) {
+      const int o[3] = {d / 9 - 1, (d / 3) % 3 - 1, d % 3 - 1};
+      double w = even[d];
+      for (int ax = 0; ax < 3; ++ax) w *= o[ax] ? u[ax] : 1.0;
+      sig += w;
+    }
+    smin = std::min(smin, sig);
+  }
+  smin -= odd;
+  if (!(smin > 0.0) || !(s1 > 0.0)) return -1.0;
+  const double g = 128.0 * std::ldexp(1.0, -48);
+  return 2.0 * g * s1 / smin;
+}
+
 template <int NC, int NR>
 static int launch_stencil_cg(const cpm_stencil *s, const double *b, double *x, const cpm_cg_opts *o, Workspace &w,
-                             cpm_cg_info *info, cudaStream_t st) {
+                             float *xlo, cpm_cg_info *info, cudaStream_t st) {
   StencilCG a{};
   a.S = to_op(s);
   a.b = b;
@@ -826,6 +924,22 @@ static int launch_stencil_cg(const cpm_stencil *s, const double *b, double *x, c
   const bool fp64 = o->precision == 0;
   // FP32 form: three grid barriers per iteration unless the caller asks for the two-barrier form
   const bool two = !fp64 && o->form == CPM_CG_FORM_TWO_BARRIER;
+  // double-float residual passes: scalar operators in the three-barrier form, with room for the split
+  // x (the free pb32 vector and xlo) and an error bound at most a quarter of the tolerance, so that
+  // most convergence decisions can be taken on them
+  a.df_err = -1.0;
+  if (!fp64 && !two && NC == 1 && xlo) {
+    const double e = df_error_bound(s);
+    if (e > 0.0 && e <= 0.25 * o->tol) {
+      a.df_err = e;
+      a.xh = w.pb32;
+      a.xl = xlo;
+      for (int d = 0; d < 27; ++d) {
+        const float h = (float)s->coef[d];
+        a.cdf[d] = df::DF(h, (float)(s->coef[d] - (double)h));
+      }
+    }
+  }
   const void *fn = fp64 ? (const void *)cg_stencil_fp64_kernel<NC, NR>
                         : two ? (const void *)cg_stencil_ir2_kernel<NC, NR> : (const void *)cg_stencil_ir_kernel<NC, NR>;
   const int threads = fp64 ? kCGThreads : kIRThreads;
@@ -886,10 +1000,20 @@ extern "C" int cpm_cg_solve_stencil(const cpm_stencil *S, const double *b, doubl
   }
   Workspace w;
   layout(unknowns, nrhs, prec, (char *)workspace, &w);
+  // the low half of the split x, where the caller sized the workspace for it
+  float *xlo = nullptr;
+  if (prec && workspace_bytes >= cpm_cg_stencil_workspace_bytes(unknowns, nrhs, prec))
+    xlo = (float *)((char *)workspace + need);
   cudaStream_t st = (cudaStream_t)stream;
-  if (S->ncomp == 3) return launch_stencil_cg<3, 1>(S, b, x, opts, w, info_dev, st);
-  return nrhs == 1 ? launch_stencil_cg<1, 1>(S, b, x, opts, w, info_dev, st)
-                   : launch_stencil_cg<1, 3>(S, b, x, opts, w, info_dev, st);
+  if (S->ncomp == 3) return launch_stencil_cg<3, 1>(S, b, x, opts, w, xlo, info_dev, st);
+  return nrhs == 1 ? launch_stencil_cg<1, 1>(S, b, x, opts, w, xlo, info_dev, st)
+                   : launch_stencil_cg<1, 3>(S, b, x, opts, w, xlo, info_dev, st);
+}
+
+extern "C" size_t cpm_cg_stencil_workspace_bytes(int64_t unknowns, int nrhs, int precision) {
+  using namespace cpm;
+  const size_t base = layout(unknowns, nrhs, precision ? 1 : 0, nullptr, nullptr);
+  return precision ? base + align256(sizeof(float) * (size_t)unknowns * nrhs) : base;
 }
 
 extern "C" int cpm_stencil_apply(const cpm_stencil *S, const double *x, double *y, double alpha, int nvec,

@@ -46,6 +46,77 @@ __device__ __forceinline__ Nbr neighbours(const Geo &S, int dof) {
   return b;
 }
 
+// ---------------------------------------------------------------- double-float operands
+// A double-float value: the unevaluated sum hi + lo of two floats, about 48 significant bits (Dekker
+// 1971).  The residual passes of the FP32 refinement CG use it where its error bound allows
+// (csrc/stencil.cu): GB300 issues FP32 instructions at about 64 times its FP64 rate.
+namespace df {
+struct DF {
+  float hi, lo;
+  __device__ __forceinline__ DF(float h = 0.0f, float l = 0.0f) : hi(h), lo(l) {}
+};
+// acc + w x, renormalised (|lo| at most half an ulp of hi).  The product's high part w.hi x.hi splits
+// exactly into p + e by an FMA; the cross terms w.hi x.lo and w.lo x.hi join e in FP32 (w.lo x.lo, below
+// 2^-48 of the product, is dropped); acc.hi + p is added exactly by Knuth's TwoSum, the low parts in
+// FP32, and Fast2Sum renormalises.  Per term the error is at most 2^-48 (13 |w x| + 3 S) with S a bound
+// of |acc| and of the sum, so a sum of 27 terms is within 94 * 2^-48 of sum |terms|.  The _rn
+// intrinsics keep the compiler from contracting the TwoSum's additions with the product.
+__device__ __forceinline__ DF fma(const DF &w, const DF &x, const DF &acc) {
+  const float p = __fmul_rn(w.hi, x.hi);
+  float e = fmaf(w.hi, x.hi, -p);
+  e = fmaf(w.hi, x.lo, e);
+  e = fmaf(w.lo, x.hi, e);
+  const float s = __fadd_rn(acc.hi, p);
+  const float bv = __fsub_rn(s, acc.hi);
+  const float err = __fadd_rn(__fsub_rn(acc.hi, __fsub_rn(s, bv)), __fsub_rn(p, bv));
+  const float l = __fadd_rn(acc.lo, __fadd_rn(err, e));
+  const float h = __fadd_rn(s, l);
+  return DF(h, __fsub_rn(l, __fsub_rn(h, s)));
+}
+}  // namespace df
+
+// An FP64 vector held as two float vectors hi + lo (hi = x rounded to float, lo = x - hi rounded).
+struct XSplit {
+  const float *hi, *lo;
+};
+template <typename T>
+__device__ __forceinline__ T ld(const XSplit &s, int64_t i, int) { return T(s.hi[i], s.lo[i]); }
+template <typename T, bool VEC>
+__device__ __forceinline__ void ldq(const XSplit &s, int64_t i, int c, T *v) {
+  if (VEC) {
+    float h[4], l[4];
+    Vec4<float>::load(s.hi + i, h);
+    Vec4<float>::load(s.lo + i, l);
+#pragma unroll
+    for (int e = 0; e < 4; ++e) v[e] = T(h[e], l[e]);
+  } else {
+#pragma unroll
+    for (int e = 0; e < 4; ++e) v[e] = ld<T>(s, i + e, c);
+  }
+}
+// Right-hand side r of an interleaved split vector of nr right-hand sides (element i at i * nr + r),
+// read one value at a time: the double-float residual of nr > 1 vectors takes one vector per pass.
+struct XSplitR {
+  const float *hi, *lo;
+  int nr, r;
+};
+template <typename T>
+__device__ __forceinline__ T ld(const XSplitR &s, int64_t i, int) {
+  const int64_t k = i * s.nr + s.r;
+  return T(s.hi[k], s.lo[k]);
+}
+template <typename T, bool VEC>
+__device__ __forceinline__ void ldq(const XSplitR &s, int64_t i, int c, T *v) {
+#pragma unroll
+  for (int e = 0; e < 4; ++e) v[e] = ld<T>(s, i + e, c);
+}
+// x into its split form at element i.
+__device__ __forceinline__ void split_store(double v, float *hi, float *lo, int64_t i) {
+  const float h = __double2float_rn(v);
+  hi[i] = h;
+  lo[i] = __double2float_rn(v - (double)h);
+}
+
 template <typename T>
 __device__ __forceinline__ const T *coefs(const StencilOp &S);
 template <>
@@ -423,11 +494,11 @@ __device__ __forceinline__ void quad_update(int64_t n, int64_t d0, int activem, 
 
 // p = r + beta p for the active systems; for systems with a pending reliable
 // update also x += d, d = 0 (own unknowns only, so the next phase's true
-// residual is a plain FP64 product on x).
+// residual is a plain product on x), and the split form of x where xh is set.
 template <int NC, int NR, int NS>
 __device__ __forceinline__ void quad_direction(int64_t n, int64_t d0, int activem, int needm,
                                                const float (&beta)[NS], float *p32, const float *r32, double *x,
-                                               float *d32) {
+                                               float *d32, float *xh = nullptr, float *xl = nullptr) {
   constexpr int H = NC == 3 ? 3 : NR;
 #pragma unroll
   for (int h = 0; h < H; ++h) {
@@ -456,6 +527,16 @@ __device__ __forceinline__ void quad_direction(int64_t n, int64_t d0, int active
         }
       Vec4<double>::store(x + i0, xv);
       Vec4<float>::store(d32 + i0, dd);
+      if (xh) {
+        float h[4], l[4];
+#pragma unroll
+        for (int e = 0; e < 4; ++e) {
+          h[e] = __double2float_rn(xv[e]);
+          l[e] = __double2float_rn(xv[e] - (double)h[e]);
+        }
+        Vec4<float>::store(xh + i0, h);
+        Vec4<float>::store(xl + i0, l);
+      }
     }
   }
 }

@@ -34,12 +34,17 @@ class CGSolver:
         self.inner_tol = 0.1   # reliable-update factor of the mixed-precision solver
         self.max_outer = 60
         self.fft_layout = N.FFT_LAYOUT_AUTO  # spectrum layout of the FFT solves
+        # FP32 stencil solves: workspace for double-float residual passes where their error bound allows
+        # (False: every reliable update takes an FP64 residual)
+        self.df_residual = True
 
-    def workspace(self, n, nrhs, prec):
-        key = (n, nrhs, prec)
+    def workspace(self, n, nrhs, prec, stencil=False):
+        """Device workspace of a solve; stencil operators take the size that enables every form."""
+        key = (n, nrhs, prec, stencil)
         ws = self._ws.get(key)
         if ws is None:
-            nbytes = N.lib().cpm_cg_workspace_bytes(n, nrhs, prec)
+            query = N.lib().cpm_cg_stencil_workspace_bytes if stencil else N.lib().cpm_cg_workspace_bytes
+            nbytes = query(n, nrhs, prec)
             ws = torch.zeros(nbytes, dtype=torch.uint8, device=self.device)
             self._ws[key] = ws
         return ws
@@ -70,8 +75,8 @@ class CGSolver:
             raise ValueError(f"solve shapes: A {A.shape}, b {tuple(b.shape)}, x {tuple(x.shape)}")
         if not (b.is_contiguous() and x.is_contiguous()) or b.dtype != torch.float64 or x.dtype != torch.float64:
             raise TypeError("b and x must be contiguous float64 device tensors")
-        ws = self.workspace(n, nrhs, prec)
         stencil = hasattr(A, "ncomp")
+        ws = self.workspace(n, nrhs, prec, stencil=stencil and self.df_residual)
         o = N.CGOpts()
         o.tol = float(tol)
         o.maxiter = int(maxiter)
@@ -140,7 +145,7 @@ def decode_info(raw: np.ndarray) -> dict:
     b = np.ascontiguousarray(raw).tobytes()
     inf = N.CGInfo.from_buffer_copy(b)
     return {"status": int(inf.status), "iters": list(inf.iters), "outer": int(inf.outer),
-            "resid": list(inf.resid), "bnorm": list(inf.bnorm)}
+            "df_updates": int(inf.df_updates), "resid": list(inf.resid), "bnorm": list(inf.bnorm)}
 
 
 _default = None

@@ -51,7 +51,7 @@ typedef struct {
   int32_t status;          /* cpm_status of the solve */
   int32_t iters[3];        /* CG iterations per right-hand side */
   int32_t outer;           /* reliable updates (mixed precision) */
-  int32_t pad;
+  int32_t df_updates;      /* of those, updates on a double-float residual (cpm_cg_solve_stencil) */
   double resid[3];         /* final ||r|| per right-hand side */
   double bnorm[3];         /* ||b|| per right-hand side */
 } cpm_cg_info;
@@ -182,9 +182,19 @@ int cpm_stencil_apply(const cpm_stencil *S, const double *x, double *y, double a
 int cpm_stencil_apply32(const cpm_stencil *S, const float *x, float *y, int nvec, int form, void *stream);
 
 /* cpm_cg_solve on a stencil operator: same semantics, options and info;
- * workspace size cpm_cg_workspace_bytes(n * ncomp, nrhs, precision). */
+ * workspace size cpm_cg_workspace_bytes(n * ncomp, nrhs, precision) at least.
+ * With cpm_cg_stencil_workspace_bytes(n * ncomp, nrhs, precision) bytes (one
+ * more float vector in the FP32 form), the FP32 form of a scalar operator may
+ * compute its reliable updates' residuals in double-float arithmetic (x held
+ * as two floats, about 48 significant bits) where their error provably stays
+ * below a quarter of tol * ||b||: the stencil's symbol bounds the operator's
+ * smallest eigenvalue, and the solve checks that every flagged row is pinned
+ * (identity row, excluded column).  Such a residual decides convergence only
+ * when it is below tol * ||b|| by more than its error bound; closer to the
+ * threshold the solve takes FP64 residuals. */
 int cpm_cg_solve_stencil(const cpm_stencil *S, const double *b, double *x, int nrhs, const cpm_cg_opts *opts,
                          void *workspace, size_t workspace_bytes, cpm_cg_info *info_dev, void *stream);
+size_t cpm_cg_stencil_workspace_bytes(int64_t unknowns, int nrhs, int precision);
 
 /* ---- block-diagonal CG over many stencil systems (the serving loop) ----
  * Replaces, for a batch of independent runs, one solve_cg call per run

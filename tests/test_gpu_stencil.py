@@ -238,3 +238,56 @@ def test_matrix_free_derivatives_and_coupling_match_csr(dims, rot):
     close(E, strain_from_u(h, n, u, R), "strain")
     E0 = rng.normal(size=6 * n)
     close(F.spmv(dev(E0)).cpu().numpy(), h["F_el"] @ E0, "F_el E0")
+
+
+@pytest.mark.parametrize("dims", [(16, 16, 16), (15, 13, 11)])
+@pytest.mark.parametrize("nrhs", [1, 3])
+def test_double_float_residuals_keep_the_fp64_stopping_test(dims, nrhs):
+    """FP32 refinement CG whose reliable updates take double-float residuals (A1, A2: scalar, even
+    along every axis, symbol bounded away from zero, every flagged row pinned) against the same solves
+    with FP64 residuals only: both meet ||b - A x|| <= tol ||b|| on the host in FP64, cold and warm,
+    with the same iteration counts to within two, and the double-float solves report their
+    double-float updates.  The demag operator (symbol zero at the zero wave vector) takes none and
+    gives the same bits either way.  Grids with nz % 4 == 0 run the quad product, the others the
+    per-DOF one."""
+    from cupymag_gb300.solvers.linear_solvers import CGSolver, decode_info, new_info
+    S, p = _sim(Nx=dims[0], Ny=dims[1], Nz=dims[2], Ndx=5, Ndy=5, Ndz=5)
+    so = S.stencil_operators()
+    csr = S.host_operators()
+    rng = np.random.default_rng(21)
+    for name in ("A1", "A2", "A_demag"):
+        A, op = csr[name], so[name]
+        n = A.shape[0]
+        shape = (n, nrhs) if nrhs > 1 else (n,)
+        b = rng.normal(size=shape)
+        if name == "A_demag":
+            b.reshape(n, -1)[0] = 0.0
+        bd = torch.as_tensor(b, device="cuda").contiguous()
+        kick = torch.as_tensor(1e-4 * rng.standard_normal(shape), device="cuda")
+        res = {}
+        for df in (True, False):
+            solver = CGSolver()
+            solver.df_residual = df
+            x = torch.zeros_like(bd)
+            info = new_info(1)
+            runs = []
+            for warm in (False, True):
+                if warm:
+                    x += kick
+                    x.reshape(n, -1)[S.DefDOF] = 0.0
+                solver.launch(op, bd, x, info[0], tol=1e-10, maxiter=20000, precision="IR", use_init=warm)
+                inf = decode_info(info[0].cpu().numpy())
+                assert inf["status"] == 0, (name, df, warm, inf)
+                xs, bb = x.cpu().numpy().reshape(n, -1), b.reshape(n, -1)
+                for r in range(nrhs):
+                    assert np.linalg.norm(bb[:, r] - A @ xs[:, r]) <= 1e-10 * np.linalg.norm(bb[:, r]), \
+                        (name, df, warm, r)
+                runs.append((inf, xs.copy()))
+            res[df] = runs
+        for (idf, xdf), (i64, x64) in zip(res[True], res[False]):
+            assert all(abs(a - c) <= 2 for a, c in zip(idf["iters"][:nrhs], i64["iters"][:nrhs])), (name, idf, i64)
+            assert i64["df_updates"] == 0
+            if name == "A_demag":
+                assert idf["df_updates"] == 0 and np.array_equal(xdf, x64), name
+            else:
+                assert idf["df_updates"] >= 1, (name, idf)
