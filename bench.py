@@ -470,12 +470,14 @@ def run_ours(args):
         kk[0] += b
         kk[1] += d
         kk[2] += 1
-    its_step = []
+    its_step, upd_step, dfu_step = [], [], []
     for s in range(args.steps):
         infs = [decode_info(info_hist[s][k].cpu().numpy()) for k in range(6)]
         row = ([infs[0]["iters"][0]] if L.ME else []) + [infs[1]["iters"][0]] + infs[2]["iters"][:3] + \
               [infs[3]["iters"][0], infs[4]["iters"][0]] + infs[5]["iters"][:3]
         its_step.append(row)
+        upd_step.append([infs[k]["outer"] for k in range(6)])
+        dfu_step.append([infs[k]["df_updates"] for k in range(6)])
     its_mean = [float(np.mean([r[j] for r in its_step])) for j in range(len(its_step[0]))]
     peak, peak_kind = peaks()
     # the dominant kernel: the CG kernel with the most time in the timed steps
@@ -568,7 +570,11 @@ def run_ours(args):
             "run": {"timed_steps": f"{args.warmup}..{args.warmup + args.steps - 1}",
                     "resident_gb": round(resident_gb, 2), "csr_operator_gb": round(op_gb, 2),
                     "setup_s": round(t_setup, 1), "cg_iterations_per_step": [round(x, 1) for x in its_mean],
-                    "warm_started_steps": int(sum(int(w.item()) for w in warm_hist))},
+                    "warm_started_steps": int(sum(int(w.item()) for w in warm_hist)),
+                    # per solve slot (elasticity, demag, g1n/g2n/g3n, g1star, g2star, A2 x3): reliable
+                    # updates (FFT solves: refinement steps), and the updates taken on a double-float residual
+                    "updates_per_step": [round(float(np.mean([r[k] for r in upd_step])), 1) for k in range(6)],
+                    "df_updates_per_step": [round(float(np.mean([r[k] for r in dfu_step])), 1) for k in range(6)]},
             "e2e": {"value": round(e2e_value, 4), "unit": "steps/s",
                     "h2d_bytes_per_step": S.n_dof * 3 * 8, "d2h_bytes_per_step": S.n_dof * 3 * 8 + 24},
             "gpu_launches": launches,

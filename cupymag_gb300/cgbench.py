@@ -4,7 +4,7 @@
                                     [--precision IR|DP] [--operators stencil|csr]
                                     [--solves 3] [--maxiter 20000] [--batch 1] [--batched]
                                     [--form 0|1|2|3] [--precond fft] [--fft-layout auto|slab|passes]
-                                    [--spmv] [--precond-apply] [--workload tet96_me]
+                                    [--spmv] [--precond-apply] [--workload tet96_me] [--no-df]
 
 Builds only the requested operator (the magnetoelastic 128^3 material), a
 seeded right-hand side with the reference's pins (b[0] = 0 for A_demag,
@@ -104,6 +104,8 @@ def main(argv=None):
                     help="time z = M r alone (the FFT apply of a stencil operator), --solves times")
     ap.add_argument("--spmv", action="store_true",
                     help="time the CSR product y = A x alone (cpm_spmv_csr), --solves times; needs --operators csr")
+    ap.add_argument("--no-df", action="store_true",
+                    help="FP64 residuals for every reliable update (no double-float residual passes)")
     ap.add_argument("--precond", default=None, choices=["fft"],
                     help="FP32 stencil solve preconditioned by the circulant inverse (FFT) inside FP64 refinement")
     args = ap.parse_args(argv)
@@ -167,6 +169,7 @@ def main(argv=None):
         # directions to resolve); plain FP32 CG restarts after the --inner-tol drop
         inner_tol = 1e-4 if args.precond else args.inner_tol
         solver = CGSolver()
+        solver.df_residual = not args.no_df
         solver.inner_tol = args.inner_tol
         solver.fft_layout = {"auto": N.FFT_LAYOUT_AUTO, "slab": N.FFT_LAYOUT_SLAB,
                              "passes": N.FFT_LAYOUT_PASSES}[args.fft_layout]
@@ -198,7 +201,7 @@ def main(argv=None):
                       "operators": args.operators, "batch": args.batch,
                       "kernel": "blockdiag" if args.batch > 1 or args.batched else "single",
                       "status": N.STATUS_NAMES[d["status"]],
-                      "iters": its, "outer": d["outer"], "ms_per_solve": round(ms, 3),
+                      "iters": its, "outer": d["outer"], "df_updates": d["df_updates"], "ms_per_solve": round(ms, 3),
                       "us_per_iter": round(1e3 * ms / max(its, 1), 2), "GB/s": round(nb / (ms / 1e3) / 1e9, 1),
                       "solve_ms": [round(t, 3) for t in times]}))
 
