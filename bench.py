@@ -11,10 +11,12 @@ with all operators and state resident in HBM.
                   [--precision DP|IR] [--operators csr|stencil] [--impl ours|reference]
 
 value:  steps/s over K steps timed with CUDA events (device-resident inputs;
-        about 1.1 GB resident at 128^3 with every operator matrix-free, far
+        about 1.5 GB resident at 128^3 with every operator matrix-free, far
         above the L2, so no flush is needed); max over ranks.
-e2e:    the same steps through the public API with the magnetisation copied in
-        from pinned host memory and the new m and <m> read back every step.
+e2e:    the same K steps again, from a copy of the state they started from,
+        through the public API with the magnetisation copied in from pinned
+        host memory and the new m and <m> read back every step (wall clock);
+        bitwise_same_m_as_timed_steps records that they reproduce the timed m.
 fp64:   the same steps from the same m0 in plain FP64 on the same GPU, with
         max |m - m_FP64| and the relative <m> error.
 roofline: the CG launches (dominant kernel): algorithmic bytes per launch
@@ -411,6 +413,9 @@ def run_ours(args):
         e1.record(stream)
         cg_events.append((A, 3 if b.dim() == 2 else 1, k, e0, e1))
 
+    # the run's state before the timed steps: the end-to-end leg below repeats the same steps from it
+    snapshot = {k: t.clone() for k, t in L._state_tensors().items()}
+    nstep0 = L.nstep
     L._cg = timed_cg
     info_hist = []
     warm_hist = []
@@ -500,13 +505,16 @@ def run_ours(args):
                               "ms": round(v[1] / args.steps, 3), "iters": round(v[2] / args.steps, 1)}
                           for k, v in dom.items()}}
 
-    # e2e: public API with host buffers
+    # e2e: public API with host buffers, the timed steps again from the state they started from
+    for k, t in L._state_tensors().items():
+        t.copy_(snapshot[k])
+    L.nstep = nstep0
     host_m = torch.empty((S.n_dof, 3), dtype=torch.float64).pin_memory()
     host_m.copy_(L.m.cpu())
     host_avg = torch.empty(3, dtype=torch.float64).pin_memory()
     torch.cuda.synchronize()
     tw = time.perf_counter()
-    for s in range(args.warmup + args.steps, args.warmup + 2 * args.steps):
+    for s in range(args.warmup, args.warmup + args.steps):
         L.m.copy_(host_m, non_blocking=True)
         L.step(fields[s])
         host_m.copy_(L.m, non_blocking=True)
@@ -515,6 +523,7 @@ def run_ours(args):
     e2e_s = time.perf_counter() - tw
     L.check()
     e2e_value = replica_throughput(args.steps, e2e_s)
+    e2e_same = bool(torch.equal(L.m, m_timed))
 
     fp64 = None
     # plain FP64 CG iterations per solve of one step (the reference's unpreconditioned CG): the
@@ -575,7 +584,8 @@ def run_ours(args):
                     # updates (FFT solves: refinement steps), and the updates taken on a double-float residual
                     "updates_per_step": [round(float(np.mean([r[k] for r in upd_step])), 1) for k in range(6)],
                     "df_updates_per_step": [round(float(np.mean([r[k] for r in dfu_step])), 1) for k in range(6)]},
-            "e2e": {"value": round(e2e_value, 4), "unit": "steps/s",
+            "e2e": {"value": round(e2e_value, 4), "unit": "steps/s", "steps": f"{args.warmup}..{args.warmup + args.steps - 1}",
+                    "bitwise_same_m_as_timed_steps": e2e_same,
                     "h2d_bytes_per_step": S.n_dof * 3 * 8, "d2h_bytes_per_step": S.n_dof * 3 * 8 + 24},
             "gpu_launches": launches,
             "fp64": fp64,

@@ -88,6 +88,7 @@ _PROTOS = {
     "cpm_spmv_csr_multi": (C.c_int, [C.POINTER(CSR), vp, vp, vp, vp, dbl, C.c_int, vp, i64, vp]),
     "cpm_cg_workspace_bytes": (C.c_size_t, [i64, C.c_int, C.c_int]),
     "cpm_cg_stencil_workspace_bytes": (C.c_size_t, [i64, C.c_int, C.c_int]),
+    "cpm_stencil_df_error_bound": (C.c_double, [C.POINTER(Stencil)]),
     "cpm_cg_solve": (C.c_int, [C.POINTER(CSR), vp, vp, C.c_int, C.POINTER(CGOpts), vp, C.c_size_t, vp, vp]),
     "cpm_cg_solve_noalloc": (C.c_int, [C.POINTER(CSR), vp, vp, C.c_int, C.POINTER(CGOpts), vp, vp]),
     "cpm_stencil_apply": (C.c_int, [C.POINTER(Stencil), vp, vp, dbl, C.c_int, vp]),

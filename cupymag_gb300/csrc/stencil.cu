@@ -1010,6 +1010,11 @@ extern "C" int cpm_cg_solve_stencil(const cpm_stencil *S, const double *b, doubl
                    : launch_stencil_cg<1, 3>(S, b, x, opts, w, xlo, info_dev, st);
 }
 
+extern "C" double cpm_stencil_df_error_bound(const cpm_stencil *S) {
+  if (!S) return -1.0;
+  return cpm::df_error_bound(S);
+}
+
 extern "C" size_t cpm_cg_stencil_workspace_bytes(int64_t unknowns, int nrhs, int precision) {
   using namespace cpm;
   const size_t base = layout(unknowns, nrhs, precision ? 1 : 0, nullptr, nullptr);

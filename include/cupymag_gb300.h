@@ -195,6 +195,11 @@ int cpm_stencil_apply32(const cpm_stencil *S, const float *x, float *y, int nvec
 int cpm_cg_solve_stencil(const cpm_stencil *S, const double *b, double *x, int nrhs, const cpm_cg_opts *opts,
                          void *workspace, size_t workspace_bytes, cpm_cg_info *info_dev, void *stream);
 size_t cpm_cg_stencil_workspace_bytes(int64_t unknowns, int nrhs, int precision);
+/* The bound behind that choice, as a multiple of ||b||: 2 g sum|c| / sigma_min with g = 128 * 2^-48 and
+ * sigma_min a lower bound of the stencil's symbol (its part even along every axis is minimised over the 8
+ * corners cos theta = +-1, the rest bounded by the sum of its magnitudes); -1 where sigma_min <= 0 or the
+ * stencil is not scalar.  Host only (reads S->coef and S->ncomp). */
+double cpm_stencil_df_error_bound(const cpm_stencil *S);
 
 /* ---- block-diagonal CG over many stencil systems (the serving loop) ----
  * Replaces, for a batch of independent runs, one solve_cg call per run

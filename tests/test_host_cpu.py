@@ -225,6 +225,58 @@ def test_fp32_product_rejects_what_its_form_cannot_take():
     assert lib.cpm_stencil_apply32(None, fake, fake, 1, 0, None) == N.CPM_BAD_ARG
 
 
+def test_double_float_error_bound_uses_the_symbol_minimum():
+    """cpm_stencil_df_error_bound (host only): 2 g sum|c| / sigma_min with g = 128 * 2^-48, sigma_min
+    taken at the 8 corners of the torus for stencils even along every axis.  Checked against the symbol's
+    minimum on a fine grid of wave vectors for the Gauss-Seidel operators A1 and A2 (Q = sum|c| / sigma_min
+    near 10.5 and 23.3) and the mass matrix (Q = 27); none for the demag operator (sigma(0) = 0) or an
+    elastic stencil; a stencil that is not even along an axis gets a larger bound, never a smaller one."""
+    import itertools
+    from cupymag_gb300 import _native as N
+    from cupymag_gb300.build import build
+    from cupymag_gb300.core.assemble_simulation_operators import SimulationOperators
+    from cupymag_gb300.physics import structured_hex as SH
+    build()
+    lib = N.load()
+    g = 128.0 * 2.0 ** -48
+    p = G.params(G.load("hex_me_rot")).with_(Nx=8, Ny=8, Nz=8, Ndx=2, Ndy=2, Ndz=2)
+    S = SimulationOperators(p, device="cpu")
+    e = S._cell()
+    th = np.linspace(0.0, 2 * np.pi, 41)
+
+    def symbol_min(c):
+        c = c.reshape(3, 3, 3)
+        cx, cy, cz = (np.cos(np.multiply.outer(th, [-1.0, 0.0, 1.0])) for _ in range(3))
+        sig = np.einsum("abc,ia,jb,kc->ijk", c, cx, cy, cz)  # even stencils: a product of cosines
+        return sig.min()
+
+    def bound(c, ncomp=1):
+        s = N.Stencil()
+        s.nx = s.ny = s.nz = 8
+        s.ncomp = ncomp
+        s.coef[:c.size] = tuple(float(v) for v in c)
+        s.flags = None
+        return lib.cpm_stencil_df_error_bound(s)
+
+    for name, K, q in (("A1", e["K"] * S.alpha1 + e["M"], 10.5), ("A2", e["K"] * S.alpha2 + e["M"], 23.3),
+                       ("M", e["M"], 27.0)):
+        c = SH.stencil_from_element(K).reshape(-1)
+        corners = min(np.einsum("abc,a,b,c->", c.reshape(3, 3, 3), *[np.array([u, 1.0, u]) for u in us])
+                      for us in itertools.product((1.0, -1.0), repeat=3))
+        assert abs(corners - symbol_min(c)) <= 1e-12 * np.abs(c).sum(), name
+        got = bound(c)
+        assert got == pytest.approx(2 * g * np.abs(c).sum() / corners, rel=1e-12), name
+        assert abs(np.abs(c).sum() / corners - q) < 0.1, name
+        assert got <= 0.25 * 1e-10, name
+        # an odd part along x: the bound grows by the odd part's magnitude in the denominator
+        odd = c.reshape(3, 3, 3).copy()
+        odd[0] += 1e-3 * np.abs(c).max()
+        assert bound(odd.reshape(-1)) > got, name
+    assert bound(SH.stencil_from_element(e["K"]).reshape(-1)) == -1.0
+    assert bound(SH.stencil_from_element(e["Kel"], 3, 3).reshape(-1), ncomp=3) == -1.0
+    assert lib.cpm_stencil_df_error_bound(None) == -1.0
+
+
 # ------------------------------------------------------------------ serving (host side)
 def test_serving_workload_shape():
     from cupymag_gb300.serving.workload import serving_requests
