@@ -43,8 +43,8 @@ from ..utils.sigma_matrices import get_Ebar_sigma
 SOLVE_NAMES = ["elasticity", "demag", "Gauss-Seidel g1n/g2n/g3n", "Gauss-Seidel g1star", "Gauss-Seidel g2star",
                "Gauss-Seidel m1starstar/m2starstar/m3starstar"]
 
-# Reliable-update factor of the FP32 solver per solve (an FP64 true residual whenever the FP32
-# residual has fallen by this factor).  Measured on GB300 at 64^3-128^3: the ill-conditioned
+# Reliable-update factor of the FP32 solver per solve (a true residual whenever the FP32 residual has
+# fallen by this factor: FP64, or double-float for A1/A2 where its proven error bound allows).  Measured on GB300 at 64^3-128^3: the ill-conditioned
 # elasticity solve converges in the fewest iterations with 0.1 (smaller factors add 25-40 %
 # iterations); the Gauss-Seidel solves (A1, A2; ~30-55 iterations) converge in the same
 # iterations down to 1e-5, so fewer FP64 products win: at 128^3 (cold, 1 and 3 right-hand sides)

@@ -62,7 +62,7 @@ typedef struct {
   int32_t maxiter;
   int32_t use_init_host;   /* x holds the initial guess (if use_init_dev is NULL) */
   const int32_t *use_init_dev; /* device flag read at launch time, or NULL */
-  int32_t precision;       /* 0 = FP64 CG, 1 = FP32 CG with FP64 reliable updates */
+  int32_t precision;       /* 0 = FP64 CG, 1 = FP32 CG with reliable updates on FP64 (or proven double-float) residuals */
   double inner_tol;        /* reliable update when the FP32 residual fell by this factor (default 0.1) */
   int32_t max_outer;       /* unused (kept for layout) */
   int32_t form;            /* FP32 stencil solvers: CPM_CG_FORM_DEFAULT (= three grid barriers per
