@@ -53,11 +53,14 @@ def estimate_bytes(p, precision="IR") -> int:
     """Device bytes one run holds.  Every operator of a served run is matrix-free (stencils of the
     solved operators, F1, Fx, Fy, Fz and F_el), so per DOF it is: 33 FP64 vectors of the step (51 with
     magnetoelastic coupling), the volume-average weights, five flag arrays and the defect mask, the
-    block-diagonal CG vectors of the largest solve (3n unknowns: five FP32 or three FP64 vectors), and
-    for runs that solve elasticity and demag with the FFT solver its workspace and plans."""
+    block-diagonal CG vectors of the largest solve (3n unknowns: five FP32 or three FP64 vectors), in the
+    precision form the residual carries of the demag and elastic solves (b and t of each), and for runs
+    that solve elasticity and demag with the FFT solver its workspace and plans."""
     n = int(p.Nx) * int(p.Ny) * int(p.Nz)
     per = (51 if p.ME else 33) * 8 + 8 + 6
     per += 3 * (20 if precision != "DP" else 24)
+    if precision != "DP":
+        per += 2 * 8 * (4 if p.ME else 1)
     if precision != "DP" and n >= FFT_MIN_DOFS:
         # FFT solves: workspace (five FP32 vectors and a complex field of 3n unknowns) and the plans'
         # inverse symbols (6 floats per DOF elastic, 1 demag)
