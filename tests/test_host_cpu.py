@@ -277,6 +277,63 @@ def test_double_float_error_bound_uses_the_symbol_minimum():
     assert lib.cpm_stencil_df_error_bound(None) == -1.0
 
 
+def _df_fma(w, x, acc):
+    """float32 emulation of the device's double-float acc + w x (csrc/stencil_ops.cuh, df::fma); each
+    operand is a (hi, lo) pair of float32 arrays.  A float32 product is exact in float64, so the FMAs are
+    the float64 expression rounded once to float32."""
+    f32, f64 = np.float32, np.float64
+    (wh, wl), (xh, xl), (ah, al) = w, x, acc
+    p = wh * xh
+    e = (wh.astype(f64) * xh - p).astype(f32)
+    e = (wh.astype(f64) * xl + e).astype(f32)
+    e = (wl.astype(f64) * xh + e).astype(f32)
+    s = ah + p
+    bv = s - ah
+    err = (ah - (s - bv)) + (p - bv)
+    low = al + (err + e)
+    h = s + low
+    return h, low - (h - s)
+
+
+def test_double_float_row_sum_stays_within_its_proven_bound():
+    """27-term rows of the Gauss-Seidel stencil in the double-float arithmetic of the residual passes
+    (emulated in float32): every row's sum is within 96 * 2^-48 of the sum of its terms' magnitudes of the
+    exact sum (94 for the arithmetic, 2 for splitting c and x into float pairs), on smooth, constant
+    (maximal cancellation) and random operands, far inside the g = 128 * 2^-48 that the bound uses."""
+    from fractions import Fraction
+    from cupymag_gb300.core.assemble_simulation_operators import SimulationOperators
+    from cupymag_gb300.physics import structured_hex as SH
+    p = G.params(G.load("hex_me_rot")).with_(Nx=8, Ny=8, Nz=8, Ndx=2, Ndy=2, Ndz=2)
+    S = SimulationOperators(p, device="cpu")
+    e = S._cell()
+    c = SH.stencil_from_element(e["K"] * S.alpha2 + e["M"]).reshape(-1)
+    rng = np.random.default_rng(5)
+    rows = 400
+    t = np.linspace(0, 1, 27)
+    xs = np.concatenate([1.0 + 1e-3 * np.sin(7 * t)[None, :] * rng.normal(size=(rows // 4, 1)),
+                         np.full((rows // 4, 27), 0.731),
+                         rng.normal(size=(rows // 2, 27)) * 10.0 ** rng.integers(-3, 3, size=(rows // 2, 1))])
+
+    def split(v):
+        hi = v.astype(np.float32)
+        return hi, (v - hi.astype(np.float64)).astype(np.float32)
+
+    ch, cl = split(np.broadcast_to(c, xs.shape))
+    xh, xl = split(xs)
+    acc = (np.zeros(rows, np.float32), np.zeros(rows, np.float32))
+    for d in range(27):
+        acc = _df_fma((ch[:, d], cl[:, d]), (xh[:, d], xl[:, d]), acc)
+    got = acc[0].astype(np.float64) + acc[1].astype(np.float64)
+    worst = 0.0
+    for r in range(rows):
+        exact = sum(Fraction(float(c[d])) * Fraction(float(xs[r, d])) for d in range(27))
+        mag = float(sum(abs(Fraction(float(c[d])) * Fraction(float(xs[r, d]))) for d in range(27)))
+        err = abs(float(Fraction(float(got[r])) - exact))
+        worst = max(worst, err / (mag * 2.0 ** -48))
+    assert worst <= 96.0, worst
+    print("largest row error in units of 2^-48 sum|terms|:", worst)
+
+
 # ------------------------------------------------------------------ serving (host side)
 def test_serving_workload_shape():
     from cupymag_gb300.serving.workload import serving_requests
