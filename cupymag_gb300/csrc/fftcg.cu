@@ -1,24 +1,32 @@
-// FP32 conjugate gradient preconditioned by the circulant inverse, inside FP64 refinement (sm_103a).
+// FFT solves of the elastic and demag operators inside FP64 refinement (sm_103a).
 //
 // On the periodic hex grid the elastic operator A_el and the demag operator
 // A_demag are block-circulant stencils except for the anchor at DOF 0, whose
 // rows and columns the reference replaces by the identity
 // (cupymag/physics/assemble_demag.py:307-341, assemble_elasticity.py:461-527).
 // The 3D DFT diagonalises the circulant part C: per wave vector k a 3x3 (or
-// 1x1) real symmetric symbol C^(k) = sum_d c_d cos(theta_k . d).  M = C'^-1,
-// with C' = C except C'^(0) = sigma I (sigma the operator's diagonal), is an
-// SPD preconditioner with M A = I + (rank <= 9), so preconditioned CG needs a
-// few tens of iterations where plain CG needs thousands (2700 for 128^3
-// elasticity).
+// 1x1) real symmetric symbol C^(k) = sum_d c_d cos(theta_k . d).
 //
-// The solve is the refinement form of the cupyx-semantics solve_cg
+// Both forms are the refinement form of the cupyx-semantics solve_cg
 // (cupymag/solvers/linear_solvers.py:59-74) with the same stopping test on the
-// FP64 residual: an outer loop computes t = b - A64 x in FP64, stops when
-// ||t|| <= tol ||b||, else runs FP32 preconditioned CG on A e = t from e = 0 until
-// its residual has dropped by inner_tol (default 1e-4) and adds e to x.  The
-// whole solve is one persistent cooperative launch; every grid barrier is
-// bounded (GridBarrier).  Per inner iteration: z = M r with r.z;
-// p = z + beta p; q = A32 p with p.q; d += alpha p, r -= alpha q with r.r.
+// FP64 residual: an outer loop computes t = b - A64 x in FP64 and stops when
+// ||t|| <= tol ||b||.  The whole solve is one persistent cooperative launch;
+// every grid barrier is bounded (GridBarrier).
+//  * Direct refinement (the default where the plan has an anchor): A e = t is
+//    solved exactly by one FFT apply of C's pseudo-inverse on t plus the
+//    anchor's column at its 26 neighbours (every component summed to zero),
+//    and a translation that sets the anchored values (anchor_rhs); x += e.
+//    FP32 gives about 5 digits per step: two steps per 128^3 solve.  A cold
+//    start's first residual is b itself (x = 0, no product); a warm start from
+//    the x of a valid residual carry takes (b - b_carry) + t_carry instead of a
+//    product (cpm_cg_opts.carry_*).
+//  * Preconditioned CG (CPM_CG_FORM_FFT_PCG, and plans without an anchor):
+//    M = C'^-1, with C' = C except C'^(0) = sigma I (sigma the operator's
+//    diagonal), is an SPD preconditioner with M A = I + (rank <= 9); FP32
+//    preconditioned CG on A e = t from e = 0 runs until its residual has
+//    dropped by inner_tol (default 1e-4), then x += e.  Per inner iteration:
+//    z = M r with r.z; p = z + beta p; q = A32 p with p.q; d += alpha p,
+//    r -= alpha q with r.r.
 //
 // z = M r has two layouts of the spectrum:
 //  * slab (the default where it fits in shared memory): r is real, so along z
