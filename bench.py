@@ -164,16 +164,17 @@ def spmv_bytes(A, nvec):
     return A.nnz * (8 + 4) + (A.shape[0] + 1) * ip + nvec * (A.shape[1] * 8 + A.shape[0] * 8)
 
 
-def stencil_launch_bytes(A, nvec, iters, outer, fp32):
+def stencil_launch_bytes(A, nvec, iters, outer, fp32, df=0):
     """Algorithmic bytes of a matrix-free CG launch: vector passes only (flags and coefficients are cached).
 
     FP64 CG: 88 B per unknown and iteration (q = A p: read p, write q; x, r update: read 4, write 2;
-    p update: read 2, write 1).  FP32 inner iterations: 44 B; each FP64 refinement sweep: 48 B
-    (residual: read x, b, write r, p, d in FP32; x += d).
+    p update: read 2, write 1).  FP32 inner iterations: 44 B; each refinement sweep: 48 B (residual: read
+    x, b, write r, p, d in FP32; x += d), and 8 B more for each of the df sweeps on a double-float residual
+    (the fold also writes x split into two floats, which that residual reads in place of x).
     """
     u = A.shape[0] * nvec
     if fp32:
-        return u * (44 * iters + 48 * max(outer, 1))
+        return u * (44 * iters + 48 * max(outer, 1) + 8 * df)
     return u * (88 * iters + 24)
 
 
@@ -460,7 +461,7 @@ def run_ours(args):
             kn, b = "cg_stencil_fft_kernel", fft_launch_bytes(A, its, inf["outer"], warm, k in L.carry)
         elif hasattr(A, "ncomp"):
             kn = "cg_stencil_ir_kernel" if fp32 else "cg_stencil_fp64_kernel"
-            b = stencil_launch_bytes(A, nv, its, inf["outer"], fp32)
+            b = stencil_launch_bytes(A, nv, its, inf["outer"], fp32, inf["df_updates"])
         else:
             kn, b = ("cg_ir_kernel" if fp32 else "cg_fp64_kernel"), cg_launch_bytes(A, nv, its, warm)
         d = e0.elapsed_time(e1)
