@@ -188,6 +188,37 @@ def test_library_exports_every_header_symbol():
     assert lib.cpm_cg_workspace_bytes(1000, 3, 1) > lib.cpm_cg_workspace_bytes(10, 1, 1)
 
 
+def test_ctypes_structs_match_the_header_layouts(tmp_path):
+    """Every ctypes mirror in _native has the size and field offsets of its C struct in
+    include/cupymag_gb300.h, as gcc lays them out (a drifted field would pass wrong values silently)."""
+    import ctypes
+    import shutil
+    import subprocess
+    from cupymag_gb300 import _native as N
+    if shutil.which("gcc") is None:
+        pytest.skip("gcc not available")
+    mirrors = {"cpm_csr": N.CSR, "cpm_cg_info": N.CGInfo, "cpm_cg_opts": N.CGOpts, "cpm_stencil": N.Stencil,
+               "cpm_batch_system": N.BatchSystem, "cpm_batch_plan": N.BatchPlan, "cpm_field_params": N.FieldParams,
+               "cpm_fft_precond": N.FftPrecondC, "cpm_deriv_stencil": N.DerivStencilC,
+               "cpm_fel_stencil": N.FelStencilC}
+    lines = ['#include <stdio.h>', '#include <stddef.h>', '#include "cupymag_gb300.h"', 'int main(void) {']
+    for cname, py in mirrors.items():
+        lines.append(f'  printf("{cname} size %zu\\n", sizeof({cname}));')
+        for fname, _ in py._fields_:
+            lines.append(f'  printf("{cname} {fname} %zu\\n", offsetof({cname}, {fname}));')
+    lines += ['  return 0;', '}']
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines) + "\n")
+    exe = tmp_path / "layout"
+    subprocess.run(["gcc", "-std=c99", "-I", os.path.join(ROOT, "include"), str(src), "-o", str(exe)], check=True)
+    out = subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout.split("\n")
+    got = {tuple(l.split()[:2]): int(l.split()[2]) for l in out if l.strip()}
+    for cname, py in mirrors.items():
+        assert got[(cname, "size")] == ctypes.sizeof(py), cname
+        for fname, _ in py._fields_:
+            assert got[(cname, fname)] == getattr(py, fname).offset, (cname, fname)
+
+
 def test_batch_work_bytes_follow_the_grid():
     """cpm_batch_work_bytes sizes a system's work vectors from its grid (host arithmetic, no GPU)."""
     from cupymag_gb300 import _native as N
